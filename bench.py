@@ -1,0 +1,371 @@
+"""Benchmark of the per-frame Tessendorf ocean update (one JSON line on rank 0).
+
+Workload (default): the plain drop-in tile at N=1024 -- L=2000 m, A=2, wind
+30 m/s at 30 deg, lambda=1.3, l=0.1, seeded uniform noise (seed 1) -- advanced
+frame by frame at dt = 1/60 s from t = 0.  A step is one frame: the row pass
+(evolution + choppy + horizontal FFT) and the column pass (vertical FFT +
+inversion + lambda + normal + Jacobian), both our kernels.  Between steps L2 is
+flushed (a 512 MiB buffer written, then a 512 MiB buffer read, which leaves L2
+holding clean lines of the flush buffer), so every frame starts from HBM as it
+would inside a renderer's frame.  Each frame is timed with CUDA events on the
+launching stream; `value` = frames / sum of frame times.
+
+e2e: the same frames through the C ABI (ocean_update) with every output map
+copied back to pinned host memory inside the timed region; the per-frame input
+is the time value (a by-value argument).
+
+--impl reference: the reference's algorithm (FP32 C++ port of the shader
+passes, oracle/ocean_oracle.c port_*) on the host cores, same config/metric.
+
+Multi-GPU (torchrun): tiles do not exchange data, so every rank advances its
+own tile (replicas, weak scaling); time = max over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "fft-ocean-waves_gb300")
+sys.path.insert(0, PKG)
+sys.path.insert(0, ROOT)
+
+METRIC = "ocean frames/s (N=1024, 3 fields + normal/J)"
+BYTES_PER_TEXEL = 92            # algorithmic bytes per texel per frame
+ROW_BYTES, COL_BYTES = 40, 52   # row pass: h0 16 + intermediate write 24; column: read 24 + outputs 28
+
+
+def c2_params(N):
+    import ocean_gb300 as og
+    import numpy as np
+    a = math.radians(30.0)
+    f = lambda v: float(np.float32(v))
+    return og.Params(N=N, L=2000.0, amplitude=2.0, wind_speed=30.0, wind_dir_x=f(math.cos(a)),
+                     wind_dir_y=f(math.sin(a)), choppiness=f(1.3), suppression=f(0.1), gravity=f(9.81))
+
+
+def peak_hbm():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            return float(json.load(fh)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def traffic_table():
+    """Per-launch DRAM bytes from the committed ncu summary, if present."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "traffic.json")) as fh:
+            return json.load(fh)
+    except Exception:
+        return {}
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled while the GPU is busy."""
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                                          "-lms", "50", "-i", str(self.index)], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        self.out = ""
+        if self.proc is not None:
+            time.sleep(0.1)
+            self.proc.terminate()
+            try:
+                self.out, _ = self.proc.communicate(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in (self.out or "").splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 8:
+                continue
+            try:
+                sm.append(float(f[0]))
+                mx.append(float(f[1]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[4:8]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_init():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        import torch
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    return world, rank, local
+
+
+def barrier_max(world, value):
+    if world == 1:
+        return value
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([value], dtype=torch.float64, device="cuda")
+    dist.barrier()
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def cpu_baseline(N, seconds, threads=None):
+    """FP32 port of the reference algorithm (oracle/) on the host cores, on a
+    time-bounded sample of consecutive frames; also the checker of the GPU
+    frame against the FP64 oracle."""
+    from oracle import oracle
+    import numpy as np
+    d = c2_params(N)
+    p = oracle.Params(N=N, L=d.L, amplitude=d.amplitude, wind_speed=d.wind_speed, wind_x=d.wind_dir_x,
+                      wind_y=d.wind_dir_y, choppiness=d.choppiness, suppression=d.suppression, gravity=d.gravity)
+    if threads:
+        oracle.set_threads(threads)
+    cores = oracle.max_threads()
+    nz = oracle.noise(1, N)
+    port = oracle.Port(p, nz)
+    port.frame(0.0)
+    frames, t0 = 0, time.perf_counter()
+    while True:
+        port.frame(frames / 60.0)
+        frames += 1
+        el = time.perf_counter() - t0
+        if el >= seconds and frames >= 3:
+            break
+    port.close()
+    return {"value": frames / el, "unit": "frames/s", "cores": cores, "kind": "port",
+            "sample": f"{frames} consecutive N={N} frames (dt=1/60 s) in {el:.1f} s, FP32 reference algorithm "
+                      f"(2*log2N radix-2 ping-pong passes per field), OpenMP {cores} threads"}
+
+
+def parity_check(N, gpu_frame, t):
+    from oracle import oracle
+    import numpy as np
+    d = c2_params(N)
+    p = oracle.Params(N=N, L=d.L, amplitude=d.amplitude, wind_speed=d.wind_speed, wind_x=d.wind_dir_x,
+                      wind_y=d.wind_dir_y, choppiness=d.choppiness, suppression=d.suppression, gravity=d.gravity)
+    h = oracle.h0(p, oracle.noise(1, N))
+    ref = oracle.update(p, h, t)
+    errs = {k: oracle.rel_l2(gpu_frame[k], ref[k]) for k in ("dx", "dy", "dz")}
+    errs["normal"] = oracle.rel_l2(gpu_frame["nj"][..., :3], ref["nj"][..., :3])
+    errs["J"] = oracle.rel_l2(gpu_frame["nj"][..., 3] - 1, ref["nj"][..., 3] - 1)
+    return {k: float(f"{v:.3g}") for k, v in errs.items()}
+
+
+def run_gpu(args, world, rank, local):
+    import numpy as np
+    import torch
+    import build as ocean_build
+    ocean_build.build()
+    import ocean_gb300 as og
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.Stream(device=dev)
+    N = args.size
+    p = c2_params(N)
+    oc = og.Ocean(p, seed=1 + rank)
+    dx, dy, dz = (torch.empty((N, N), dtype=torch.float32, device=dev) for _ in range(3))
+    nj = torch.empty((N, N, 4), dtype=torch.float32, device=dev)
+    fl_w = torch.empty(128 << 20, dtype=torch.float32, device=dev)   # 512 MiB
+    fl_r = torch.ones(128 << 20, dtype=torch.float32, device=dev)
+    fl_sink = torch.empty((), dtype=torch.float32, device=dev)
+
+    def flush():
+        fl_w.zero_()
+        torch.sum(fl_r, dtype=torch.float32, out=fl_sink)
+
+    launches = 0
+    with torch.cuda.stream(stream):
+        for i in range(args.warmup):
+            flush()
+            oc.update(i / 60.0, dx, dy, dz, nj, stream=stream)
+        torch.cuda.synchronize()
+        K = args.steps
+        ev = [[torch.cuda.Event(enable_timing=True) for _ in range(3)] for _ in range(K)]
+        with ClockSampler(local) as clk:
+            if world > 1:
+                torch.distributed.barrier()
+            torch.cuda.synchronize()
+            wall0 = time.perf_counter()
+            for i in range(K):
+                flush()
+                t = (args.warmup + i) / 60.0
+                ev[i][0].record(stream)
+                oc.update_rows(t, stream=stream)
+                ev[i][1].record(stream)
+                oc.update_columns(dx, dy, dz, nj, stream=stream)
+                ev[i][2].record(stream)
+                launches += 2
+            torch.cuda.synchronize()
+            wall = time.perf_counter() - wall0
+            if world > 1:
+                torch.distributed.barrier()
+            row_ms = [ev[i][0].elapsed_time(ev[i][1]) for i in range(K)]
+            col_ms = [ev[i][1].elapsed_time(ev[i][2]) for i in range(K)]
+            frame_ms = [ev[i][0].elapsed_time(ev[i][2]) for i in range(K)]
+            total_s = barrier_max(world, sum(frame_ms) / 1e3)
+
+            # e2e: C-ABI call + all outputs copied to pinned host memory, every frame.
+            hdx, hdy, hdz = (torch.empty((N, N), dtype=torch.float32, pin_memory=True) for _ in range(3))
+            hnj = torch.empty((N, N, 4), dtype=torch.float32, pin_memory=True)
+            E = max(20, K // 4)
+            for i in range(3):
+                oc.update(i / 60.0, dx, dy, dz, nj, stream=stream)
+                for hsrc, hdst in ((dx, hdx), (dy, hdy), (dz, hdz), (nj, hnj)):
+                    hdst.copy_(hsrc, non_blocking=True)
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            ee = []
+            for i in range(E):
+                flush()
+                a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                a.record(stream)
+                oc.update(i / 60.0, dx, dy, dz, nj, stream=stream)
+                for hsrc, hdst in ((dx, hdx), (dy, hdy), (dz, hdz), (nj, hnj)):
+                    hdst.copy_(hsrc, non_blocking=True)
+                b.record(stream)
+                ee.append((a, b))
+            torch.cuda.synchronize()
+            e2e_s = barrier_max(world, sum(a.elapsed_time(b) for a, b in ee) / 1e3)
+        clocks = clk.summary()
+        # one frame at a known time for the parity check
+        t_chk = 1000 / 60.0
+        oc.update(t_chk, dx, dy, dz, nj, stream=stream)
+        torch.cuda.synchronize()
+        frame = {"dx": dx.cpu().numpy(), "dy": dy.cpu().numpy(), "dz": dz.cpu().numpy(), "nj": nj.cpu().numpy()}
+    oc.close()
+
+    if rank != 0:
+        return None
+    value = world * K / total_s
+    ms = 1e3 * total_s / K
+    row_avg = sum(row_ms) / K
+    col_avg = sum(col_ms) / K
+    dominant = "k_col_pass" if col_avg >= row_avg else "k_row_pass"
+    dom_ms = max(col_avg, row_avg)
+    dom_bytes = (COL_BYTES if dominant == "k_col_pass" else ROW_BYTES) * N * N
+    peak, peak_kind = peak_hbm()
+    achieved = dom_bytes / (dom_ms * 1e-3) / 1e9
+    traffic = traffic_table().get(f"{dominant}@{N}")
+    frame_gbs = BYTES_PER_TEXEL * N * N / (ms * 1e-3) / 1e9
+    out = {
+        "metric": METRIC, "value": round(value, 1), "unit": "frames/s", "n_gpus": world, "steps": K,
+        "warmup": args.warmup, "ms_per_step": round(ms, 5), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded splitmix64 uniform noise, seed 1)",
+        "config": {"workload": f"plain tile N={N}, L=2000 m, A=2, V=30 m/s @30deg, lambda=1.3, l=0.1, "
+                               f"frames at dt=1/60 s", "N": N, "fields": 3,
+                   "l2": "flushed between frames (512 MiB write + 512 MiB read)", "parallelism": f"replicas x{world}"},
+        "kernel_ms": {"k_row_pass": round(row_avg, 5), "k_col_pass": round(col_avg, 5)},
+        "roofline": {"bound": "hbm", "kernel": dominant, "achieved": round(achieved, 1), "peak": peak,
+                     "unit": "GB/s", "frac": round(achieved / peak, 4), "peak_source": peak_kind,
+                     "algorithmic_bytes_per_launch": dom_bytes, "traffic": traffic},
+        "roofline_frame": {"bytes_per_frame": BYTES_PER_TEXEL * N * N, "achieved": round(frame_gbs, 1),
+                           "frac": round(frame_gbs / peak, 4)},
+        "e2e": {"value": round(world * E / e2e_s, 1), "unit": "frames/s", "h2d_bytes_per_step": 8,
+                "d2h_bytes_per_step": 28 * N * N,
+                "path": "ocean_update (C ABI) + D2H of dx, dy, dz, normal_j to pinned host buffers"},
+        "gpu_launches": launches,
+        "clocks": clocks,
+        "wall_s_timed_region": round(wall, 4),
+    }
+    if not args.no_cpu:
+        out["cpu_baseline"] = cpu_baseline(N, args.cpu_seconds)
+        out["err_vs_fp64"] = parity_check(N, frame, t_chk)
+    return out
+
+
+def run_reference(args, world, rank):
+    """The reference's algorithm on the host cores (FP32 port, OpenMP)."""
+    if rank != 0:
+        return None
+    from oracle import oracle
+    N = args.size
+    d = c2_params(N)
+    p = oracle.Params(N=N, L=d.L, amplitude=d.amplitude, wind_speed=d.wind_speed, wind_x=d.wind_dir_x,
+                      wind_y=d.wind_dir_y, choppiness=d.choppiness, suppression=d.suppression, gravity=d.gravity)
+    cores = oracle.max_threads()
+    port = oracle.Port(p, oracle.noise(1, N))
+    for i in range(args.warmup):
+        port.frame(i / 60.0)
+    ts = []
+    for i in range(args.steps):
+        t0 = time.perf_counter()
+        port.frame((args.warmup + i) / 60.0)
+        ts.append(time.perf_counter() - t0)
+    port.close()
+    total = sum(ts)
+    value = args.steps / total
+    return {
+        "metric": METRIC, "value": round(value, 3), "unit": "frames/s", "impl": "reference", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * total / args.steps, 3),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded splitmix64 uniform noise, seed 1)",
+        "config": {"workload": f"plain tile N={N}, L=2000 m, A=2, V=30 m/s @30deg, lambda=1.3, l=0.1, "
+                               f"frames at dt=1/60 s", "N": N, "fields": 3},
+        "cpu_baseline": {"value": round(value, 3), "unit": "frames/s", "cores": cores, "kind": "port",
+                         "sample": f"{args.steps} consecutive N={N} frames; FP32 port of the reference's GLSL passes "
+                                   f"(the GL path itself is unavailable on this box)"},
+        "e2e": {"value": round(value, 3), "unit": "frames/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=1000)
+    ap.add_argument("--warmup", type=int, default=10)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--size", type=int, default=1024)
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    world, rank, local = int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("RANK", "0")), \
+        int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        out = run_reference(args, world, rank)
+    else:
+        world, rank, local = dist_init()
+        out = run_gpu(args, world, rank, local)
+    if out is not None:
+        print(json.dumps(out), flush=True)
+    if world > 1 and args.impl != "reference":
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,191 @@
+// fft_line.cuh -- complex FP32 FFT building blocks for the ocean kernels.
+//
+// A "line" is one N-point transform (one row or one column of a spectrum).
+// It is computed by G = N/R1 cooperating threads, each holding R1 complex
+// values in registers, as a Stockham auto-sort FFT of 2 or 3 passes
+// (radices R1, R2[, R3]; every radix <= 32 and dividing R1):
+//
+//   pass 1 (radix R1, Ns = 1):   thread t owns inputs x[t + r*N/R1], r < R1,
+//                                so a line is loaded with unit stride across
+//                                threads (coalesced rows / bank-free columns).
+//   pass p (radix R, Ns = prod of earlier radices): butterfly j reads
+//                                x[j + r*N/R] from shared memory, multiplies
+//                                by W_{Ns*R}^{(j mod Ns)*r}, does an R-point
+//                                DFT in registers and writes outputs to
+//                                ((j/Ns)*Ns*R + j mod Ns) + r*Ns.
+//   after the last pass         butterfly j holds X[j + r*N/R_last], again
+//                                unit stride across threads (coalesced store).
+//
+// The unnormalised inverse transform (SIGN = +1, exponent +2*pi*i*n*k/N) is
+// what the reference's butterfly passes compute (butterfly_cs.glsl:54-132,
+// twiddles exp(+2*pi*i*k/N) twiddle_factors_cs.glsl:37-38).  SIGN = -1 gives
+// the forward transform used by the adjoint.
+//
+// Shared-memory exchange buffers are padded by one complex per R1 entries:
+// the pass-1 writes (stride R1 across threads) and the later unit-stride
+// reads are then free of bank conflicts for 8-byte accesses.
+#pragma once
+#include <cuda_runtime.h>
+
+namespace ocean {
+
+__device__ __forceinline__ float2 operator+(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ float2 operator-(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ float2 cmul(float2 a, float2 b)
+{
+    return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__device__ __forceinline__ float2 conjf2(float2 a) { return make_float2(a.x, -a.y); }
+
+// cos(2*pi*k/32) and sin(2*pi*k/32) for k < 16, rounded to float.
+__host__ __device__ constexpr float cos32(int k)
+{
+    switch (k) {
+    case 0: return 1.0f;
+    case 1: return 0.980785280403230449f;
+    case 2: return 0.923879532511286756f;
+    case 3: return 0.831469612302545237f;
+    case 4: return 0.707106781186547524f;
+    case 5: return 0.555570233019602225f;
+    case 6: return 0.382683432365089772f;
+    case 7: return 0.195090322016128268f;
+    case 8: return 0.0f;
+    default: return -cos32(16 - k);
+    }
+}
+__host__ __device__ constexpr float sin32(int k) { return k <= 8 ? cos32(8 - k) : cos32(k - 8); }
+
+// x * W_32^idx with W = exp(SIGN * 2*pi*i/32); idx is a compile-time constant
+// after unrolling, so the branches fold away.
+template <int SIGN>
+__device__ __forceinline__ float2 mul_w32(float2 x, int idx)
+{
+    if (idx == 0) return x;
+    if (idx == 8) return SIGN > 0 ? make_float2(-x.y, x.x) : make_float2(x.y, -x.x);
+    const float c = cos32(idx), s = SIGN > 0 ? sin32(idx) : -sin32(idx);
+    return make_float2(x.x * c - x.y * s, x.x * s + x.y * c);
+}
+
+__host__ __device__ constexpr int bitrev_n(int i, int n)
+{
+    int r = 0;
+    for (int b = 1; b < n; b <<= 1) {
+        r = (r << 1) | (i & 1);
+        i >>= 1;
+    }
+    return r;
+}
+
+// In-register R-point DFT (R = 1..32, power of two), natural order in and out.
+// Radix-2 decimation in time on bit-reversed input.
+template <int R, int SIGN>
+__device__ __forceinline__ void dft(float2* v)
+{
+#pragma unroll
+    for (int i = 0; i < R; ++i) {
+        const int j = bitrev_n(i, R);
+        if (j > i) {
+            float2 t = v[i];
+            v[i]     = v[j];
+            v[j]     = t;
+        }
+    }
+#pragma unroll
+    for (int h = 1; h < R; h <<= 1) {
+#pragma unroll
+        for (int k = 0; k < h; ++k) {
+            const int idx = k * (16 / h);  // W_{2h}^k == W_32^{16k/h}
+#pragma unroll
+            for (int i = k; i < R; i += 2 * h) {
+                float2 b = mul_w32<SIGN>(v[i + h], idx);
+                float2 a = v[i];
+                v[i]     = a + b;
+                v[i + h] = a - b;
+            }
+        }
+    }
+}
+
+template <int N_, int R1_, int R2_, int R3_ = 1>
+struct LineCfg {
+    static constexpr int N    = N_;
+    static constexpr int R1   = R1_;
+    static constexpr int R2   = R2_;
+    static constexpr int R3   = R3_;
+    static constexpr int G    = N / R1;      // threads per line
+    static constexpr int E    = R1;          // complex values per thread
+    static constexpr int NPAD = N + N / R1;  // padded exchange-buffer length
+    static_assert(R1 * R2 * R3 == N, "radices must multiply to N");
+    static_assert(R1 <= 32 && R2 <= R1 && R3 <= R1 && R1 % R2 == 0 && R1 % R3 == 0, "bad radices");
+    __device__ __forceinline__ static int pad(int i) { return i + i / R1; }
+};
+
+// Line-size -> decomposition used by every kernel.
+template <int N> struct LineFor;
+template <> struct LineFor<32>   { using type = LineCfg<32, 8, 4>; };
+template <> struct LineFor<64>   { using type = LineCfg<64, 8, 8>; };
+template <> struct LineFor<128>  { using type = LineCfg<128, 16, 8>; };
+template <> struct LineFor<256>  { using type = LineCfg<256, 16, 16>; };
+template <> struct LineFor<512>  { using type = LineCfg<512, 32, 16>; };
+template <> struct LineFor<1024> { using type = LineCfg<1024, 32, 32>; };
+template <> struct LineFor<2048> { using type = LineCfg<2048, 32, 8, 8>; };
+
+// One exchange + pass: the registers hold the outputs of a pass of radix RP
+// with stride NSP; they are written to `buf`, re-read as the inputs of a pass
+// of radix RN (stride NSP*RP), twiddled and transformed.  Contains two
+// __syncthreads(): every thread of the block must call it.
+template <class C, int RP, int NSP, int RN, int SIGN>
+__device__ __forceinline__ void stockham_pass(float2* v, float2* buf, const float2* tw, int t)
+{
+    constexpr int N   = C::N;
+    constexpr int NSN = NSP * RP;
+#pragma unroll
+    for (int b = 0; b < C::R1 / RP; ++b) {
+        const int j    = t + b * C::G;
+        const int idxD = (j / NSP) * NSP * RP + (j % NSP);
+#pragma unroll
+        for (int r = 0; r < RP; ++r) buf[C::pad(idxD + r * NSP)] = v[b * RP + r];
+    }
+    __syncthreads();
+#pragma unroll
+    for (int b = 0; b < C::R1 / RN; ++b) {
+        const int j = t + b * C::G;
+#pragma unroll
+        for (int r = 0; r < RN; ++r) v[b * RN + r] = buf[C::pad(j + r * (N / RN))];
+    }
+    __syncthreads();
+#pragma unroll
+    for (int b = 0; b < C::R1 / RN; ++b) {
+        const int j = t + b * C::G;
+        const int k = j % NSN;
+#pragma unroll
+        for (int r = 1; r < RN; ++r) {
+            float2 w = tw[(k * r * (N / (NSN * RN))) & (N - 1)];
+            if (SIGN < 0) w.y = -w.y;
+            v[b * RN + r] = cmul(v[b * RN + r], w);
+        }
+        dft<RN, SIGN>(v + b * RN);
+    }
+}
+
+// Full line transform.  On entry v[r] = x[t + r*N/R1]; on exit
+// v[b*RL + r] = X[(t + b*G) + r*(N/RL)] with RL the last radix.
+// tw: N-entry table tw[i] = exp(+2*pi*i*i/N) (conjugated here for SIGN < 0).
+template <class C, int SIGN>
+__device__ __forceinline__ void line_fft(float2* v, float2* buf, const float2* tw, int t)
+{
+    dft<C::R1, SIGN>(v);
+    stockham_pass<C, C::R1, 1, C::R2, SIGN>(v, buf, tw, t);
+    if constexpr (C::R3 > 1) stockham_pass<C, C::R2, C::R1, C::R3, SIGN>(v, buf, tw, t);
+}
+
+template <class C>
+struct LineOut {
+    static constexpr int RL = C::R3 > 1 ? C::R3 : C::R2;
+    static constexpr int B  = C::R1 / RL;          // butterflies per thread in the last pass
+    static constexpr int NS = C::N / RL;           // output stride of the last pass
+    // position of register e = b*RL + r after line_fft
+    __device__ __forceinline__ static int pos(int t, int e) { return (t + (e / RL) * C::G) + (e % RL) * NS; }
+};
+
+}  // namespace ocean

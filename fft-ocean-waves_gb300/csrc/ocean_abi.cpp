@@ -1,0 +1,382 @@
+// ocean_abi.cpp -- the Ocean handle and the extern "C" entry points of
+// include/ocean.h.  Host C++; all device work is in the .cu translation units.
+//
+// The handle replaces FFTOceanWaves' hot-path state (main.cpp:1589-1599,
+// 1640-1646): h0 (m_tilde_h0_k / m_tilde_h0_minus_k), the row-pass
+// intermediate (in place of m_tilde_h0_t_* and m_ping_pong), the twiddle
+// table (in place of m_twiddle_factors) and, optionally, headless output
+// buffers (m_dx, m_dy, m_dz, m_normal_map).
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/ocean.h"
+#include "ocean_internal.h"
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const std::string& msg)
+{
+    g_err = msg;
+    return code;
+}
+
+int cuda_fail(cudaError_t e, const char* what)
+{
+    return fail(OCEAN_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+bool is_pow2(int n) { return n > 0 && (n & (n - 1)) == 0; }
+
+int validate(const ocean_params* p)
+{
+    if (!p) return fail(OCEAN_ERR_INVALID, "params is NULL");
+    if (!is_pow2(p->N) || p->N < OCEAN_MIN_N || p->N > OCEAN_MAX_N)
+        return fail(OCEAN_ERR_INVALID, "N must be a power of two in [32, 2048], got " + std::to_string(p->N));
+    const float vals[] = {p->L, p->amplitude, p->wind_speed, p->wind_dir_x, p->wind_dir_y,
+                          p->choppiness, p->suppression, p->gravity};
+    for (float v : vals)
+        if (!std::isfinite(v)) return fail(OCEAN_ERR_INVALID, "non-finite ocean parameter");
+    if (!(p->L > 0.0f)) return fail(OCEAN_ERR_INVALID, "patch length L must be > 0");
+    if (p->amplitude < 0.0f) return fail(OCEAN_ERR_INVALID, "amplitude must be >= 0");
+    if (!(p->wind_speed > 0.0f)) return fail(OCEAN_ERR_INVALID, "wind speed must be > 0");
+    if (p->wind_dir_x == 0.0f && p->wind_dir_y == 0.0f) return fail(OCEAN_ERR_INVALID, "wind direction is zero");
+    if (p->flags & ~OCEAN_FLAG_LITERAL_CONJ) return fail(OCEAN_ERR_INVALID, "unknown flag bits");
+    return OCEAN_OK;
+}
+
+double gravity_of(const ocean_params& p) { return p.gravity > 0.0f ? (double)p.gravity : 9.81; }
+
+ocean::H0Args h0_args(const ocean_params& p)
+{
+    const double g  = gravity_of(p);
+    const double wn = std::sqrt((double)p.wind_dir_x * p.wind_dir_x + (double)p.wind_dir_y * p.wind_dir_y);
+    const double Lp = (double)p.wind_speed * p.wind_speed / g;   // tilde_h0_k_cs.glsl:78
+    ocean::H0Args a;
+    a.N             = p.N;
+    a.two_pi_over_L = (float)(2.0 * M_PI / p.L);
+    a.amplitude     = p.amplitude;
+    a.inv_Lp2       = (float)(1.0 / (Lp * Lp));
+    a.l2            = (float)((double)p.suppression * p.suppression);
+    a.wx            = (float)(p.wind_dir_x / wn);
+    a.wy            = (float)(p.wind_dir_y / wn);
+    return a;
+}
+
+}  // namespace
+
+// splitmix64 (Steele, Lea & Flood 2014): i-th draw uses state seed + (i+1)*gamma.
+static inline uint64_t splitmix64_at(uint64_t seed, uint64_t i)
+{
+    uint64_t z = seed + (i + 1) * 0x9E3779B97F4A7C15ull;
+    z          = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z          = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+struct ocean_s {
+    ocean_params p{};
+    int          N = 0;
+    float4*      h0     = nullptr;  // [N][N]
+    float2*      inter  = nullptr;  // [3][N/2+1][N]
+    float2*      tw     = nullptr;  // [N]
+    float*       noise  = nullptr;  // [4][N][N], kept for ocean_set_params
+    float*       out    = nullptr;  // handle-owned outputs: dx, dy, dz, normal_j
+    double       K      = 0.0;      // sqrt(g/(2*pi*L))
+    double       w_dc   = 0.0;      // sqrt(g*1e-5): the floored DC frequency
+
+    ~ocean_s()
+    {
+        cudaFree(h0);
+        cudaFree(inter);
+        cudaFree(tw);
+        cudaFree(noise);
+        cudaFree(out);
+    }
+
+    void set_consts()
+    {
+        const double g = gravity_of(p);
+        K    = std::sqrt(g / (2.0 * M_PI * (double)p.L));
+        w_dc = std::sqrt(g * 0.00001);  // tilde_h0_t_cs.glsl:76-79 at k = 0
+    }
+
+    ocean::FrameConsts frame(double t) const
+    {
+        ocean::FrameConsts fc;
+        const double kt = K * t;
+        fc.kt_hi        = (float)kt;
+        fc.kt_lo        = (float)(kt - (double)fc.kt_hi);
+        const double dc = w_dc * t / (2.0 * M_PI);
+        fc.dc_cycles    = (float)(dc - std::nearbyint(dc));
+        return fc;
+    }
+
+    int build_h0(cudaStream_t s)
+    {
+        cudaError_t e = ocean::launch_h0(h0_args(p), noise, h0, s);
+        if (e != cudaSuccess) return cuda_fail(e, "h0 init launch");
+        return OCEAN_OK;
+    }
+};
+
+extern "C" {
+
+const char* ocean_last_error(void) { return g_err.c_str(); }
+
+int ocean_version(void) { return 100; }
+
+int ocean_fill_noise(uint64_t seed, int32_t N, float* host_out)
+{
+    if (!host_out) return fail(OCEAN_ERR_INVALID, "host_out is NULL");
+    if (!is_pow2(N) || N > 65536) return fail(OCEAN_ERR_INVALID, "N must be a power of two");
+    const uint64_t n = 4ull * (uint64_t)N * (uint64_t)N;
+    for (uint64_t i = 0; i < n; ++i) {
+        const uint64_t z = splitmix64_at(seed, i);
+        host_out[i]      = (float)((double)((z >> 40) + 1) * (1.0 / 16777216.0));
+    }
+    return OCEAN_OK;
+}
+
+int ocean_bit_reversed_indices(int32_t N, int32_t* host_out)
+{
+    if (!host_out) return fail(OCEAN_ERR_INVALID, "host_out is NULL");
+    if (!is_pow2(N) || N < 2 || N > 65536) return fail(OCEAN_ERR_INVALID, "N must be a power of two in [2, 65536]");
+    int lg = 0;
+    while ((1 << lg) < N) ++lg;
+    for (int i = 0; i < N; ++i) {
+        int r = 0;
+        for (int b = 0; b < lg; ++b) r |= ((i >> b) & 1) << (lg - 1 - b);
+        host_out[i] = r;
+    }
+    return OCEAN_OK;
+}
+
+int ocean_butterfly_table(int32_t N, float* host_out)
+{
+    if (!host_out) return fail(OCEAN_ERR_INVALID, "host_out is NULL");
+    if (!is_pow2(N) || N < 2 || N > 65536) return fail(OCEAN_ERR_INVALID, "N must be a power of two in [2, 65536]");
+    int lg = 0;
+    while ((1 << lg) < N) ++lg;
+    std::vector<int32_t> br(N);
+    ocean_bit_reversed_indices(N, br.data());
+    for (int s = 0; s < lg; ++s)
+        for (int y = 0; y < N; ++y) {
+            const long   span = 1L << s;
+            const long   k    = ((long)y * (N >> (s + 1))) % N;   // twiddle_factors_cs.glsl:37
+            const bool   top  = (y % (2L << s)) < span;             // :44
+            float*       o    = host_out + 4 * ((size_t)s * N + y);
+            o[0] = (float)std::cos(2.0 * M_PI * (double)k / N);
+            o[1] = (float)std::sin(2.0 * M_PI * (double)k / N);
+            if (s == 0) {                                           // :50-58, bit-reversed pairs
+                o[2] = (float)(top ? br[y] : br[y - 1]);
+                o[3] = (float)(top ? br[y + 1] : br[y]);
+            } else {                                                // :60-68
+                o[2] = (float)(top ? y : y - span);
+                o[3] = (float)(top ? y + span : y);
+            }
+        }
+    return OCEAN_OK;
+}
+
+int ocean_compute_h0(const ocean_params* params, const float* noise_dev, float* h0_dev, void* stream)
+{
+    int rc = validate(params);
+    if (rc) return rc;
+    if (!noise_dev || !h0_dev) return fail(OCEAN_ERR_INVALID, "NULL device pointer");
+    if (reinterpret_cast<uintptr_t>(h0_dev) % 16) return fail(OCEAN_ERR_INVALID, "h0_dev must be 16-byte aligned");
+    cudaError_t e = ocean::launch_h0(h0_args(*params), noise_dev, reinterpret_cast<float4*>(h0_dev),
+                                     static_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess) return cuda_fail(e, "h0 init launch");
+    return OCEAN_OK;
+}
+
+int ocean_create(const ocean_params* params, const float* noise_host, ocean_t** out)
+{
+    if (!out) return fail(OCEAN_ERR_INVALID, "out is NULL");
+    *out = nullptr;
+    int rc = validate(params);
+    if (rc) return rc;
+    if (!noise_host) return fail(OCEAN_ERR_INVALID, "noise_host is NULL");
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
+    int major = 0, minor = 0;
+    cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev);
+    cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, dev);
+    if (major != 10 || minor != 3)
+        return fail(OCEAN_ERR_UNSUPPORTED, "kernels are built for sm_103a only; device is sm_" +
+                                               std::to_string(major) + std::to_string(minor));
+
+    ocean_s* o = new (std::nothrow) ocean_s();
+    if (!o) return fail(OCEAN_ERR_NOMEM, "host allocation failed");
+    o->p = *params;
+    o->N = params->N;
+    o->set_consts();
+    const size_t N = (size_t)o->N;
+    if ((e = cudaMalloc(&o->h0, N * N * sizeof(float4))) != cudaSuccess ||
+        (e = cudaMalloc(&o->inter, 3 * (N / 2 + 1) * N * sizeof(float2))) != cudaSuccess ||
+        (e = cudaMalloc(&o->tw, N * sizeof(float2))) != cudaSuccess ||
+        (e = cudaMalloc(&o->noise, 4 * N * N * sizeof(float))) != cudaSuccess) {
+        delete o;
+        return fail(OCEAN_ERR_NOMEM, std::string("device allocation failed: ") + cudaGetErrorString(e));
+    }
+    std::vector<float2> tw(N);
+    for (size_t k = 0; k < N; ++k) {
+        const double a = 2.0 * M_PI * (double)k / (double)N;
+        tw[k]          = make_float2((float)std::cos(a), (float)std::sin(a));
+    }
+    if ((e = cudaMemcpy(o->tw, tw.data(), N * sizeof(float2), cudaMemcpyHostToDevice)) != cudaSuccess ||
+        (e = cudaMemcpy(o->noise, noise_host, 4 * N * N * sizeof(float), cudaMemcpyHostToDevice)) != cudaSuccess) {
+        delete o;
+        return cuda_fail(e, "upload");
+    }
+    if ((rc = o->build_h0(0)) != OCEAN_OK) {
+        delete o;
+        return rc;
+    }
+    if ((e = cudaStreamSynchronize(0)) != cudaSuccess) {
+        delete o;
+        return cuda_fail(e, "h0 init");
+    }
+    *out = o;
+    return OCEAN_OK;
+}
+
+int ocean_create_seeded(const ocean_params* params, uint64_t seed, ocean_t** out)
+{
+    if (!out) return fail(OCEAN_ERR_INVALID, "out is NULL");
+    *out = nullptr;
+    int rc = validate(params);
+    if (rc) return rc;
+    std::vector<float> nz(4 * (size_t)params->N * params->N);
+    ocean_fill_noise(seed, params->N, nz.data());
+    return ocean_create(params, nz.data(), out);
+}
+
+void ocean_destroy(ocean_t* o) { delete o; }
+
+int ocean_get_params(const ocean_t* o, ocean_params* params)
+{
+    if (!o || !params) return fail(OCEAN_ERR_INVALID, "NULL argument");
+    *params = o->p;
+    return OCEAN_OK;
+}
+
+int ocean_set_params(ocean_t* o, const ocean_params* params)
+{
+    if (!o) return fail(OCEAN_ERR_INVALID, "ocean is NULL");
+    int rc = validate(params);
+    if (rc) return rc;
+    if (params->N != o->N) return fail(OCEAN_ERR_INVALID, "ocean_set_params cannot change N");
+    o->p = *params;
+    o->set_consts();
+    if ((rc = o->build_h0(0)) != OCEAN_OK) return rc;
+    cudaError_t e = cudaStreamSynchronize(0);
+    if (e != cudaSuccess) return cuda_fail(e, "h0 init");
+    return OCEAN_OK;
+}
+
+int ocean_get_h0(const ocean_t* o, float* dst, void* stream)
+{
+    if (!o || !dst) return fail(OCEAN_ERR_INVALID, "NULL argument");
+    cudaError_t e = cudaMemcpyAsync(dst, o->h0, (size_t)o->N * o->N * sizeof(float4), cudaMemcpyDefault,
+                                    static_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess) return cuda_fail(e, "ocean_get_h0");
+    return OCEAN_OK;
+}
+
+int ocean_set_h0(ocean_t* o, const float* src, void* stream)
+{
+    if (!o || !src) return fail(OCEAN_ERR_INVALID, "NULL argument");
+    cudaError_t e = cudaMemcpyAsync(o->h0, src, (size_t)o->N * o->N * sizeof(float4), cudaMemcpyDefault,
+                                    static_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess) return cuda_fail(e, "ocean_set_h0");
+    return OCEAN_OK;
+}
+
+int ocean_get_outputs(ocean_t* o, ocean_outputs* out)
+{
+    if (!o || !out) return fail(OCEAN_ERR_INVALID, "NULL argument");
+    const size_t NN = (size_t)o->N * o->N;
+    if (!o->out) {
+        cudaError_t e = cudaMalloc(&o->out, NN * 7 * sizeof(float));
+        if (e != cudaSuccess) {
+            o->out = nullptr;
+            return fail(OCEAN_ERR_NOMEM, std::string("output allocation failed: ") + cudaGetErrorString(e));
+        }
+    }
+    out->dx       = o->out;
+    out->dy       = o->out + NN;
+    out->dz       = o->out + 2 * NN;
+    out->normal_j = o->out + 3 * NN;
+    return OCEAN_OK;
+}
+
+int ocean_update_rows(ocean_t* o, double t, void* stream)
+{
+    if (!o) return fail(OCEAN_ERR_INVALID, "ocean is NULL");
+    if (!std::isfinite(t)) return fail(OCEAN_ERR_INVALID, "time is not finite");
+    ocean::RowArgs ra;
+    ra.h0           = o->h0;
+    ra.inter        = o->inter;
+    ra.tw           = o->tw;
+    ra.fc           = o->frame(t);
+    ra.literal_conj = (o->p.flags & OCEAN_FLAG_LITERAL_CONJ) ? 1 : 0;
+    cudaError_t e   = ocean::launch_row_pass(o->N, ra, static_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess) return cuda_fail(e, "row pass launch");
+    return OCEAN_OK;
+}
+
+int ocean_update_columns(ocean_t* o, const ocean_outputs* out, void* stream)
+{
+    if (!o) return fail(OCEAN_ERR_INVALID, "ocean is NULL");
+    ocean_outputs own;
+    if (!out) {
+        int rc = ocean_get_outputs(o, &own);
+        if (rc) return rc;
+        out = &own;
+    }
+    if (!out->dx || !out->dy || !out->dz || !out->normal_j) return fail(OCEAN_ERR_INVALID, "NULL output pointer");
+    const uintptr_t al = reinterpret_cast<uintptr_t>(out->dx) | reinterpret_cast<uintptr_t>(out->dy) |
+                         reinterpret_cast<uintptr_t>(out->dz) | reinterpret_cast<uintptr_t>(out->normal_j);
+    if (al % 16) return fail(OCEAN_ERR_INVALID, "output pointers must be 16-byte aligned");
+    ocean::ColArgs ca;
+    ca.inter      = o->inter;
+    ca.tw         = o->tw;
+    ca.dx         = out->dx;
+    ca.dy         = out->dy;
+    ca.dz         = out->dz;
+    ca.nj         = reinterpret_cast<float4*>(out->normal_j);
+    ca.scale      = (float)(0.5 / ((double)o->N * o->N));
+    ca.lambda     = o->p.choppiness;
+    ca.inv2d      = (float)((double)o->N / (2.0 * (double)o->p.L));
+    cudaError_t e = ocean::launch_col_pass(o->N, ca, static_cast<cudaStream_t>(stream));
+    if (e != cudaSuccess) return cuda_fail(e, "column pass launch");
+    return OCEAN_OK;
+}
+
+int ocean_update(ocean_t* o, double t, const ocean_outputs* out, void* stream)
+{
+    if (!o) return fail(OCEAN_ERR_INVALID, "ocean is NULL");
+    if (!std::isfinite(t)) return fail(OCEAN_ERR_INVALID, "time is not finite");
+    ocean_outputs own;
+    if (!out) {
+        int rc = ocean_get_outputs(o, &own);
+        if (rc) return rc;
+        out = &own;
+    }
+    if (!out->dx || !out->dy || !out->dz || !out->normal_j) return fail(OCEAN_ERR_INVALID, "NULL output pointer");
+    int rc = ocean_update_rows(o, t, stream);
+    if (rc) return rc;
+    return ocean_update_columns(o, out, stream);
+}
+
+}  // extern "C"

@@ -1,0 +1,240 @@
+"""ctypes binding of include/ocean.h (libocean_gb300.so).
+
+This is the binding a Python caller of the library uses; it mirrors the
+reference's per-frame interface (FFTOceanWaves::init / update, main.cpp:199-255):
+``Ocean(params, noise)`` runs the init-time h0 and table set-up and
+``Ocean.update(t)`` runs one frame of the hot path on the GPU.
+
+The library must have been built (``python fft-ocean-waves_gb300/build.py``
+or ``__graft_entry__.build()``); there is no CPU fallback and loading fails
+loudly when it is missing.  Device buffers are passed as integer addresses;
+torch tensors are accepted where convenient (``data_ptr()``).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import dataclasses
+import math
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libocean_gb300.so")
+
+OCEAN_OK = 0
+OCEAN_ERR_INVALID = -1
+OCEAN_ERR_CUDA = -2
+OCEAN_ERR_NOMEM = -3
+OCEAN_ERR_UNSUPPORTED = -4
+OCEAN_FLAG_LITERAL_CONJ = 1
+
+# Every entry point include/ocean.h declares (checked by the CPU tests).
+EXPORTS = [
+    "ocean_create", "ocean_create_seeded", "ocean_destroy", "ocean_update", "ocean_update_rows",
+    "ocean_update_columns", "ocean_get_outputs",
+    "ocean_set_params", "ocean_get_params", "ocean_get_h0", "ocean_set_h0", "ocean_compute_h0",
+    "ocean_fill_noise", "ocean_bit_reversed_indices", "ocean_butterfly_table", "ocean_last_error",
+    "ocean_version",
+]
+
+
+class OceanError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"ocean error {code}: {msg}")
+        self.code = code
+
+
+class ocean_params(C.Structure):
+    _fields_ = [("N", C.c_int32), ("flags", C.c_uint32), ("L", C.c_float), ("amplitude", C.c_float),
+                ("wind_speed", C.c_float), ("wind_dir_x", C.c_float), ("wind_dir_y", C.c_float),
+                ("choppiness", C.c_float), ("suppression", C.c_float), ("gravity", C.c_float)]
+
+
+class ocean_outputs(C.Structure):
+    _fields_ = [("dx", C.c_void_p), ("dy", C.c_void_p), ("dz", C.c_void_p), ("normal_j", C.c_void_p)]
+
+
+@dataclasses.dataclass
+class Params:
+    """Tile parameters (defaults: the reference's main.cpp:1631-1646)."""
+    N: int = 256
+    L: float = 1000.0
+    amplitude: float = 2.0
+    wind_speed: float = 80.0
+    wind_dir_x: float = 1.0
+    wind_dir_y: float = 1.0
+    choppiness: float = 0.75
+    suppression: float = 0.1
+    gravity: float = 9.81
+    literal_conj: bool = False
+
+    @staticmethod
+    def from_angle(N, L, amplitude, wind_speed, angle_deg, choppiness, suppression=0.1, **kw):
+        a = math.radians(angle_deg)
+        return Params(N=N, L=L, amplitude=amplitude, wind_speed=wind_speed, wind_dir_x=math.cos(a),
+                      wind_dir_y=math.sin(a), choppiness=choppiness, suppression=suppression, **kw)
+
+    def c(self) -> ocean_params:
+        return ocean_params(self.N, OCEAN_FLAG_LITERAL_CONJ if self.literal_conj else 0, self.L,
+                            self.amplitude, self.wind_speed, self.wind_dir_x, self.wind_dir_y,
+                            self.choppiness, self.suppression, self.gravity)
+
+
+_lib = None
+
+
+def load() -> C.CDLL:
+    """Load libocean_gb300.so; raises if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise OceanError(OCEAN_ERR_UNSUPPORTED,
+                         f"{LIB_PATH} is missing: build it with fft-ocean-waves_gb300/build.py")
+    L = C.CDLL(LIB_PATH)
+    vp, P = C.c_void_p, C.POINTER
+    L.ocean_create.argtypes = [P(ocean_params), P(C.c_float), P(vp)]
+    L.ocean_create_seeded.argtypes = [P(ocean_params), C.c_uint64, P(vp)]
+    L.ocean_destroy.argtypes = [vp]
+    L.ocean_destroy.restype = None
+    L.ocean_update.argtypes = [vp, C.c_double, P(ocean_outputs), vp]
+    L.ocean_update_rows.argtypes = [vp, C.c_double, vp]
+    L.ocean_update_columns.argtypes = [vp, P(ocean_outputs), vp]
+    L.ocean_get_outputs.argtypes = [vp, P(ocean_outputs)]
+    L.ocean_set_params.argtypes = [vp, P(ocean_params)]
+    L.ocean_get_params.argtypes = [vp, P(ocean_params)]
+    L.ocean_get_h0.argtypes = [vp, vp, vp]
+    L.ocean_set_h0.argtypes = [vp, vp, vp]
+    L.ocean_compute_h0.argtypes = [P(ocean_params), vp, vp, vp]
+    L.ocean_fill_noise.argtypes = [C.c_uint64, C.c_int32, P(C.c_float)]
+    L.ocean_bit_reversed_indices.argtypes = [C.c_int32, P(C.c_int32)]
+    L.ocean_butterfly_table.argtypes = [C.c_int32, P(C.c_float)]
+    L.ocean_last_error.restype = C.c_char_p
+    for name in EXPORTS:
+        if name not in ("ocean_destroy", "ocean_last_error"):
+            getattr(L, name).restype = C.c_int
+    _lib = L
+    return L
+
+
+def check(rc: int) -> None:
+    if rc != OCEAN_OK:
+        raise OceanError(rc, load().ocean_last_error().decode())
+
+
+def _addr(x) -> int | None:
+    if x is None:
+        return None
+    if isinstance(x, int):
+        return x
+    if hasattr(x, "data_ptr"):
+        return x.data_ptr()
+    raise TypeError(f"cannot take a device address of {type(x)}")
+
+
+def _stream(s) -> int | None:
+    if s is None:
+        return None
+    if isinstance(s, int):
+        return s
+    return s.cuda_stream  # torch.cuda.Stream
+
+
+def fill_noise(seed: int, N: int):
+    import numpy as np
+    out = np.empty((4, N, N), dtype=np.float32)
+    check(load().ocean_fill_noise(seed, N, out.ctypes.data_as(C.POINTER(C.c_float))))
+    return out
+
+
+def bit_reversed_indices(N: int):
+    import numpy as np
+    out = np.empty(N, dtype=np.int32)
+    check(load().ocean_bit_reversed_indices(N, out.ctypes.data_as(C.POINTER(C.c_int32))))
+    return out
+
+
+def butterfly_table(N: int):
+    import numpy as np
+    lg = N.bit_length() - 1
+    out = np.empty((lg, N, 4), dtype=np.float32)
+    check(load().ocean_butterfly_table(N, out.ctypes.data_as(C.POINTER(C.c_float))))
+    return out
+
+
+def compute_h0(params: Params, noise_dev, h0_dev, stream=None) -> None:
+    cp = params.c()
+    check(load().ocean_compute_h0(C.byref(cp), _addr(noise_dev), _addr(h0_dev), _stream(stream)))
+
+
+class Ocean:
+    """One ocean tile on the GPU (handle of include/ocean.h)."""
+
+    def __init__(self, params: Params, noise=None, seed: int | None = None):
+        L = load()
+        self.params = params
+        self._h = C.c_void_p()
+        cp = params.c()
+        if noise is not None:
+            import numpy as np
+            nz = np.ascontiguousarray(noise, dtype=np.float32)
+            if nz.size != 4 * params.N * params.N:
+                raise ValueError("noise must hold 4*N*N floats")
+            check(L.ocean_create(C.byref(cp), nz.ctypes.data_as(C.POINTER(C.c_float)), C.byref(self._h)))
+        else:
+            check(L.ocean_create_seeded(C.byref(cp), int(seed or 0), C.byref(self._h)))
+
+    @property
+    def handle(self) -> int:
+        return self._h.value
+
+    def update(self, t: float, dx=None, dy=None, dz=None, normal_j=None, stream=None) -> None:
+        """One frame at time t.  Without output buffers, the handle's own
+        buffers (``outputs()``) are written."""
+        if dx is None:
+            check(load().ocean_update(self._h, float(t), None, _stream(stream)))
+            return
+        o = ocean_outputs(_addr(dx), _addr(dy), _addr(dz), _addr(normal_j))
+        check(load().ocean_update(self._h, float(t), C.byref(o), _stream(stream)))
+
+    def update_rows(self, t: float, stream=None) -> None:
+        check(load().ocean_update_rows(self._h, float(t), _stream(stream)))
+
+    def update_columns(self, dx=None, dy=None, dz=None, normal_j=None, stream=None) -> None:
+        if dx is None:
+            check(load().ocean_update_columns(self._h, None, _stream(stream)))
+            return
+        o = ocean_outputs(_addr(dx), _addr(dy), _addr(dz), _addr(normal_j))
+        check(load().ocean_update_columns(self._h, C.byref(o), _stream(stream)))
+
+    def outputs(self) -> dict:
+        o = ocean_outputs()
+        check(load().ocean_get_outputs(self._h, C.byref(o)))
+        return {"dx": o.dx, "dy": o.dy, "dz": o.dz, "normal_j": o.normal_j}
+
+    def set_params(self, params: Params) -> None:
+        cp = params.c()
+        check(load().ocean_set_params(self._h, C.byref(cp)))
+        self.params = params
+
+    def get_h0(self, dst, stream=None) -> None:
+        check(load().ocean_get_h0(self._h, _addr(dst), _stream(stream)))
+
+    def set_h0(self, src, stream=None) -> None:
+        check(load().ocean_set_h0(self._h, _addr(src), _stream(stream)))
+
+    def close(self) -> None:
+        if self._h and self._h.value:
+            load().ocean_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,149 @@
+/*
+ * ocean.h -- C ABI of the GB300 Tessendorf FFT ocean library.
+ *
+ * Drop-in for the per-frame compute-shader path of diharaw/fft-ocean-waves
+ * (src/main.cpp, class FFTOceanWaves).  All file:line citations below are
+ * paths inside that project.
+ *
+ * Conventions
+ *   - Every int-returning call returns OCEAN_OK (0) or a negative OCEAN_ERR_*;
+ *     ocean_last_error() then describes the failure (thread-local string).
+ *     No C++ exception crosses this boundary.
+ *   - Device buffers are row-major [y][x] with x the column (the reference's
+ *     image coordinate gl_GlobalInvocationID.xy).  Mode (x, y) holds the wave
+ *     vector k = 2*pi*(x - N/2, y - N/2)/L (tilde_h0_k_cs.glsl:76-77).
+ *   - `stream` is a cudaStream_t passed as void* (NULL = legacy default
+ *     stream).  Calls that take a stream are asynchronous and stream-ordered.
+ *   - A handle is not thread-safe; distinct handles may be used concurrently.
+ *   - Device output pointers must be 16-byte aligned.
+ */
+#ifndef OCEAN_GB300_H
+#define OCEAN_GB300_H
+
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define OCEAN_API __attribute__((visibility("default")))
+#else
+#define OCEAN_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define OCEAN_OK 0
+#define OCEAN_ERR_INVALID -1     /* bad argument (size, pointer, parameter) */
+#define OCEAN_ERR_CUDA -2        /* a CUDA runtime call or launch failed   */
+#define OCEAN_ERR_NOMEM -3       /* device or host allocation failed       */
+#define OCEAN_ERR_UNSUPPORTED -4 /* no kernel for this device / size       */
+
+#define OCEAN_MIN_N 32
+#define OCEAN_MAX_N 2048
+
+/* Flags for ocean_params.flags */
+/* Reproduce tilde_h0_t_cs.glsl:42-48,94 literally: its conjugate() returns the
+ * argument unchanged, so h0(-k) enters the evolution unconjugated.  Default
+ * (flag clear) is the textbook conj(h0(-k)). */
+#define OCEAN_FLAG_LITERAL_CONJ 1u
+
+/* Spectrum parameters: the reference's uniforms u_N, u_L, u_Amplitude,
+ * u_WindSpeed, u_WindDirection, u_SuppressFactor (tilde_h0_k_cs.glsl:19-24)
+ * and u_Choppiness (grid_tes.glsl:33), with defaults main.cpp:1631-1646. */
+typedef struct ocean_params {
+    int32_t  N;           /* grid size: power of two, 32..2048 (main.cpp:17,1645)   */
+    uint32_t flags;       /* OCEAN_FLAG_*                                           */
+    float    L;           /* patch length, metres (reference: int u_L = 1000)       */
+    float    amplitude;   /* Phillips A (2.0)                                       */
+    float    wind_speed;  /* V, m/s (80.0)                                          */
+    float    wind_dir_x;  /* wind direction, normalised internally (main.cpp:555)   */
+    float    wind_dir_y;  /*   reference default (1, 1)                             */
+    float    choppiness;  /* lambda applied to Dx, Dz (0.75)                         */
+    float    suppression; /* small-wave cutoff l, metres (0.1)                      */
+    float    gravity;     /* g (9.81, tilde_h0_k_cs.glsl:26); <= 0 selects 9.81      */
+} ocean_params;
+
+/* Per-frame outputs, device pointers, each N*N elements row-major.
+ * dx, dy, dz: R32F displacement maps (the reference's m_dx, m_dy, m_dz,
+ * main.cpp:1096-1098) with dx, dz already multiplied by lambda.
+ * normal_j: RGBA32F (nx, ny, nz, J): the Sobel normal of dy
+ * (normal_map_cs.glsl:24-54, periodic integer taps) and the Jacobian of the
+ * rendered surface p = x - (dx, dz) (reference normal.w is 1). */
+typedef struct ocean_outputs {
+    float* dx;
+    float* dy;
+    float* dz;
+    float* normal_j; /* N*N*4 floats */
+} ocean_outputs;
+
+typedef struct ocean_s ocean_t;
+
+/* Create a tile: validates params, uploads the four U(0,1] noise planes
+ * (host pointer, 4*N*N floats, [plane][y][x]; planes 0/1 feed h0(k), 2/3 feed
+ * h0(-k)) and builds h0 on the device.
+ * Replaces FFTOceanWaves::init's tilde_h0_k(), generate_bit_reversed_indices()
+ * and generate_twiddle_factors() (main.cpp:217-220, :553-583, :711-744).
+ * Synchronous. */
+OCEAN_API int ocean_create(const ocean_params* params, const float* noise_host, ocean_t** out);
+
+/* ocean_create with noise from ocean_fill_noise(seed, N). */
+OCEAN_API int ocean_create_seeded(const ocean_params* params, uint64_t seed, ocean_t** out);
+
+OCEAN_API void ocean_destroy(ocean_t* ocean);
+
+/* One frame at time t (seconds, double; the phase omega*t is reduced in
+ * double-float precision).  Replaces tilde_h0_t(); butterfly_fft(dy),
+ * butterfly_fft(dx), butterfly_fft(dz); generate_normal_map()
+ * (main.cpp:240-244).  out == NULL writes the handle-owned buffers returned
+ * by ocean_get_outputs().  Two kernel launches on `stream`. */
+OCEAN_API int ocean_update(ocean_t* ocean, double t, const ocean_outputs* out, void* stream);
+
+/* ocean_update in its two stages, for callers that interleave other work or
+ * time the kernels separately: the row stage (evolution + horizontal FFT,
+ * replacing tilde_h0_t() and the horizontal butterfly passes, main.cpp:240,
+ * :626-640) and the column stage (vertical FFT + inversion + normal map,
+ * main.cpp:647-707).  ocean_update == rows then columns on one stream. */
+OCEAN_API int ocean_update_rows(ocean_t* ocean, double t, void* stream);
+OCEAN_API int ocean_update_columns(ocean_t* ocean, const ocean_outputs* out, void* stream);
+
+/* Handle-owned output buffers (allocated on first use); the headless
+ * stand-ins for the reference's GL textures m_dx/m_dy/m_dz/m_normal_map. */
+OCEAN_API int ocean_get_outputs(ocean_t* ocean, ocean_outputs* out);
+
+/* Replace the spectrum parameters (same N) and rebuild h0 from the stored
+ * noise.  The reference reads GUI edits of wind speed and amplitude
+ * (main.cpp:348-358) but never re-runs tilde_h0_k(), so they have no effect
+ * there; here they do.  Synchronous. */
+OCEAN_API int ocean_set_params(ocean_t* ocean, const ocean_params* params);
+OCEAN_API int ocean_get_params(const ocean_t* ocean, ocean_params* params);
+
+/* Checkpoint / restore of the spectrum state: N*N*4 floats
+ * (h0k.re, h0k.im, h0minusk.re, h0minusk.im) per mode, host or device
+ * pointer (unified addressing), stream-ordered. */
+OCEAN_API int ocean_get_h0(const ocean_t* ocean, float* dst, void* stream);
+OCEAN_API int ocean_set_h0(ocean_t* ocean, const float* src, void* stream);
+
+/* Stateless h0 initialisation (tilde_h0_k_cs.glsl:35-93) into a caller
+ * buffer: noise_dev (device, 4*N*N) -> h0_dev (device, N*N*4). */
+OCEAN_API int ocean_compute_h0(const ocean_params* params, const float* noise_dev, float* h0_dev, void* stream);
+
+/* Seeded uniform noise: splitmix64 -> 24-bit uniforms in (0, 1], 4*N*N
+ * floats [plane][y][x] into a host buffer.  Stands in for the blue-noise
+ * textures data/noise/LDR_LLL1_{0..3}.png (main.cpp:1085-1088). */
+OCEAN_API int ocean_fill_noise(uint64_t seed, int32_t N, float* host_out);
+
+/* The reference's FFT tables, host side, for callers that consumed them:
+ * bit-reversed indices (main.cpp:29-64,733-744), N int32, and the butterfly
+ * table (twiddle_factors_cs.glsl:34-69): log2(N) x N x 4 floats
+ * (Re w, Im w, index p, index q).  The kernels use their own Stockham
+ * twiddles and do not need either. */
+OCEAN_API int ocean_bit_reversed_indices(int32_t N, int32_t* host_out);
+OCEAN_API int ocean_butterfly_table(int32_t N, float* host_out);
+
+OCEAN_API const char* ocean_last_error(void);
+OCEAN_API int ocean_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* OCEAN_GB300_H */

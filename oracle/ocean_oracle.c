@@ -1,0 +1,511 @@
+/*
+ * ocean_oracle.c -- TEST INFRASTRUCTURE ONLY.
+ *
+ * CPU restatement of diharaw/fft-ocean-waves' per-frame ocean path, used as the
+ * checker for the CUDA library and as the timed CPU baseline.  Nothing in the
+ * product links this file: only tests/, __graft_entry__.smoke() and bench.py's
+ * CPU-baseline leg load it.
+ *
+ * Two restatements live here:
+ *
+ *   orc_*   FP64 oracle.  Follows the shader arithmetic with every quantity in
+ *           double, the phase w*t included, and the 2-D inverse transform done
+ *           by an FP64 radix-2 FFT.  This is the reference the GPU results are
+ *           graded against (relative L2 <= 1e-5 per field).
+ *
+ *   port_*  FP32 port of the reference's *algorithm*: the same passes the GL
+ *           demo dispatches per frame (spectrum pass, 2*log2(N) table-driven
+ *           radix-2 ping-pong passes per field, inversion, Sobel normal map),
+ *           each pass a full-grid sweep parallelised with OpenMP.  It is the
+ *           CPU baseline bench.py times, and a second parity point.
+ *
+ * Pinned semantics (the reference leaves these undefined or quirky):
+ *   Q1  tilde_h0_t_cs.glsl:42-48 `conjugate()` returns its argument unchanged.
+ *       Default here is the textbook conj(h0(-k)); literal_conj=1 reproduces
+ *       the shader (no conjugation).
+ *   Q3  tilde_h0_k_cs.glsl:76-77,44: normalize(k) at k=0 is NaN.  The DC mode
+ *       is pinned to h0 = 0.
+ *   Q4  pow(x, 2.0) with x<0 is undefined in GLSL (tilde_h0_k_cs.glsl:44);
+ *       (k^.w^)^2 is used.
+ *   Q7  normal_map_cs.glsl:37-44 samples the height map through a sampler
+ *       whose filter/wrap are left to the GL framework.  Pinned: integer texel
+ *       taps with periodic wrap.
+ *   Q8  Outputs are Dx*lambda, Dy, Dz*lambda (grid_tes.glsl:60-62 applies
+ *       lambda with a minus sign at render time; the renderer subtracts), and
+ *       the Jacobian of p = x - (Dx, Dz) with periodic central differences of
+ *       spacing L/N goes in normal.w (a build addition; the reference's
+ *       normal.w is 1).
+ */
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#define ORC_PI 3.14159265358979323846
+
+typedef struct orc_params {
+    int32_t N;
+    int32_t literal_conj;
+    double L;           /* patch length in metres (the shader's u_L, an int there) */
+    double amplitude;   /* u_Amplitude */
+    double wind_speed;  /* u_WindSpeed */
+    double wind_x;      /* u_WindDirection, normalised here as main.cpp:555 does */
+    double wind_y;
+    double choppiness;  /* lambda (grid_tes.glsl:61-62 u_Choppiness) */
+    double suppression; /* u_SuppressFactor, small-wave cutoff l in metres */
+    double gravity;     /* g = 9.81 in the shaders */
+} orc_params;
+
+static int ilog2i(int n)
+{
+    int l = 0;
+    while ((1 << l) < n) ++l;
+    return l;
+}
+
+/* ------------------------------------------------------------------------- */
+/* FP64 oracle                                                               */
+/* ------------------------------------------------------------------------- */
+
+/* Phillips amplitude a(k) = clamp(sqrt(P(k))/sqrt(2), -4000, 4000) of
+ * tilde_h0_k_cs.glsl:35-45,76-88, in double.  P(-k) == P(k) with (k^.w^)^2,
+ * so h0minusk uses the same amplitude (tilde_h0_k_cs.glsl:88). */
+static double orc_amp(const orc_params* p, double kx, double kz, double wx, double wy, int* clamped)
+{
+    double kl  = sqrt(kx * kx + kz * kz);
+    double km  = kl < 0.00001 ? 0.00001 : kl;           /* :81-82 */
+    double k2  = km * km;                               /* :84 */
+    double Lp  = p->wind_speed * p->wind_speed / p->gravity; /* :78 */
+    double sup = exp(-k2 * p->suppression * p->suppression); /* :35-38 */
+    double kd  = (kx * wx + kz * wy) / kl;              /* dot(normalize(k), w) */
+    double P   = p->amplitude * exp(-1.0 / (k2 * Lp * Lp)) * (kd * kd) * sup / (k2 * k2); /* :42-45 */
+    double a   = sqrt(P) / sqrt(2.0);                   /* :87 */
+    if (clamped) *clamped = a > 4000.0;
+    return a > 4000.0 ? 4000.0 : a;                     /* clamp(.., -4000, 4000); a >= 0 */
+}
+
+/* Number of modes the +-4000 clamp is active on (diagnostic for tests). */
+int orc_count_clamped(const orc_params* p)
+{
+    int N = p->N, n = 0;
+    double wn = sqrt(p->wind_x * p->wind_x + p->wind_y * p->wind_y);
+    for (int y = 0; y < N; ++y)
+        for (int x = 0; x < N; ++x) {
+            double ix = x - N / 2.0, iz = y - N / 2.0;
+            if (ix == 0.0 && iz == 0.0) continue;
+            int c = 0;
+            orc_amp(p, 2.0 * ORC_PI * ix / p->L, 2.0 * ORC_PI * iz / p->L, p->wind_x / wn, p->wind_y / wn, &c);
+            n += c;
+        }
+    return n;
+}
+
+/* h0 initialisation: tilde_h0_k_cs.glsl:51-68 (Box-Muller) and :74-93.
+ * noise: four N*N planes [plane][y][x] of U(0,1] values (the four noise
+ * textures sampled at texel (x, y)).  h0: N*N*4 doubles per mode
+ * (h0k.re, h0k.im, h0minusk.re, h0minusk.im), row-major [y][x]. */
+void orc_h0(const orc_params* p, const float* noise, double* h0)
+{
+    int    N  = p->N;
+    size_t NN = (size_t)N * N;
+    double wn = sqrt(p->wind_x * p->wind_x + p->wind_y * p->wind_y);
+    double wx = p->wind_x / wn, wy = p->wind_y / wn;    /* main.cpp:555 */
+    for (int y = 0; y < N; ++y)
+        for (int x = 0; x < N; ++x) {
+            size_t i  = (size_t)y * N + x;
+            double ix = x - N / 2.0, iz = y - N / 2.0;  /* :76 */
+            double kx = 2.0 * ORC_PI * ix / p->L, kz = 2.0 * ORC_PI * iz / p->L; /* :77 */
+            double a  = (ix == 0.0 && iz == 0.0) ? 0.0 : orc_amp(p, kx, kz, wx, wy, NULL); /* Q3 */
+            double n[4];
+            for (int q = 0; q < 4; ++q) {
+                double v = noise[q * NN + i];
+                n[q]     = v < 0.001 ? 0.001 : (v > 1.0 ? 1.0 : v); /* :55-58 */
+            }
+            double u0 = 2.0 * ORC_PI * n[0], v0 = sqrt(-2.0 * log(n[1])); /* :60-61 */
+            double u1 = 2.0 * ORC_PI * n[2], v1 = sqrt(-2.0 * log(n[3])); /* :62-63 */
+            h0[4 * i + 0] = v0 * cos(u0) * a;            /* :92 rnd.xy * h0k */
+            h0[4 * i + 1] = v0 * sin(u0) * a;
+            h0[4 * i + 2] = v1 * cos(u1) * a;            /* :93 rnd.zw * h0minusk */
+            h0[4 * i + 3] = v1 * sin(u1) * a;
+        }
+}
+
+/* Per-frame spectra: tilde_h0_t_cs.glsl:70-131 in double.
+ * spec: 3 fields [f][y][x][re,im], f = 0 (Dx), 1 (Dy, height), 2 (Dz). */
+void orc_spectrum(const orc_params* p, const double* h0, double t, double* spec)
+{
+    int    N  = p->N;
+    size_t NN = (size_t)N * N;
+    for (int y = 0; y < N; ++y)
+        for (int x = 0; x < N; ++x) {
+            size_t i  = (size_t)y * N + x;
+            double ix = x - N / 2.0, iz = y - N / 2.0;  /* :72 */
+            double kx = 2.0 * ORC_PI * ix / p->L, kz = 2.0 * ORC_PI * iz / p->L; /* :73 */
+            double km = sqrt(kx * kx + kz * kz);
+            if (km < 0.00001) km = 0.00001;             /* :76-77 */
+            double w  = sqrt(p->gravity * km);          /* :79 */
+            double c  = cos(w * t), s = sin(w * t);     /* :96-97 (FP64 phase) */
+            double ar = h0[4 * i + 0], ai = h0[4 * i + 1];
+            double br = h0[4 * i + 2], bi = h0[4 * i + 3];
+            if (!p->literal_conj) bi = -bi;             /* Q1: conj(h0(-k)) */
+            /* hy = a e^{iwt} + b e^{-iwt} (:110) */
+            double hr = ar * c - ai * s + br * c + bi * s;
+            double hi = ar * s + ai * c - br * s + bi * c;
+            /* hx = (-i kx/|k|) hy (:113-118), hz = (-i kz/|k|) hy (:121-126) */
+            double fx = -kx / km, fz = -kz / km;
+            spec[2 * (0 * NN + i) + 0] = -fx * hi;
+            spec[2 * (0 * NN + i) + 1] = fx * hr;
+            spec[2 * (1 * NN + i) + 0] = hr;
+            spec[2 * (1 * NN + i) + 1] = hi;
+            spec[2 * (2 * NN + i) + 0] = -fz * hi;
+            spec[2 * (2 * NN + i) + 1] = fz * hr;
+        }
+}
+
+/* In-place radix-2 FFT of n complex doubles (interleaved), exponent sign `sg`.
+ * Unnormalised. */
+static void orc_fft1(double* a, int n, int stride, int sg)
+{
+    int lg = ilog2i(n);
+    for (int i = 0; i < n; ++i) {
+        int r = 0;
+        for (int b = 0; b < lg; ++b) r |= ((i >> b) & 1) << (lg - 1 - b);
+        if (r > i) {
+            double* u = a + 2 * (size_t)i * stride;
+            double* v = a + 2 * (size_t)r * stride;
+            double  t0 = u[0], t1 = u[1];
+            u[0] = v[0]; u[1] = v[1]; v[0] = t0; v[1] = t1;
+        }
+    }
+    for (int h = 1; h < n; h <<= 1)
+        for (int k = 0; k < h; ++k) {
+            double ang = sg * ORC_PI * k / h;
+            double wr = cos(ang), wi = sin(ang);
+            for (int i = k; i < n; i += 2 * h) {
+                double* u = a + 2 * (size_t)i * stride;
+                double* v = a + 2 * (size_t)(i + h) * stride;
+                double  br = v[0] * wr - v[1] * wi, bi = v[0] * wi + v[1] * wr;
+                v[0] = u[0] - br; v[1] = u[1] - bi;
+                u[0] += br; u[1] += bi;
+            }
+        }
+}
+
+/* Re of the unnormalised 2-D inverse DFT (positive exponent) that the
+ * butterfly passes compute (butterfly_cs.glsl:54-132), followed by the
+ * (-1)^(x+y)/N^2 of inversion_cs.glsl:29-41.  spec_f: one field [y][x][2]. */
+void orc_ifft2_real(int N, const double* spec_f, double* d)
+{
+    size_t  NN = (size_t)N * N;
+    double* a  = (double*)malloc(2 * NN * sizeof(double));
+    memcpy(a, spec_f, 2 * NN * sizeof(double));
+    for (int y = 0; y < N; ++y) orc_fft1(a + 2 * (size_t)y * N, N, 1, +1);
+    for (int x = 0; x < N; ++x) orc_fft1(a + 2 * (size_t)x, N, N, +1);
+    double inv = 1.0 / ((double)N * N);
+    for (int y = 0; y < N; ++y)
+        for (int x = 0; x < N; ++x) {
+            double perm = ((x + y) & 1) ? -1.0 : 1.0;
+            d[(size_t)y * N + x] = perm * a[2 * ((size_t)y * N + x)] * inv;
+        }
+    free(a);
+}
+
+/* Output stage: lambda scaling (Q8), Sobel normal on Dy (normal_map_cs.glsl:
+ * 37-53, Q7), Jacobian (Q8).  raw: 3 planes (Dx, Dy, Dz) before lambda.
+ * nj: N*N*4 (nx, ny, nz, J). */
+void orc_finish(const orc_params* p, const double* raw, double* dx, double* dy, double* dz, double* nj)
+{
+    int    N  = p->N;
+    size_t NN = (size_t)N * N;
+    double lam = p->choppiness;
+    for (size_t i = 0; i < NN; ++i) {
+        dx[i] = lam * raw[i];
+        dy[i] = raw[NN + i];
+        dz[i] = lam * raw[2 * NN + i];
+    }
+    double inv2d = (double)N / (2.0 * p->L);            /* 1 / (2 * L/N) */
+#define AT(arr, xx, yy) arr[(size_t)(((yy) + N) % N) * N + (size_t)(((xx) + N) % N)]
+    for (int y = 0; y < N; ++y)
+        for (int x = 0; x < N; ++x) {
+            double z0 = AT(dy, x - 1, y - 1), z1 = AT(dy, x, y - 1), z2 = AT(dy, x + 1, y - 1);
+            double z3 = AT(dy, x - 1, y), z4 = AT(dy, x + 1, y);
+            double z5 = AT(dy, x - 1, y + 1), z6 = AT(dy, x, y + 1), z7 = AT(dy, x + 1, y + 1);
+            double nz = z0 + 2 * z1 + z2 - z5 - 2 * z6 - z7; /* :49 */
+            double nx = z0 + 2 * z3 + z5 - z2 - 2 * z4 - z7; /* :50 */
+            double ny = 1.0;
+            double rn = 1.0 / sqrt(nx * nx + ny * ny + nz * nz);
+            double dxx = (AT(dx, x + 1, y) - AT(dx, x - 1, y)) * inv2d;
+            double dxz = (AT(dx, x, y + 1) - AT(dx, x, y - 1)) * inv2d;
+            double dzx = (AT(dz, x + 1, y) - AT(dz, x - 1, y)) * inv2d;
+            double dzz = (AT(dz, x, y + 1) - AT(dz, x, y - 1)) * inv2d;
+            size_t i = (size_t)y * N + x;
+            nj[4 * i + 0] = nx * rn;
+            nj[4 * i + 1] = ny * rn;
+            nj[4 * i + 2] = nz * rn;
+            nj[4 * i + 3] = (1.0 - dxx) * (1.0 - dzz) - dxz * dzx;
+        }
+#undef AT
+}
+
+/* One full frame from h0 at time t (double). */
+void orc_update(const orc_params* p, const double* h0, double t, double* dx, double* dy, double* dz, double* nj)
+{
+    size_t  NN   = (size_t)p->N * p->N;
+    double* spec = (double*)malloc(6 * NN * sizeof(double));
+    double* raw  = (double*)malloc(3 * NN * sizeof(double));
+    orc_spectrum(p, h0, t, spec);
+    for (int f = 0; f < 3; ++f) orc_ifft2_real(p->N, spec + 2 * f * NN, raw + f * NN);
+    orc_finish(p, raw, dx, dy, dz, nj);
+    free(spec);
+    free(raw);
+}
+
+/* FFT tables of the reference, restated in double.
+ * Bit reversal over log2(N) bits: main.cpp:35-64 (reverse_bits) as used by
+ * generate_bit_reversed_indices() main.cpp:733-744. */
+void orc_bit_reversed(int N, int32_t* out)
+{
+    int lg = ilog2i(N);
+    for (int i = 0; i < N; ++i) {
+        int r = 0;
+        for (int b = 0; b < lg; ++b) r |= ((i >> b) & 1) << (lg - 1 - b);
+        out[i] = r;
+    }
+}
+
+/* Butterfly table twiddle_factors_cs.glsl:34-69: table[s][y] =
+ * (Re w, Im w, index p, index q) for stage s < log2(N), row y < N,
+ * w = exp(+2 pi i k / N), k = (y * N / 2^(s+1)) mod N.  out: log2N*N*4. */
+void orc_twiddle_table(int N, double* out)
+{
+    int      lg = ilog2i(N);
+    int32_t* br = (int32_t*)malloc(sizeof(int32_t) * N);
+    orc_bit_reversed(N, br);
+    for (int s = 0; s < lg; ++s)
+        for (int y = 0; y < N; ++y) {
+            long   span = 1L << s;
+            double k    = fmod((double)y * ((double)N / (double)(2L << s)), (double)N); /* :37 */
+            int    top  = (y % (2L << s)) < span;                                        /* :44 */
+            double* o   = out + 4 * ((size_t)s * N + y);
+            o[0] = cos(2.0 * ORC_PI * k / N);
+            o[1] = sin(2.0 * ORC_PI * k / N);
+            if (s == 0) {                                                                /* :50-58 */
+                o[2] = top ? br[y] : br[y - 1];
+                o[3] = top ? br[y + 1] : br[y];
+            } else {                                                                     /* :60-68 */
+                o[2] = top ? y : y - span;
+                o[3] = top ? y + span : y;
+            }
+        }
+    free(br);
+}
+
+/* ------------------------------------------------------------------------- */
+/* FP32 port of the reference algorithm (CPU baseline)                        */
+/* ------------------------------------------------------------------------- */
+
+typedef struct port_state {
+    orc_params p;
+    int        N, lg;
+    float*     h0;      /* N*N*4 */
+    float*     tw;      /* lg*N*4 (w.re, w.im, p, q) */
+    float*     spec;    /* 3 fields N*N*2 (the RGBA32F spectrum textures, .rg used) */
+    float*     pong;    /* N*N*2 ping-pong texture */
+    float*     raw;     /* 3 planes of inversion output */
+} port_state;
+
+/* tilde_h0_k_cs.glsl in FP32 (same pins as the oracle). */
+static void port_h0(port_state* s, const float* noise)
+{
+    const orc_params* p = &s->p;
+    int    N  = s->N;
+    size_t NN = (size_t)N * N;
+    float  wn = sqrtf((float)(p->wind_x * p->wind_x + p->wind_y * p->wind_y));
+    float  wx = (float)p->wind_x / wn, wy = (float)p->wind_y / wn;
+    float  Lp = (float)(p->wind_speed * p->wind_speed / p->gravity);
+    float  A = (float)p->amplitude, l = (float)p->suppression, L = (float)p->L;
+    const float PI = 3.14159265358979f;
+#pragma omp parallel for schedule(static)
+    for (int y = 0; y < N; ++y)
+        for (int x = 0; x < N; ++x) {
+            size_t i  = (size_t)y * N + x;
+            float  ix = (float)x - N / 2.0f, iz = (float)y - N / 2.0f;
+            float  kx = 2.0f * PI * ix / L, kz = 2.0f * PI * iz / L;
+            float  kl = sqrtf(kx * kx + kz * kz);
+            float  km = kl < 0.00001f ? 0.00001f : kl;
+            float  k2 = km * km;
+            float  a  = 0.0f;
+            if (!(ix == 0.0f && iz == 0.0f)) {
+                float kd = (kx * wx + kz * wy) / kl;
+                float P  = A * expf(-1.0f / (k2 * Lp * Lp)) * kd * kd * expf(-k2 * l * l) / (k2 * k2);
+                a        = sqrtf(P) / sqrtf(2.0f);
+                if (a > 4000.0f) a = 4000.0f;
+            }
+            float n[4];
+            for (int q = 0; q < 4; ++q) {
+                float v = noise[q * NN + i];
+                n[q]    = v < 0.001f ? 0.001f : (v > 1.0f ? 1.0f : v);
+            }
+            float u0 = 2.0f * PI * n[0], v0 = sqrtf(-2.0f * logf(n[1]));
+            float u1 = 2.0f * PI * n[2], v1 = sqrtf(-2.0f * logf(n[3]));
+            s->h0[4 * i + 0] = v0 * cosf(u0) * a;
+            s->h0[4 * i + 1] = v0 * sinf(u0) * a;
+            s->h0[4 * i + 2] = v1 * cosf(u1) * a;
+            s->h0[4 * i + 3] = v1 * sinf(u1) * a;
+        }
+}
+
+port_state* port_create(const orc_params* p, const float* noise)
+{
+    port_state* s = (port_state*)calloc(1, sizeof(port_state));
+    s->p  = *p;
+    s->N  = p->N;
+    s->lg = ilog2i(p->N);
+    size_t NN = (size_t)s->N * s->N;
+    s->h0   = (float*)malloc(NN * 4 * sizeof(float));
+    s->tw   = (float*)malloc((size_t)s->lg * s->N * 4 * sizeof(float));
+    s->spec = (float*)malloc(3 * NN * 2 * sizeof(float));
+    s->pong = (float*)malloc(NN * 2 * sizeof(float));
+    s->raw  = (float*)malloc(3 * NN * sizeof(float));
+    port_h0(s, noise);
+    /* twiddle texture, FP32 (twiddle_factors_cs.glsl is an FP32 shader) */
+    double* t64 = (double*)malloc((size_t)s->lg * s->N * 4 * sizeof(double));
+    orc_twiddle_table(s->N, t64);
+    for (size_t i = 0; i < (size_t)s->lg * s->N * 4; ++i) s->tw[i] = (float)t64[i];
+    free(t64);
+    return s;
+}
+
+void port_destroy(port_state* s)
+{
+    if (!s) return;
+    free(s->h0); free(s->tw); free(s->spec); free(s->pong); free(s->raw);
+    free(s);
+}
+
+/* tilde_h0_t_cs.glsl:70-131 in FP32 with FP32 time (main.cpp:599). */
+static void port_spectrum(port_state* s, float t)
+{
+    int    N  = s->N;
+    size_t NN = (size_t)N * N;
+    float  L = (float)s->p.L, g = (float)s->p.gravity;
+    int    lit = s->p.literal_conj;
+    const float PI = 3.14159265358979f;
+#pragma omp parallel for schedule(static)
+    for (int y = 0; y < N; ++y)
+        for (int x = 0; x < N; ++x) {
+            size_t i  = (size_t)y * N + x;
+            float  kx = 2.0f * PI * ((float)x - N / 2.0f) / L, kz = 2.0f * PI * ((float)y - N / 2.0f) / L;
+            float  km = sqrtf(kx * kx + kz * kz);
+            if (km < 0.00001f) km = 0.00001f;
+            float w = sqrtf(g * km);
+            float c = cosf(w * t), sn = sinf(w * t);
+            float ar = s->h0[4 * i], ai = s->h0[4 * i + 1], br = s->h0[4 * i + 2], bi = s->h0[4 * i + 3];
+            if (!lit) bi = -bi;
+            float hr = ar * c - ai * sn + br * c + bi * sn;
+            float hi = ar * sn + ai * c - br * sn + bi * c;
+            float fx = -kx / km, fz = -kz / km;
+            s->spec[2 * (0 * NN + i)] = -fx * hi; s->spec[2 * (0 * NN + i) + 1] = fx * hr;
+            s->spec[2 * (1 * NN + i)] = hr;       s->spec[2 * (1 * NN + i) + 1] = hi;
+            s->spec[2 * (2 * NN + i)] = -fz * hi; s->spec[2 * (2 * NN + i) + 1] = fz * hr;
+        }
+}
+
+/* butterfly_fft() main.cpp:612-683: log2N horizontal then log2N vertical
+ * radix-2 passes (butterfly_cs.glsl:54-132), ping-pong between the spectrum
+ * texture and one scratch texture, then inversion_cs.glsl into `out`. */
+static void port_butterfly_fft(port_state* s, float* tex, float* out)
+{
+    int    N = s->N;
+    float* buf[2] = { tex, s->pong };
+    int    pp = 0;
+    for (int dir = 0; dir < 2; ++dir)
+        for (int st = 0; st < s->lg; ++st) {
+            const float* src = buf[pp];
+            float*       dst = buf[pp ^ 1];
+#pragma omp parallel for schedule(static)
+            for (int y = 0; y < N; ++y)
+                for (int x = 0; x < N; ++x) {
+                    const float* d = s->tw + 4 * ((size_t)st * N + (dir == 0 ? x : y));
+                    int ip = (int)d[2], iq = (int)d[3];
+                    size_t a = dir == 0 ? (size_t)y * N + ip : (size_t)ip * N + x;
+                    size_t b = dir == 0 ? (size_t)y * N + iq : (size_t)iq * N + x;
+                    float pr = src[2 * a], pi = src[2 * a + 1], qr = src[2 * b], qi = src[2 * b + 1];
+                    dst[2 * ((size_t)y * N + x)]     = pr + (d[0] * qr - d[1] * qi);
+                    dst[2 * ((size_t)y * N + x) + 1] = pi + (d[0] * qi + d[1] * qr);
+                }
+            pp ^= 1;
+        }
+    const float* res = buf[pp];
+    float        inv = 1.0f / (float)(N * N);
+#pragma omp parallel for schedule(static)
+    for (int y = 0; y < N; ++y)
+        for (int x = 0; x < N; ++x) {
+            float perm = ((x + y) & 1) ? -1.0f : 1.0f;          /* inversion_cs.glsl:29-31 */
+            out[(size_t)y * N + x] = perm * (res[2 * ((size_t)y * N + x)] * inv);
+        }
+}
+
+/* One frame of the reference algorithm (main.cpp:240-244) plus the lambda /
+ * Jacobian additions, FP32.  Outputs as orc_finish. */
+void port_frame(port_state* s, float t, float* dx, float* dy, float* dz, float* nj)
+{
+    int    N  = s->N;
+    size_t NN = (size_t)N * N;
+    port_spectrum(s, t);
+    port_butterfly_fft(s, s->spec + 2 * NN, s->raw + NN);   /* dy */
+    port_butterfly_fft(s, s->spec + 0, s->raw);             /* dx */
+    port_butterfly_fft(s, s->spec + 4 * NN, s->raw + 2 * NN); /* dz */
+    float lam = (float)s->p.choppiness, inv2d = (float)N / (2.0f * (float)s->p.L);
+    const float* rx = s->raw;
+    const float* ry = s->raw + NN;
+    const float* rz = s->raw + 2 * NN;
+#pragma omp parallel for schedule(static)
+    for (int y = 0; y < N; ++y) {
+        int ym = (y + N - 1) % N, yp = (y + 1) % N;
+        for (int x = 0; x < N; ++x) {
+            int    xm = (x + N - 1) % N, xp = (x + 1) % N;
+            size_t i  = (size_t)y * N + x;
+            float z0 = ry[ym * N + xm], z1 = ry[ym * N + x], z2 = ry[ym * N + xp];
+            float z3 = ry[y * N + xm], z4 = ry[y * N + xp];
+            float z5 = ry[yp * N + xm], z6 = ry[yp * N + x], z7 = ry[yp * N + xp];
+            float nz = z0 + 2 * z1 + z2 - z5 - 2 * z6 - z7;
+            float nx = z0 + 2 * z3 + z5 - z2 - 2 * z4 - z7;
+            float rn = 1.0f / sqrtf(nx * nx + 1.0f + nz * nz);
+            float dxx = lam * (rx[y * N + xp] - rx[y * N + xm]) * inv2d;
+            float dxz = lam * (rx[yp * N + x] - rx[ym * N + x]) * inv2d;
+            float dzx = lam * (rz[y * N + xp] - rz[y * N + xm]) * inv2d;
+            float dzz = lam * (rz[yp * N + x] - rz[ym * N + x]) * inv2d;
+            dx[i] = lam * rx[i];
+            dy[i] = ry[i];
+            dz[i] = lam * rz[i];
+            nj[4 * i + 0] = nx * rn;
+            nj[4 * i + 1] = rn;
+            nj[4 * i + 2] = nz * rn;
+            nj[4 * i + 3] = (1.0f - dxx) * (1.0f - dzz) - dxz * dzx;
+        }
+    }
+}
+
+const float* port_h0_ptr(const port_state* s) { return s->h0; }
+
+int port_max_threads(void)
+{
+#ifdef _OPENMP
+    return omp_get_max_threads();
+#else
+    return 1;
+#endif
+}
+
+void port_set_threads(int n)
+{
+#ifdef _OPENMP
+    if (n > 0) omp_set_num_threads(n);
+#else
+    (void)n;
+#endif
+}

@@ -1,0 +1,241 @@
+"""Python face of the oracle -- TEST INFRASTRUCTURE ONLY.
+
+Loads oracle/_build/libocean_oracle.so (built by oracle/build_oracle.py) and
+exposes the FP64 restatement of the reference ocean path (``h0``,
+``spectrum``, ``update``, FFT tables) and the FP32 port of the reference
+algorithm (``Port``), plus the seeded noise generator shared with the CUDA
+library.  Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg
+import this module.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import dataclasses
+import math
+import os
+
+import numpy as np
+
+from . import build_oracle
+
+_LIB = None
+
+
+class _OrcParams(C.Structure):
+    _fields_ = [("N", C.c_int32), ("literal_conj", C.c_int32), ("L", C.c_double),
+                ("amplitude", C.c_double), ("wind_speed", C.c_double),
+                ("wind_x", C.c_double), ("wind_y", C.c_double),
+                ("choppiness", C.c_double), ("suppression", C.c_double),
+                ("gravity", C.c_double)]
+
+
+@dataclasses.dataclass
+class Params:
+    """Spectrum parameters of one ocean tile (the reference's uniforms,
+    main.cpp:1631-1646 and tilde_h0_k_cs.glsl:19-24)."""
+    N: int = 256
+    L: float = 1000.0
+    amplitude: float = 2.0
+    wind_speed: float = 80.0
+    wind_x: float = 1.0
+    wind_y: float = 1.0
+    choppiness: float = 0.75
+    suppression: float = 0.1
+    gravity: float = 9.81
+    literal_conj: bool = False
+
+    @staticmethod
+    def from_angle(N, L, amplitude, wind_speed, angle_deg, choppiness, suppression=0.1, **kw):
+        a = math.radians(angle_deg)
+        return Params(N=N, L=L, amplitude=amplitude, wind_speed=wind_speed,
+                      wind_x=math.cos(a), wind_y=math.sin(a), choppiness=choppiness,
+                      suppression=suppression, **kw)
+
+    def _c(self) -> _OrcParams:
+        return _OrcParams(self.N, int(self.literal_conj), self.L, self.amplitude, self.wind_speed,
+                          self.wind_x, self.wind_y, self.choppiness, self.suppression, self.gravity)
+
+
+def lib():
+    global _LIB
+    if _LIB is None:
+        path = build_oracle.build()
+        L = C.CDLL(path)
+        dp = C.POINTER(C.c_double)
+        fp = C.POINTER(C.c_float)
+        pp = C.POINTER(_OrcParams)
+        L.orc_h0.argtypes = [pp, fp, dp]
+        L.orc_spectrum.argtypes = [pp, dp, C.c_double, dp]
+        L.orc_ifft2_real.argtypes = [C.c_int, dp, dp]
+        L.orc_finish.argtypes = [pp, dp, dp, dp, dp, dp]
+        L.orc_update.argtypes = [pp, dp, C.c_double, dp, dp, dp, dp]
+        L.orc_bit_reversed.argtypes = [C.c_int, C.POINTER(C.c_int32)]
+        L.orc_twiddle_table.argtypes = [C.c_int, dp]
+        L.orc_count_clamped.argtypes = [pp]
+        L.orc_count_clamped.restype = C.c_int
+        L.port_create.argtypes = [pp, fp]
+        L.port_create.restype = C.c_void_p
+        L.port_destroy.argtypes = [C.c_void_p]
+        L.port_frame.argtypes = [C.c_void_p, C.c_float, fp, fp, fp, fp]
+        L.port_h0_ptr.argtypes = [C.c_void_p]
+        L.port_h0_ptr.restype = fp
+        L.port_max_threads.restype = C.c_int
+        L.port_set_threads.argtypes = [C.c_int]
+        _LIB = L
+    return _LIB
+
+
+def _p(a, ct):
+    return a.ctypes.data_as(C.POINTER(ct))
+
+
+# ---------------------------------------------------------------------------
+# Seeded noise: splitmix64 (Steele, Lea & Flood 2014) -> 24-bit uniforms in
+# (0, 1].  The i-th draw of a stream seeded with s uses state s + (i+1)*gamma.
+# Plane order [4][N][N]; planes 0/1 feed h0k, 2/3 feed h0minusk.
+# ---------------------------------------------------------------------------
+_GAMMA = np.uint64(0x9E3779B97F4A7C15)
+
+
+def splitmix64(seed: int, count: int) -> np.ndarray:
+    with np.errstate(over="ignore"):
+        i = np.arange(1, count + 1, dtype=np.uint64)
+        z = np.uint64(seed & 0xFFFFFFFFFFFFFFFF) + i * _GAMMA
+        z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+        z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+        z = z ^ (z >> np.uint64(31))
+    return z
+
+
+def noise(seed: int, N: int) -> np.ndarray:
+    """Four N x N planes of U(0,1] float32 noise for tile seed `seed`."""
+    z = splitmix64(seed, 4 * N * N)
+    u = ((z >> np.uint64(40)).astype(np.float64) + 1.0) * (2.0 ** -24)
+    return u.astype(np.float32).reshape(4, N, N)
+
+
+# ---------------------------------------------------------------------------
+# FP64 oracle
+# ---------------------------------------------------------------------------
+
+def h0(p: Params, nz: np.ndarray) -> np.ndarray:
+    nz = np.ascontiguousarray(nz, dtype=np.float32)
+    assert nz.shape == (4, p.N, p.N)
+    out = np.empty((p.N, p.N, 4), dtype=np.float64)
+    cp = p._c()
+    lib().orc_h0(C.byref(cp), _p(nz, C.c_float), _p(out, C.c_double))
+    return out
+
+
+def count_clamped(p: Params) -> int:
+    cp = p._c()
+    return lib().orc_count_clamped(C.byref(cp))
+
+
+def spectrum(p: Params, h0a: np.ndarray, t: float) -> np.ndarray:
+    """(3, N, N) complex128 spectra (Dx, Dy, Dz) at time t."""
+    h0a = np.ascontiguousarray(h0a, dtype=np.float64)
+    out = np.empty((3, p.N, p.N, 2), dtype=np.float64)
+    cp = p._c()
+    lib().orc_spectrum(C.byref(cp), _p(h0a, C.c_double), float(t), _p(out, C.c_double))
+    return out[..., 0] + 1j * out[..., 1]
+
+
+def update(p: Params, h0a: np.ndarray, t: float) -> dict:
+    """One frame: dict of dx, dy, dz (N, N) and nj (N, N, 4), float64."""
+    h0a = np.ascontiguousarray(h0a, dtype=np.float64)
+    N = p.N
+    dx, dy, dz = (np.empty((N, N)) for _ in range(3))
+    nj = np.empty((N, N, 4))
+    cp = p._c()
+    lib().orc_update(C.byref(cp), _p(h0a, C.c_double), float(t), _p(dx, C.c_double),
+                     _p(dy, C.c_double), _p(dz, C.c_double), _p(nj, C.c_double))
+    return {"dx": dx, "dy": dy, "dz": dz, "nj": nj}
+
+
+def finish(p: Params, raw: np.ndarray) -> dict:
+    """Output stage (lambda, Sobel normal, Jacobian) from raw (3, N, N)."""
+    raw = np.ascontiguousarray(raw, dtype=np.float64)
+    N = p.N
+    dx, dy, dz = (np.empty((N, N)) for _ in range(3))
+    nj = np.empty((N, N, 4))
+    cp = p._c()
+    lib().orc_finish(C.byref(cp), _p(raw, C.c_double), _p(dx, C.c_double), _p(dy, C.c_double),
+                     _p(dz, C.c_double), _p(nj, C.c_double))
+    return {"dx": dx, "dy": dy, "dz": dz, "nj": nj}
+
+
+def ifft2_real(spec_f: np.ndarray) -> np.ndarray:
+    N = spec_f.shape[0]
+    a = np.ascontiguousarray(np.stack([spec_f.real, spec_f.imag], -1), dtype=np.float64)
+    out = np.empty((N, N))
+    lib().orc_ifft2_real(N, _p(a, C.c_double), _p(out, C.c_double))
+    return out
+
+
+def bit_reversed(N: int) -> np.ndarray:
+    out = np.empty(N, dtype=np.int32)
+    lib().orc_bit_reversed(N, _p(out, C.c_int32))
+    return out
+
+
+def twiddle_table(N: int) -> np.ndarray:
+    lg = N.bit_length() - 1
+    out = np.empty((lg, N, 4))
+    lib().orc_twiddle_table(N, _p(out, C.c_double))
+    return out
+
+
+# ---------------------------------------------------------------------------
+# FP32 port of the reference algorithm (CPU baseline)
+# ---------------------------------------------------------------------------
+
+class Port:
+    """The reference's per-frame algorithm in FP32 C with OpenMP: spectrum
+    pass, 2*log2(N) table-driven radix-2 ping-pong passes per field,
+    inversion, Sobel normal map (main.cpp:240-244)."""
+
+    def __init__(self, p: Params, nz: np.ndarray):
+        self.p = p
+        nz = np.ascontiguousarray(nz, dtype=np.float32)
+        cp = p._c()
+        self._s = lib().port_create(C.byref(cp), _p(nz, C.c_float))
+        N = p.N
+        self.dx, self.dy, self.dz = (np.empty((N, N), np.float32) for _ in range(3))
+        self.nj = np.empty((N, N, 4), np.float32)
+
+    def h0(self) -> np.ndarray:
+        N = self.p.N
+        ptr = lib().port_h0_ptr(self._s)
+        return np.ctypeslib.as_array(ptr, shape=(N, N, 4)).copy()
+
+    def frame(self, t: float) -> dict:
+        lib().port_frame(self._s, float(t), _p(self.dx, C.c_float), _p(self.dy, C.c_float),
+                         _p(self.dz, C.c_float), _p(self.nj, C.c_float))
+        return {"dx": self.dx, "dy": self.dy, "dz": self.dz, "nj": self.nj}
+
+    def close(self):
+        if self._s:
+            lib().port_destroy(self._s)
+            self._s = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def max_threads() -> int:
+    return lib().port_max_threads()
+
+
+def set_threads(n: int) -> None:
+    lib().port_set_threads(int(n))
+
+
+def rel_l2(a, b) -> float:
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    den = np.linalg.norm(b.ravel())
+    return float(np.linalg.norm((a - b).ravel()) / (den if den > 0 else 1.0))

@@ -1,0 +1,104 @@
+"""GPU parity: the CUDA path through the C ABI against the FP64 oracle on the
+same seeded noise.  Tolerance: relative L2 <= 1e-5 per output field (Dx, Dy,
+Dz, normal xyz, Jacobian) and <= 1e-6 for h0."""
+import math
+
+import numpy as np
+import pytest
+
+from conftest import rel_l2
+import params as P
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-5
+
+
+@pytest.fixture(scope="module")
+def torch_cuda():
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    return torch
+
+
+def _run(torch, ocean_lib, d, times, literal=False):
+    """Create the tile through the C ABI, run frames, return host copies."""
+    N = d["N"]
+    lp = P.lib_params(d, literal_conj=literal)
+    dev = torch.device("cuda")
+    outs = []
+    with ocean_lib.Ocean(lp, seed=d["seed"]) as oc:
+        h0 = torch.empty((N, N, 4), dtype=torch.float32, device=dev)
+        oc.get_h0(h0)
+        dx, dy, dz = (torch.empty((N, N), dtype=torch.float32, device=dev) for _ in range(3))
+        nj = torch.empty((N, N, 4), dtype=torch.float32, device=dev)
+        for t in times:
+            oc.update(t, dx, dy, dz, nj)
+            torch.cuda.synchronize()
+            outs.append({"dx": dx.cpu().numpy().copy(), "dy": dy.cpu().numpy().copy(),
+                         "dz": dz.cpu().numpy().copy(), "nj": nj.cpu().numpy().copy()})
+        h0h = h0.cpu().numpy()
+    return h0h, outs
+
+
+def _check(o, ref, tol=TOL):
+    errs = {k: rel_l2(o[k], ref[k]) for k in ("dx", "dy", "dz")}
+    errs["normal"] = rel_l2(o["nj"][..., :3], ref["nj"][..., :3])
+    errs["J"] = rel_l2(o["nj"][..., 3] - 1.0, ref["nj"][..., 3] - 1.0)
+    bad = {k: v for k, v in errs.items() if not v <= tol}
+    assert not bad, errs
+    return errs
+
+
+@pytest.mark.parametrize("N", [32, 64, 128, 256, 512, 1024, 2048])
+def test_parity_sizes(torch_cuda, ocean_lib, oracle_mod, N):
+    d = P.c2(N)
+    p = P.oracle_params(d)
+    h0ref = oracle_mod.h0(p, oracle_mod.noise(d["seed"], N))
+    times = [0.0, 1.0 / 60.0, 7.25]
+    h0g, outs = _run(torch_cuda, ocean_lib, d, times)
+    assert rel_l2(h0g, h0ref) < 1e-6
+    for t, o in zip(times, outs):
+        _check(o, oracle_mod.update(p, h0ref, t))
+
+
+def test_parity_c1(torch_cuda, ocean_lib, oracle_mod):
+    """The N=256 configuration at t = 1 s."""
+    d = P.c1()
+    p = P.oracle_params(d)
+    h0ref = oracle_mod.h0(p, oracle_mod.noise(d["seed"], d["N"]))
+    h0g, outs = _run(torch_cuda, ocean_lib, d, [1.0])
+    assert rel_l2(h0g, h0ref) < 1e-6
+    _check(outs[0], oracle_mod.update(p, h0ref, 1.0))
+
+
+def test_parity_literal_conj(torch_cuda, ocean_lib, oracle_mod):
+    """OCEAN_FLAG_LITERAL_CONJ reproduces the shader's no-op conjugate()."""
+    d = P.c1()
+    p = P.oracle_params(d, literal_conj=True)
+    h0ref = oracle_mod.h0(p, oracle_mod.noise(d["seed"], d["N"]))
+    _, outs = _run(torch_cuda, ocean_lib, d, [1.0, 33.3], literal=True)
+    _check(outs[0], oracle_mod.update(p, h0ref, 1.0))
+    _check(outs[1], oracle_mod.update(p, h0ref, 33.3))
+
+
+@pytest.mark.parametrize("N", [512, 1024])
+def test_phase_precision_large_t(torch_cuda, ocean_lib, oracle_mod, N):
+    """t = 1e5 s: FP32 w*t would be off by ~0.03 rad; the double-float phase
+    keeps the FP64-oracle tolerance."""
+    d = P.c2(N)
+    p = P.oracle_params(d)
+    h0ref = oracle_mod.h0(p, oracle_mod.noise(d["seed"], N))
+    _, outs = _run(torch_cuda, ocean_lib, d, [1e5, 1e5 + 1.0 / 60.0])
+    _check(outs[0], oracle_mod.update(p, h0ref, 1e5))
+    _check(outs[1], oracle_mod.update(p, h0ref, 1e5 + 1.0 / 60.0))
+
+
+def test_reference_defaults(torch_cuda, ocean_lib, oracle_mod):
+    """The reference demo's own parameters (V=80, A=2, L=1000, N=256)."""
+    d = P.reference_default(256)
+    p = P.oracle_params(d)
+    h0ref = oracle_mod.h0(p, oracle_mod.noise(d["seed"], 256))
+    _, outs = _run(torch_cuda, ocean_lib, d, [12.5])
+    _check(outs[0], oracle_mod.update(p, h0ref, 12.5))
