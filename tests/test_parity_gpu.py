@@ -102,3 +102,25 @@ def test_reference_defaults(torch_cuda, ocean_lib, oracle_mod):
     h0ref = oracle_mod.h0(p, oracle_mod.noise(d["seed"], 256))
     _, outs = _run(torch_cuda, ocean_lib, d, [12.5])
     _check(outs[0], oracle_mod.update(p, h0ref, 12.5))
+
+
+@pytest.mark.parametrize("name", ["ref_frame_N32", "ref_frame_N64"])
+def test_matches_reference_shader_golden(torch_cuda, ocean_lib, name):
+    """The CUDA path in literal-conjugate mode with lambda = 1 against frames the
+    reference's own compute shaders produced (tests/golden/make_golden.py)."""
+    import json
+    import os
+    from conftest import ROOT
+    z = np.load(os.path.join(ROOT, "tests", "golden", name + ".npz"))
+    meta = json.loads(str(z["meta"]))
+    d = dict(N=meta["N"], L=float(meta["L"]), amplitude=meta["A"], wind_speed=meta["V"], wind_x=meta["wx"],
+             wind_y=meta["wy"], choppiness=1.0, suppression=meta["l"], seed=meta["seed"])
+    h0g, outs = _run(torch_cuda, ocean_lib, d, [float(t) for t in z["times"]], literal=True)
+    N = d["N"]
+    g = np.concatenate([z["h0k"], z["h0minusk"]], -1).astype(np.float64)
+    g[N // 2, N // 2] = 0.0
+    assert rel_l2(h0g, g) < 2e-6
+    for i, o in enumerate(outs):
+        for k in ("dx", "dy", "dz"):
+            assert rel_l2(o[k], z[f"{k}_{i}"]) < 1e-5, k
+        assert rel_l2(o["nj"][..., :3], z[f"normal_{i}"][..., :3]) < 1e-5
