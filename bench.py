@@ -179,7 +179,9 @@ def parity_check(N, gpu_frame, t):
     ref = oracle.update(p, h, t)
     errs = {k: oracle.rel_l2(gpu_frame[k], ref[k]) for k in ("dx", "dy", "dz")}
     errs["normal"] = oracle.rel_l2(gpu_frame["nj"][..., :3], ref["nj"][..., :3])
-    errs["J"] = oracle.rel_l2(gpu_frame["nj"][..., 3] - 1, ref["nj"][..., 3] - 1)
+    errs["J"] = oracle.rel_l2(gpu_frame["nj"][..., 3], ref["nj"][..., 3])
+    errs["J_max_abs"] = float(np.abs(gpu_frame["nj"][..., 3].astype(np.float64) - ref["nj"][..., 3]).max())
+    errs["dy_max_abs"] = float(np.abs(gpu_frame["dy"].astype(np.float64) - ref["dy"]).max())
     return {k: float(f"{v:.3g}") for k, v in errs.items()}
 
 

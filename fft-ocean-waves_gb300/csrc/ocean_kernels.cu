@@ -292,7 +292,10 @@ __global__ void __launch_bounds__(ColCfg<N>::THREADS) k_col_pass(ColArgs a)
         a.dx[o] = vx;
         a.dy[o] = zc;
         a.dz[o] = vz;
-        a.nj[o] = make_float4(nx * rn, rn, nz * rn, (1.0f - dxx) * (1.0f - dzz) - dxz * dzx);
+        // J = (1 - dxx)(1 - dzz) - dxz*dzx, formed as 1 + deviation so that the
+        // only rounding at the scale of 1 is the final add
+        const float dJ = (dxx * dzz - dxz * dzx) - dxx - dzz;
+        a.nj[o] = make_float4(nx * rn, rn, nz * rn, 1.0f + dJ);
     }
 }
 
