@@ -48,9 +48,10 @@ def _check(o, ref, tol=TOL):
     errs["J"] = rel_l2(o["nj"][..., 3], ref["nj"][..., 3])
     bad = {k: v for k, v in errs.items() if not v <= tol}
     assert not bad, errs
-    # J sits near 1, where FP32 resolves 6e-8: bound its absolute error too
-    dj = np.abs(o["nj"][..., 3].astype(np.float64) - ref["nj"][..., 3]).max()
-    assert dj < 5e-7, dj
+    # J is O(1): bound its absolute error by a few FP32 ulps of its magnitude too
+    jref = ref["nj"][..., 3]
+    dj = np.abs(o["nj"][..., 3].astype(np.float64) - jref).max()
+    assert dj < 5e-7 * max(1.0, float(np.abs(jref).max())), dj
     return errs
 
 
