@@ -206,7 +206,7 @@ def run_gpu(args, world, rank, local):
 
     def flush():
         fl_w.zero_()
-        torch.sum(fl_r, dtype=torch.float32, out=fl_sink)
+        torch.sum(fl_r, dim=(0,), out=fl_sink)
 
     launches = 0
     with torch.cuda.stream(stream):

@@ -263,6 +263,102 @@ void orc_update(const orc_params* p, const double* h0, double t, double* dx, dou
     free(raw);
 }
 
+/* FP64 adjoint of orc_update's displacement outputs (Dx, Dy, Dz) over T
+ * frames.  The loss gradient is given per frame as g_dx, g_dy, g_dz
+ * (T*N*N each, NULL = zero).  Outputs:
+ *   dh0    N*N*4: dL/dh0 per mode in the complex convention dL/dRe + i dL/dIm
+ *          for (h0k, h0minusk), summed over the frames;
+ *   grads  [0] dL/dA, [1] dL/dV, [2] dL/dtheta (wind direction angle),
+ *          [3] dL/dlambda.  The suppression length l, L and g are constants;
+ *          modes on the +-4000 clamp and the DC mode do not depend on A, V,
+ *          theta.
+ * Steps per frame: forward 2-D DFT of (-1)^(x+y)/N^2 * g (the transpose of
+ * the inverse butterfly network + inversion), transpose of the choppy
+ * multiply, conjugate phase rotation. */
+void orc_backward(const orc_params* p, const double* h0, const double* times, int T, const double* g_dx,
+                  const double* g_dy, const double* g_dz, double* dh0, double* grads)
+{
+    int     N  = p->N;
+    size_t  NN = (size_t)N * N;
+    double* G  = (double*)malloc(3 * 2 * NN * sizeof(double));
+    double  lam = p->choppiness, dlam = 0.0;
+    memset(dh0, 0, NN * 4 * sizeof(double));
+    for (int j = 0; j < T; ++j) {
+        const double* gs[3] = { g_dx ? g_dx + j * NN : NULL, g_dy ? g_dy + j * NN : NULL, g_dz ? g_dz + j * NN : NULL };
+        for (int f = 0; f < 3; ++f) {
+            double* a = G + f * 2 * NN;
+            for (int y = 0; y < N; ++y)
+                for (int x = 0; x < N; ++x) {
+                    size_t i = (size_t)y * N + x;
+                    double s = (((x + y) & 1) ? -1.0 : 1.0) / ((double)N * N);
+                    a[2 * i]     = gs[f] ? s * gs[f][i] : 0.0;
+                    a[2 * i + 1] = 0.0;
+                }
+            for (int y = 0; y < N; ++y) orc_fft1(a + 2 * (size_t)y * N, N, 1, -1);
+            for (int x = 0; x < N; ++x) orc_fft1(a + 2 * (size_t)x, N, N, -1);
+        }
+        double t = times[j];
+        for (int y = 0; y < N; ++y)
+            for (int x = 0; x < N; ++x) {
+                size_t i  = (size_t)y * N + x;
+                double kx = 2.0 * ORC_PI * (x - N / 2.0) / p->L, kz = 2.0 * ORC_PI * (y - N / 2.0) / p->L;
+                double km = sqrt(kx * kx + kz * kz);
+                if (km < 0.00001) km = 0.00001;
+                double w = sqrt(p->gravity * km), c = cos(w * t), s = sin(w * t);
+                double gxr = G[2 * i], gxi = G[2 * i + 1];
+                double gyr = G[2 * (NN + i)], gyi = G[2 * (NN + i) + 1];
+                double gzr = G[2 * (2 * NN + i)], gzi = G[2 * (2 * NN + i) + 1];
+                double ux = kx / km, uz = kz / km;           /* conj(a_x) = +i ux, conj(a_z) = +i uz */
+                double tr = gyr + lam * (-ux * gxi - uz * gzi);
+                double ti = gyi + lam * (ux * gxr + uz * gzr);
+                /* dh0k += e^{-iwt} Gtot */
+                dh0[4 * i + 0] += tr * c + ti * s;
+                dh0[4 * i + 1] += ti * c - tr * s;
+                if (!p->literal_conj) { /* dh0mk += conj(Gtot) e^{-iwt} */
+                    dh0[4 * i + 2] += tr * c - ti * s;
+                    dh0[4 * i + 3] += -ti * c - tr * s;
+                } else {                /* dh0mk += e^{+iwt} Gtot */
+                    dh0[4 * i + 2] += tr * c - ti * s;
+                    dh0[4 * i + 3] += ti * c + tr * s;
+                }
+                /* dlambda: Re(conj(Gx) Xx + conj(Gz) Xz), Xx = -i ux Xy, Xz = -i uz Xy */
+                double ar = h0[4 * i], ai = h0[4 * i + 1], br = h0[4 * i + 2], bi = h0[4 * i + 3];
+                if (!p->literal_conj) bi = -bi;
+                double hr = ar * c - ai * s + br * c + bi * s;
+                double hi = ar * s + ai * c - br * s + bi * c;
+                double xxr = ux * hi, xxi = -ux * hr, xzr = uz * hi, xzi = -uz * hr;
+                dlam += gxr * xxr + gxi * xxi + gzr * xzr + gzi * xzi;
+            }
+    }
+    free(G);
+    /* chain through a(k) = clamp(sqrt(P)/sqrt2): h0 = xi * a with fixed noise xi */
+    double wn = sqrt(p->wind_x * p->wind_x + p->wind_y * p->wind_y);
+    double wx = p->wind_x / wn, wy = p->wind_y / wn;
+    double Lp = p->wind_speed * p->wind_speed / p->gravity;
+    double dA = 0.0, dV = 0.0, dth = 0.0;
+    for (int y = 0; y < N; ++y)
+        for (int x = 0; x < N; ++x) {
+            double ix = x - N / 2.0, iz = y - N / 2.0;
+            if (ix == 0.0 && iz == 0.0) continue;
+            size_t i  = (size_t)y * N + x;
+            double kx = 2.0 * ORC_PI * ix / p->L, kz = 2.0 * ORC_PI * iz / p->L;
+            int    cl = 0;
+            double a  = orc_amp(p, kx, kz, wx, wy, &cl);
+            if (cl || a == 0.0) continue;
+            double Q = dh0[4 * i] * h0[4 * i] + dh0[4 * i + 1] * h0[4 * i + 1] + dh0[4 * i + 2] * h0[4 * i + 2] +
+                       dh0[4 * i + 3] * h0[4 * i + 3];      /* a * dL/da */
+            double kl = sqrt(kx * kx + kz * kz);
+            double cdir = (kx * wx + kz * wy) / kl, cperp = (-kx * wy + kz * wx) / kl;
+            dA  += Q / (2.0 * p->amplitude);
+            dV  += Q * 2.0 * p->wind_speed / (p->gravity * kl * kl * Lp * Lp * Lp);
+            dth += Q * cperp / cdir;
+        }
+    grads[0] = dA;
+    grads[1] = dV;
+    grads[2] = dth;
+    grads[3] = dlam;
+}
+
 /* FFT tables of the reference, restated in double.
  * Bit reversal over log2(N) bits: main.cpp:35-64 (reverse_bits) as used by
  * generate_bit_reversed_indices() main.cpp:733-744. */

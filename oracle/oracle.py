@@ -69,6 +69,7 @@ def lib():
         L.orc_ifft2_real.argtypes = [C.c_int, dp, dp]
         L.orc_finish.argtypes = [pp, dp, dp, dp, dp, dp]
         L.orc_update.argtypes = [pp, dp, C.c_double, dp, dp, dp, dp]
+        L.orc_backward.argtypes = [pp, dp, dp, C.c_int, dp, dp, dp, dp, dp]
         L.orc_bit_reversed.argtypes = [C.c_int, C.POINTER(C.c_int32)]
         L.orc_twiddle_table.argtypes = [C.c_int, dp]
         L.orc_count_clamped.argtypes = [pp]
@@ -171,6 +172,23 @@ def ifft2_real(spec_f: np.ndarray) -> np.ndarray:
     out = np.empty((N, N))
     lib().orc_ifft2_real(N, _p(a, C.c_double), _p(out, C.c_double))
     return out
+
+
+def backward(p: Params, h0a: np.ndarray, times, g_dx=None, g_dy=None, g_dz=None):
+    """FP64 adjoint: returns (dh0 (N, N, 4), dict(dA, dV, dtheta, dlambda)) for
+    upstream gradients g_* of shape (T, N, N) (None = zero)."""
+    h0a = np.ascontiguousarray(h0a, dtype=np.float64)
+    ts = np.ascontiguousarray(np.atleast_1d(times), dtype=np.float64)
+    T = len(ts)
+    gs = [None if g is None else np.ascontiguousarray(np.reshape(g, (T, p.N, p.N)), dtype=np.float64)
+          for g in (g_dx, g_dy, g_dz)]
+    dh0 = np.empty((p.N, p.N, 4))
+    gr = np.empty(4)
+    cp = p._c()
+    lib().orc_backward(C.byref(cp), _p(h0a, C.c_double), _p(ts, C.c_double), T,
+                       *[(_p(g, C.c_double) if g is not None else None) for g in gs],
+                       _p(dh0, C.c_double), _p(gr, C.c_double))
+    return dh0, {"dA": gr[0], "dV": gr[1], "dtheta": gr[2], "dlambda": gr[3]}
 
 
 def bit_reversed(N: int) -> np.ndarray:

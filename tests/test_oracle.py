@@ -217,3 +217,49 @@ def test_tables(oracle_mod):
             b[i] = a[int(T[s, i, 2])] + w * a[int(T[s, i, 3])]
         a = b
     assert np.abs(a - np.fft.ifft(x) * N).max() < 1e-12
+
+
+@pytest.mark.parametrize("literal", [False, True])
+def test_oracle_adjoint_matches_finite_differences(oracle_mod, literal):
+    """FP64 adjoint (orc_backward) against central finite differences of the
+    FP64 forward, for L = sum_t sum_f <g_f(t), D_f(t)> with fixed random g."""
+    N = 16
+    base = dict(N=N, L=800.0, amplitude=3.0, wind_speed=22.0, wind_x=math.cos(0.9), wind_y=math.sin(0.9),
+                choppiness=1.1, suppression=0.1, literal_conj=literal)
+    nz = oracle_mod.noise(3, N)
+    times = [0.3, 1.7, 4.0]
+    rng = np.random.default_rng(0)
+    g = [rng.standard_normal((3, N, N)) for _ in range(3)]
+
+    def loss(prm, h=None):
+        p = oracle_mod.Params(**prm)
+        hh = oracle_mod.h0(p, nz) if h is None else h
+        s = 0.0
+        for j, t in enumerate(times):
+            o = oracle_mod.update(p, hh, t)
+            s += np.sum(g[0][j] * o["dx"]) + np.sum(g[1][j] * o["dy"]) + np.sum(g[2][j] * o["dz"])
+        return s
+
+    p = oracle_mod.Params(**base)
+    h = oracle_mod.h0(p, nz)
+    dh0, gr = oracle_mod.backward(p, h, times, *g)
+    for name, key in (("dA", "amplitude"), ("dV", "wind_speed"), ("dlambda", "choppiness")):
+        e = 1e-5 * base[key]
+        a, b = dict(base), dict(base)
+        a[key] += e
+        b[key] -= e
+        fd = (loss(a) - loss(b)) / (2 * e)
+        assert abs(fd - gr[name]) <= 1e-6 * abs(fd), (name, fd, gr[name])
+    e = 1e-6
+    a, b = dict(base), dict(base)
+    a["wind_x"], a["wind_y"] = math.cos(0.9 + e), math.sin(0.9 + e)
+    b["wind_x"], b["wind_y"] = math.cos(0.9 - e), math.sin(0.9 - e)
+    fd = (loss(a) - loss(b)) / (2 * e)
+    assert abs(fd - gr["dtheta"]) <= 1e-6 * abs(fd)
+    for (yy, xx, c) in [(5, 7, 0), (12, 3, 1), (1, 14, 2), (8, 8, 3), (0, 0, 2)]:
+        e = 1e-4
+        ha, hb = h.copy(), h.copy()
+        ha[yy, xx, c] += e
+        hb[yy, xx, c] -= e
+        fd = (loss(base, ha) - loss(base, hb)) / (2 * e)
+        assert abs(fd - dh0[yy, xx, c]) <= 1e-6 * max(1.0, abs(fd)), (yy, xx, c, fd, dh0[yy, xx, c])
