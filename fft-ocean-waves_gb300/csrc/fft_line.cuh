@@ -66,24 +66,28 @@ __device__ __forceinline__ float2 mul_w32(float2 x, int idx)
     return make_float2(x.x * c - x.y * s, x.x * s + x.y * c);
 }
 
-__host__ __device__ constexpr int bitrev_n(int i, int n)
+__host__ __device__ constexpr int ilog2c(int n) { return n <= 1 ? 0 : 1 + ilog2c(n / 2); }
+
+// Bit reversal of i over `bits` bits (linear loop: fully unrolled and folded
+// when i and bits are compile-time constants).
+__host__ __device__ constexpr int bitrev_bits(int i, int bits)
 {
     int r = 0;
-    for (int b = 1; b < n; b <<= 1) {
-        r = (r << 1) | (i & 1);
-        i >>= 1;
-    }
+    for (int b = 0; b < bits; ++b) r |= ((i >> b) & 1) << (bits - 1 - b);
     return r;
 }
 
 // In-register R-point DFT (R = 1..32, power of two), natural order in and out.
-// Radix-2 decimation in time on bit-reversed input.
+// Radix-2 decimation in time on bit-reversed input.  Every loop has a linear
+// induction variable so that it unrolls completely and all register indices
+// are compile-time constants.
 template <int R, int SIGN>
 __device__ __forceinline__ void dft(float2* v)
 {
+    constexpr int LG = ilog2c(R);
 #pragma unroll
     for (int i = 0; i < R; ++i) {
-        const int j = bitrev_n(i, R);
+        const int j = bitrev_bits(i, LG);
         if (j > i) {
             float2 t = v[i];
             v[i]     = v[j];
@@ -91,12 +95,14 @@ __device__ __forceinline__ void dft(float2* v)
         }
     }
 #pragma unroll
-    for (int h = 1; h < R; h <<= 1) {
+    for (int s = 0; s < LG; ++s) {
+        const int h = 1 << s;
 #pragma unroll
         for (int k = 0; k < h; ++k) {
-            const int idx = k * (16 / h);  // W_{2h}^k == W_32^{16k/h}
+            const int idx = k * (16 >> s);  // W_{2h}^k == W_32^{16k/h}
 #pragma unroll
-            for (int i = k; i < R; i += 2 * h) {
+            for (int g = 0; g < R / (2 * h); ++g) {
+                const int i = k + g * 2 * h;
                 float2 b = mul_w32<SIGN>(v[i + h], idx);
                 float2 a = v[i];
                 v[i]     = a + b;
@@ -135,34 +141,64 @@ template <> struct LineFor<2048> { using type = LineCfg<2048, 32, 8, 8>; };
 // of radix RN (stride NSP*RP), twiddled and transformed.  Contains two
 // __syncthreads(): every thread of the block must call it.
 template <class C, int RP, int NSP, int RN, int SIGN>
-__device__ __forceinline__ void stockham_pass(float2* v, float2* buf, const float2* tw, int t)
+__device__ __forceinline__ void stockham_pass(float2* v, float2* buf, const float2* tw, int t, bool active)
 {
     constexpr int N   = C::N;
     constexpr int NSN = NSP * RP;
+    if (active) {
 #pragma unroll
-    for (int b = 0; b < C::R1 / RP; ++b) {
+        for (int b = 0; b < C::R1 / RP; ++b) {
+            const int j    = t + b * C::G;
+            const int idxD = (j / NSP) * NSP * RP + (j % NSP);
+#pragma unroll
+            for (int r = 0; r < RP; ++r) buf[C::pad(idxD + r * NSP)] = v[b * RP + r];
+        }
+    }
+    __syncthreads();
+    if (active) {
+#pragma unroll
+        for (int b = 0; b < C::R1 / RN; ++b) {
+            const int j = t + b * C::G;
+#pragma unroll
+            for (int r = 0; r < RN; ++r) v[b * RN + r] = buf[C::pad(j + r * (N / RN))];
+        }
+    }
+    __syncthreads();
+    if (!active) return;
+#pragma unroll
+    for (int b = 0; b < C::R1 / RN; ++b) {
         const int j    = t + b * C::G;
-        const int idxD = (j / NSP) * NSP * RP + (j % NSP);
+        const int k    = j % NSN;
+        const int step = N / (NSN * RN);
+        if constexpr (RN <= 8) {
 #pragma unroll
-        for (int r = 0; r < RP; ++r) buf[C::pad(idxD + r * NSP)] = v[b * RP + r];
-    }
-    __syncthreads();
+            for (int r = 1; r < RN; ++r) {
+                float2 w = tw[(k * r * step) & (N - 1)];
+                if (SIGN < 0) w.y = -w.y;
+                v[b * RN + r] = cmul(v[b * RN + r], w);
+            }
+        } else {
+            // W^{kr} = A[r mod 8] * B[r div 8]: 7 + RN/8 - 1 table reads instead of
+            // RN - 1, which keeps the live twiddle registers few (one extra
+            // rounding per twiddle)
+            float2 A[8], B[RN / 8];
+            A[0] = make_float2(1.0f, 0.0f);
+            B[0] = A[0];
 #pragma unroll
-    for (int b = 0; b < C::R1 / RN; ++b) {
-        const int j = t + b * C::G;
+            for (int i = 1; i < 8; ++i) {
+                A[i] = tw[(k * i * step) & (N - 1)];
+                if (SIGN < 0) A[i].y = -A[i].y;
+            }
 #pragma unroll
-        for (int r = 0; r < RN; ++r) v[b * RN + r] = buf[C::pad(j + r * (N / RN))];
-    }
-    __syncthreads();
+            for (int i = 1; i < RN / 8; ++i) {
+                B[i] = tw[(k * 8 * i * step) & (N - 1)];
+                if (SIGN < 0) B[i].y = -B[i].y;
+            }
 #pragma unroll
-    for (int b = 0; b < C::R1 / RN; ++b) {
-        const int j = t + b * C::G;
-        const int k = j % NSN;
-#pragma unroll
-        for (int r = 1; r < RN; ++r) {
-            float2 w = tw[(k * r * (N / (NSN * RN))) & (N - 1)];
-            if (SIGN < 0) w.y = -w.y;
-            v[b * RN + r] = cmul(v[b * RN + r], w);
+            for (int r = 1; r < RN; ++r) {
+                const float2 w = (r & 7) == 0 ? B[r >> 3] : ((r >> 3) == 0 ? A[r] : cmul(A[r & 7], B[r >> 3]));
+                v[b * RN + r] = cmul(v[b * RN + r], w);
+            }
         }
         dft<RN, SIGN>(v + b * RN);
     }
@@ -171,12 +207,13 @@ __device__ __forceinline__ void stockham_pass(float2* v, float2* buf, const floa
 // Full line transform.  On entry v[r] = x[t + r*N/R1]; on exit
 // v[b*RL + r] = X[(t + b*G) + r*(N/RL)] with RL the last radix.
 // tw: N-entry table tw[i] = exp(+2*pi*i*i/N) (conjugated here for SIGN < 0).
+// Threads with active == false do no work but take part in the barriers.
 template <class C, int SIGN>
-__device__ __forceinline__ void line_fft(float2* v, float2* buf, const float2* tw, int t)
+__device__ __forceinline__ void line_fft(float2* v, float2* buf, const float2* tw, int t, bool active = true)
 {
-    dft<C::R1, SIGN>(v);
-    stockham_pass<C, C::R1, 1, C::R2, SIGN>(v, buf, tw, t);
-    if constexpr (C::R3 > 1) stockham_pass<C, C::R2, C::R1, C::R3, SIGN>(v, buf, tw, t);
+    if (active) dft<C::R1, SIGN>(v);
+    stockham_pass<C, C::R1, 1, C::R2, SIGN>(v, buf, tw, t, active);
+    if constexpr (C::R3 > 1) stockham_pass<C, C::R2, C::R1, C::R3, SIGN>(v, buf, tw, t, active);
 }
 
 template <class C>

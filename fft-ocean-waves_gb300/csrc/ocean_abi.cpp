@@ -6,8 +6,11 @@
 // intermediate (in place of m_tilde_h0_t_* and m_ping_pong), the twiddle
 // table (in place of m_twiddle_factors) and, optionally, headless output
 // buffers (m_dx, m_dy, m_dz, m_normal_map).
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
@@ -52,6 +55,21 @@ int validate(const ocean_params* p)
     return OCEAN_OK;
 }
 
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no -lcuda).
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder()
+{
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    if (!fn) {
+        void*                           p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    }
+    return fn;
+}
+
 double gravity_of(const ocean_params& p) { return p.gravity > 0.0f ? (double)p.gravity : 9.81; }
 
 ocean::H0Args h0_args(const ocean_params& p)
@@ -85,10 +103,16 @@ struct ocean_s {
     ocean_params p{};
     int          N = 0;
     float4*      h0     = nullptr;  // [N][N]
-    float2*      inter  = nullptr;  // [3][N/2+1][N]
+    float2*      inter  = nullptr;  // [3][N/2+1][N+2] (periodic pad column each side)
+    unsigned*    status = nullptr;  // device status word (bounded-wait time-outs)
+    CUtensorMap  inter_map;         // column-pass view of inter
     float2*      tw     = nullptr;  // [N]
     float*       noise  = nullptr;  // [4][N][N], kept for ocean_set_params
     float*       out    = nullptr;  // handle-owned outputs: dx, dy, dz, normal_j
+    float2*      adj    = nullptr;  // adjoint scratch: [frames][3][N/2+1][N]
+    int          adj_frames = 0;
+    double*      sums   = nullptr;  // adjoint parameter sums (4 doubles)
+    bool         pdl_next = false;  // the next column pass directly follows this handle's row pass
     double       K      = 0.0;      // sqrt(g/(2*pi*L))
     double       w_dc   = 0.0;      // sqrt(g*1e-5): the floored DC frequency
 
@@ -96,9 +120,12 @@ struct ocean_s {
     {
         cudaFree(h0);
         cudaFree(inter);
+        cudaFree(status);
         cudaFree(tw);
         cudaFree(noise);
         cudaFree(out);
+        cudaFree(adj);
+        cudaFree(sums);
     }
 
     void set_consts()
@@ -221,12 +248,39 @@ int ocean_create(const ocean_params* params, const float* noise_host, ocean_t** 
     o->N = params->N;
     o->set_consts();
     const size_t N = (size_t)o->N;
+    const size_t H = (size_t)ocean::inter_rows(o->N), NP = (size_t)ocean::inter_pitch(o->N);
     if ((e = cudaMalloc(&o->h0, N * N * sizeof(float4))) != cudaSuccess ||
-        (e = cudaMalloc(&o->inter, 3 * (N / 2 + 1) * N * sizeof(float2))) != cudaSuccess ||
+        (e = cudaMalloc(&o->inter, 3 * H * NP * sizeof(float2))) != cudaSuccess ||
+        (e = cudaMalloc(&o->status, sizeof(unsigned))) != cudaSuccess ||
         (e = cudaMalloc(&o->tw, N * sizeof(float2))) != cudaSuccess ||
         (e = cudaMalloc(&o->noise, 4 * N * N * sizeof(float))) != cudaSuccess) {
         delete o;
         return fail(OCEAN_ERR_NOMEM, std::string("device allocation failed: ") + cudaGetErrorString(e));
+    }
+    if ((e = cudaMemset(o->status, 0, sizeof(unsigned))) != cudaSuccess) {
+        delete o;
+        return cuda_fail(e, "status clear");
+    }
+    {
+        // Column-pass tensor map: the intermediate as floats [3*H rows][2*NP].
+        PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
+        if (!enc) {
+            delete o;
+            return fail(OCEAN_ERR_UNSUPPORTED, "cuTensorMapEncodeTiled is not available from the driver");
+        }
+        unsigned box[2];
+        ocean::col_pass_box(o->N, box);
+        cuuint64_t dims[2]    = {2 * NP, 3 * H};
+        cuuint64_t strides[1] = {2 * NP * sizeof(float)};
+        cuuint32_t boxd[2]    = {box[0], box[1]};
+        cuuint32_t estr[2]    = {1, 1};
+        CUresult   r = enc(&o->inter_map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, o->inter, dims, strides, boxd, estr,
+                           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                           CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+        if (r != CUDA_SUCCESS) {
+            delete o;
+            return fail(OCEAN_ERR_CUDA, "cuTensorMapEncodeTiled failed: " + std::to_string((int)r));
+        }
     }
     std::vector<float2> tw(N);
     for (size_t k = 0; k < N; ++k) {
@@ -328,6 +382,7 @@ int ocean_update_rows(ocean_t* o, double t, void* stream)
     ra.h0           = o->h0;
     ra.inter        = o->inter;
     ra.tw           = o->tw;
+    ra.status       = o->status;
     ra.fc           = o->frame(t);
     ra.literal_conj = (o->p.flags & OCEAN_FLAG_LITERAL_CONJ) ? 1 : 0;
     cudaError_t e   = ocean::launch_row_pass(o->N, ra, static_cast<cudaStream_t>(stream));
@@ -349,7 +404,8 @@ int ocean_update_columns(ocean_t* o, const ocean_outputs* out, void* stream)
                          reinterpret_cast<uintptr_t>(out->dz) | reinterpret_cast<uintptr_t>(out->normal_j);
     if (al % 16) return fail(OCEAN_ERR_INVALID, "output pointers must be 16-byte aligned");
     ocean::ColArgs ca;
-    ca.inter      = o->inter;
+    ca.map        = o->inter_map;
+    ca.status     = o->status;
     ca.tw         = o->tw;
     ca.dx         = out->dx;
     ca.dy         = out->dy;
@@ -358,7 +414,8 @@ int ocean_update_columns(ocean_t* o, const ocean_outputs* out, void* stream)
     ca.scale      = (float)(0.5 / ((double)o->N * o->N));
     ca.lambda     = o->p.choppiness;
     ca.inv2d      = (float)((double)o->N / (2.0 * (double)o->p.L));
-    cudaError_t e = ocean::launch_col_pass(o->N, ca, static_cast<cudaStream_t>(stream));
+    cudaError_t e = ocean::launch_col_pass(o->N, ca, static_cast<cudaStream_t>(stream), o->pdl_next);
+    o->pdl_next   = false;
     if (e != cudaSuccess) return cuda_fail(e, "column pass launch");
     return OCEAN_OK;
 }
@@ -376,7 +433,101 @@ int ocean_update(ocean_t* o, double t, const ocean_outputs* out, void* stream)
     if (!out->dx || !out->dy || !out->dz || !out->normal_j) return fail(OCEAN_ERR_INVALID, "NULL output pointer");
     int rc = ocean_update_rows(o, t, stream);
     if (rc) return rc;
+    o->pdl_next = true;   // columns follow rows on the same stream: overlap their set-up
     return ocean_update_columns(o, out, stream);
+}
+
+int ocean_device_status(ocean_t* o, void* stream)
+{
+    if (!o) return fail(OCEAN_ERR_INVALID, "ocean is NULL");
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    unsigned     h = 0;
+    cudaError_t  e;
+    if ((e = cudaMemcpyAsync(&h, o->status, sizeof(h), cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
+        (e = cudaMemsetAsync(o->status, 0, sizeof(unsigned), s)) != cudaSuccess ||
+        (e = cudaStreamSynchronize(s)) != cudaSuccess)
+        return cuda_fail(e, "device status");
+    if (h) return fail(OCEAN_ERR_TIMEOUT, "a kernel's bounded wait for its TMA copies timed out");
+    return OCEAN_OK;
+}
+
+int ocean_backward(ocean_t* o, const double* times, int32_t T, const float* g_dx, const float* g_dy,
+                   const float* g_dz, uint32_t flags, ocean_grads* grads, void* stream)
+{
+    if (!o || !grads || !times) return fail(OCEAN_ERR_INVALID, "NULL argument");
+    if (T < 1) return fail(OCEAN_ERR_INVALID, "T must be >= 1");
+    if (flags & ~OCEAN_GRAD_ACCUMULATE) return fail(OCEAN_ERR_INVALID, "unknown flag bits");
+    for (int j = 0; j < T; ++j)
+        if (!std::isfinite(times[j])) return fail(OCEAN_ERR_INVALID, "time is not finite");
+    const uintptr_t al = reinterpret_cast<uintptr_t>(g_dx) | reinterpret_cast<uintptr_t>(g_dy) |
+                         reinterpret_cast<uintptr_t>(g_dz) | reinterpret_cast<uintptr_t>(grads->dh0);
+    if (al % 16) return fail(OCEAN_ERR_INVALID, "gradient pointers must be 16-byte aligned");
+    cudaStream_t s  = static_cast<cudaStream_t>(stream);
+    const size_t N  = (size_t)o->N, NN = N * N, H = N / 2 + 1;
+    const size_t per_frame = 3 * H * N * sizeof(float2);
+    int chunk = (int)std::min<size_t>((size_t)ocean::kMaxChunkFrames, std::max<size_t>(1, (512ull << 20) / per_frame));
+    chunk     = std::min(chunk, (int)T);
+    cudaError_t e;
+    if (o->adj_frames < chunk) {
+        cudaFree(o->adj);
+        o->adj        = nullptr;
+        o->adj_frames = 0;
+        if ((e = cudaMalloc(&o->adj, per_frame * chunk)) != cudaSuccess)
+            return fail(OCEAN_ERR_NOMEM, std::string("adjoint scratch allocation failed: ") + cudaGetErrorString(e));
+        o->adj_frames = chunk;
+    }
+    if (!o->sums && (e = cudaMalloc(&o->sums, 4 * sizeof(double))) != cudaSuccess) {
+        o->sums = nullptr;
+        return fail(OCEAN_ERR_NOMEM, std::string("allocation failed: ") + cudaGetErrorString(e));
+    }
+    if (!(flags & OCEAN_GRAD_ACCUMULATE)) {
+        grads->dA = grads->dV = grads->dtheta = grads->dlambda = 0.0;
+        if (grads->dh0 && (e = cudaMemsetAsync(grads->dh0, 0, NN * sizeof(float4), s)) != cudaSuccess)
+            return cuda_fail(e, "dh0 clear");
+    }
+    if ((e = cudaMemsetAsync(o->sums, 0, 4 * sizeof(double), s)) != cudaSuccess) return cuda_fail(e, "sums clear");
+
+    const ocean::H0Args ha = h0_args(o->p);
+    const double g = gravity_of(o->p), V = o->p.wind_speed, Lw = V * V / g;
+    for (int c0 = 0; c0 < T; c0 += chunk) {
+        const int n = std::min(chunk, (int)T - c0);
+        ocean::AdjColArgs ca;
+        ca.gx    = g_dx ? g_dx + (size_t)c0 * NN : nullptr;
+        ca.gy    = g_dy ? g_dy + (size_t)c0 * NN : nullptr;
+        ca.gz    = g_dz ? g_dz + (size_t)c0 * NN : nullptr;
+        ca.inter = o->adj;
+        ca.tw    = o->tw;
+        ca.scale = (float)(0.5 / (double)NN);
+        if ((e = ocean::launch_adj_col(o->N, n, ca, s)) != cudaSuccess) return cuda_fail(e, "adjoint column pass");
+        ocean::AdjRowArgs ra;
+        ra.inter         = o->adj;
+        ra.h0            = o->h0;
+        ra.tw            = o->tw;
+        ra.dh0           = reinterpret_cast<float4*>(grads->dh0);
+        ra.sums          = o->sums;
+        ra.T             = n;
+        ra.literal_conj  = (o->p.flags & OCEAN_FLAG_LITERAL_CONJ) ? 1 : 0;
+        ra.lambda        = o->p.choppiness;
+        ra.two_pi_over_L = ha.two_pi_over_L;
+        ra.amplitude     = ha.amplitude;
+        ra.inv_Lp2       = ha.inv_Lp2;
+        ra.l2            = ha.l2;
+        ra.wx            = ha.wx;
+        ra.wy            = ha.wy;
+        ra.wA            = o->p.amplitude > 0.0f ? (float)(0.5 / o->p.amplitude) : 0.0f;
+        ra.wV            = (float)(2.0 * V / (g * Lw * Lw * Lw));
+        for (int j = 0; j < n; ++j) ra.fc[j] = o->frame(times[c0 + j]);
+        if ((e = ocean::launch_adj_row(o->N, ra, s)) != cudaSuccess) return cuda_fail(e, "adjoint row pass");
+    }
+    double h[4];
+    if ((e = cudaMemcpyAsync(h, o->sums, sizeof(h), cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
+        (e = cudaStreamSynchronize(s)) != cudaSuccess)
+        return cuda_fail(e, "adjoint sums");
+    grads->dA += h[0];
+    grads->dV += h[1];
+    grads->dtheta += h[2];
+    grads->dlambda += h[3];
+    return OCEAN_OK;
 }
 
 }  // extern "C"

@@ -1,6 +1,7 @@
 // ocean_internal.h -- kernel launch interface shared by the host code and the
 // CUDA translation units.  Not part of the public ABI.
 #pragma once
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -21,16 +22,26 @@ struct H0Args {
     float wx, wy;         // normalised wind direction
 };
 
+// Row-pass output ("intermediate"): three fields (Dx, Dy, Dz) of rows
+// y' = 0..N/2 of the row-transformed Hermitian spectra.  Each row holds N+2
+// complex values: padded column p = x + 1 for x = -1..N, with x = -1 and x = N
+// the periodic copies of x = N-1 and x = 0, so that any column tile together
+// with its two neighbour columns is one contiguous 16-byte-aligned box.
+__host__ __device__ constexpr int inter_pitch(int N) { return N + 2; }
+__host__ __device__ constexpr int inter_rows(int N) { return N / 2 + 1; }
+
 struct RowArgs {
-    const float4* h0;     // [N][N]
-    float2*       inter;  // [3][N/2+1][N]   (Dx, Dy, Dz) half spectra after the row pass
-    const float2* tw;     // [N] exp(+2*pi*i*k/N)
+    const float4* h0;      // [N][N]
+    float2*       inter;   // [3][N/2+1][N+2]
+    const float2* tw;      // [N] exp(+2*pi*i*k/N)
+    unsigned*     status;  // device status word (bounded-wait time-outs)
     FrameConsts   fc;
     int           literal_conj;
 };
 
 struct ColArgs {
-    const float2* inter;
+    CUtensorMap   map;     // 2-D tensor map over inter: floats [3*(N/2+1)][2*(N+2)]
+    unsigned*     status;
     const float2* tw;
     float*        dx;
     float*        dy;
@@ -41,9 +52,44 @@ struct ColArgs {
     float         inv2d;   // N/(2L): central-difference factor
 };
 
+// ---------------------------------------------------------------------------
+// Adjoint (ocean_backward)
+// ---------------------------------------------------------------------------
+constexpr int kMaxChunkFrames = 64;   // frames per adjoint launch pair
+
+struct AdjColArgs {
+    const float* gx;  // upstream dL/dDx of the chunk's first frame, [T][N][N]; NULL = 0
+    const float* gy;
+    const float* gz;
+    float2*      inter;  // [T][3][N/2+1][N]: column-transformed gradients, rows 0..N/2
+    const float2* tw;
+    float        scale;  // 0.5/N^2: (-1)^(x+y)/N^2 of the inversion and the unpacking 1/2
+};
+
+struct AdjRowArgs {
+    const float2* inter;
+    const float4* h0;
+    const float2* tw;
+    float4*       dh0;   // dL/dh0 accumulator [N][N] (added to); NULL = not wanted
+    double*       sums;  // [4]: dA, dV, dtheta, dlambda (atomically added to)
+    int           T;
+    int           literal_conj;
+    float         lambda;
+    float         two_pi_over_L, amplitude, inv_Lp2, l2, wx, wy;  // to re-derive a(k) and its clamp
+    float         wA;    // 1/(2A)
+    float         wV;    // 2V/(g Lw^3); dV weight is wV/|k|^2
+    FrameConsts   fc[kMaxChunkFrames];
+};
+
+cudaError_t launch_adj_col(int N, int T, const AdjColArgs& a, cudaStream_t s);
+cudaError_t launch_adj_row(int N, const AdjRowArgs& a, cudaStream_t s);
+
 cudaError_t launch_h0(const H0Args& a, const float* noise, float4* h0, cudaStream_t s);
 cudaError_t launch_row_pass(int N, const RowArgs& a, cudaStream_t s);
-cudaError_t launch_col_pass(int N, const ColArgs& a, cudaStream_t s);
+// pdl: launch as a programmatic dependent of the preceding kernel in `s`.
+cudaError_t launch_col_pass(int N, const ColArgs& a, cudaStream_t s, bool pdl);
+// Box of the column-pass tensor map at size N: {inner floats, rows}.
+void col_pass_box(int N, unsigned box[2]);
 // Shared memory the two passes need at size N (bytes), for validation.
 size_t row_pass_smem(int N);
 size_t col_pass_smem(int N);

@@ -9,88 +9,30 @@
 //               (inversion_cs.glsl:35), so each field is first made Hermitian,
 //               X_H(k) = (X(k) + conj X(-k))/2, which leaves Re unchanged and
 //               makes the row-transformed rows y' and N-y' conjugates: only
-//               rows 0..N/2 are transformed and stored.  A CTA owns the row
-//               pair (y', N-y'), reads each h0 mode once and shares one phase
-//               w*t per mode pair.
+//               rows 0..N/2 are transformed and stored.  Persistent CTAs walk
+//               the row pairs (y', N-y'); the two h0 rows of the next pairs are
+//               fetched with 1-D bulk TMA copies into a two-stage shared-memory
+//               ring while the current pair is transformed, and the phase w*t
+//               is computed once per mode pair for all three fields.
 //
 //   k_col_pass  vertical inverse FFT (butterfly_cs.glsl:95-132) on column
-//               tiles staged in shared memory, with two real results packed
-//               per complex transform (Dy + i*Dx per column, Dz of two
-//               columns), fused with the (-1)^(x+y)/N^2 inversion
-//               (inversion_cs.glsl:29-41), lambda scaling, the Sobel normal
-//               (normal_map_cs.glsl:37-53) and the Jacobian.  Each tile also
-//               transforms the two neighbouring columns it needs for the
-//               stencils.
+//               tiles fetched by 2-D tensor TMA (tile + one neighbour column on
+//               each side, thanks to the periodic padding of the
+//               intermediate), with two real results packed per complex
+//               transform (Dy + i*Dx per column, Dz of two columns), fused with
+//               the (-1)^(x+y)/N^2 inversion (inversion_cs.glsl:29-41), lambda
+//               scaling, the Sobel normal (normal_map_cs.glsl:37-53) and the
+//               Jacobian.  Launched as a programmatic dependent of the row pass
+//               so its set-up overlaps the row pass's tail.
 #include <cuda_runtime.h>
 #include <stdint.h>
 
 #include "fft_line.cuh"
+#include "ocean_device.cuh"
 #include "ocean_internal.h"
+#include "tma.cuh"
 
 namespace ocean {
-
-// ---------------------------------------------------------------------------
-// Phase w*t in double-float arithmetic.
-// w = sqrt(g*|k|), |k| = (2*pi/L)*sqrt(m), m = ix^2 + iz^2 (exact integer), so
-// w*t/(2*pi) = K*t*m^(1/4) with K = sqrt(g/(2*pi*L)).  K*t comes from the host
-// as a double-float; m^(1/4) is formed by two double-float square roots
-// (Dekker 1971: one Newton correction on the FP32 root with an exact FMA
-// residual) and the product by Dekker's two-product via FMA.  The integer
-// number of cycles is dropped before sincospi, so the reduced phase keeps
-// ~1e-7 absolute accuracy at any t the double can carry.
-// ---------------------------------------------------------------------------
-struct dfl {
-    float hi, lo;
-};
-
-__device__ __forceinline__ dfl df_sqrt_int(float a)  // a >= 1, an exact integer
-{
-    float s = __fsqrt_rn(a);
-    float e = __fmaf_rn(-s, s, a);
-    return {s, __fmul_rn(e, 0.5f * __frcp_rn(s))};
-}
-
-__device__ __forceinline__ dfl df_sqrt(dfl a)
-{
-    float s = __fsqrt_rn(a.hi);
-    float e = __fadd_rn(__fmaf_rn(-s, s, a.hi), a.lo);
-    float c = __fmul_rn(e, 0.5f * __frcp_rn(s));
-    float r = __fadd_rn(s, c);
-    return {r, __fadd_rn(c, -__fadd_rn(r, -s))};
-}
-
-__device__ __forceinline__ dfl df_mul(dfl a, dfl b)
-{
-    float p = __fmul_rn(a.hi, b.hi);
-    float e = __fmaf_rn(a.hi, b.hi, -p);
-    e       = __fmaf_rn(a.hi, b.lo, e);
-    e       = __fmaf_rn(a.lo, b.hi, e);
-    return {p, e};
-}
-
-// cos/sin of the phase of mode m (m = ix^2 + iz^2) at the frame's time.
-__device__ __forceinline__ void mode_phase(int m, const FrameConsts& fc, float& c, float& s)
-{
-    float f;
-    if (m == 0) {
-        f = fc.dc_cycles;
-    } else {
-        dfl q   = df_sqrt(df_sqrt_int((float)m));
-        dfl cyc = df_mul(dfl{fc.kt_hi, fc.kt_lo}, q);
-        float n = rintf(cyc.hi);
-        f       = __fadd_rn(__fadd_rn(cyc.hi, -n), cyc.lo);
-        f       = __fadd_rn(f, -rintf(f));
-    }
-    sincospif(2.0f * f, &s, &c);
-}
-
-// h(k,t) = h0(k) e^{iwt} + conj(h0(-k)) e^{-iwt} (tilde_h0_t_cs.glsl:110);
-// literal_conj reproduces the shader's no-op conjugate() (:42-48).
-__device__ __forceinline__ float2 evolve(float4 h, float c, float s, int literal_conj)
-{
-    float bi = literal_conj ? h.w : -h.w;
-    return make_float2(h.x * c - h.y * s + h.z * c + bi * s, h.x * s + h.y * c - h.z * s + bi * c);
-}
 
 // ---------------------------------------------------------------------------
 // h0 initialisation (tilde_h0_k_cs.glsl:35-93), one thread per mode.
@@ -122,180 +64,338 @@ __global__ void k_h0_init(H0Args a, const float* __restrict__ noise, float4* __r
     h0[i] = make_float4(v0 * c0, v0 * s0, v1 * c1, v1 * s1);
 }
 
+// Dynamic shared memory, 128-byte aligned (TMA box destinations need it).
+__device__ __forceinline__ float2* align_smem(unsigned char* raw)
+{
+    return reinterpret_cast<float2*>((reinterpret_cast<uintptr_t>(raw) + 127) & ~uintptr_t(127));
+}
+
 // ---------------------------------------------------------------------------
 // Row pass.
 // ---------------------------------------------------------------------------
 template <int N>
 struct RowCfg {
     using L = typename LineFor<N>::type;
-    static constexpr int PAIRS   = L::G >= 32 ? 1 : 32 / L::G;  // row pairs per CTA
+    static constexpr int PAIRS   = L::G >= 32 ? 1 : 32 / L::G;  // row pairs per work item
     static constexpr int LINES   = 3 * PAIRS;
     static constexpr int THREADS = LINES * L::G;
-    static constexpr size_t SMEM = sizeof(float2) * (N + (size_t)LINES * L::NPAD);
-    static constexpr int GRID    = (N / 2 + 1 + PAIRS - 1) / PAIRS;
+    static constexpr int ITEMS   = (N / 2 + 1 + PAIRS - 1) / PAIRS;
+    static constexpr int STAGES  = 2;
+    // shared memory (float2 units): tw[N] | h0 ring [STAGES][PAIRS][2][N] float4 |
+    // work area = max(hy [PAIRS][2][N], line buffers [LINES][NPAD])
+    static constexpr size_t RING  = (size_t)STAGES * PAIRS * 2 * N * 2;
+    static constexpr size_t HY    = (size_t)PAIRS * 2 * N;
+    static constexpr size_t XB    = (size_t)LINES * L::NPAD;
+    static constexpr size_t WORK  = HY > XB ? HY : XB;
+    static constexpr size_t SMEM  = sizeof(float2) * (N + RING + WORK) + 128;   // + base alignment slack
+    static constexpr uint32_t ROW_BYTES = N * sizeof(float4);
 };
+
+template <int N>
+__device__ __forceinline__ void row_issue(const RowArgs& a, float4* ring_stage, uint64_t* bar, int item)
+{
+    using RC = RowCfg<N>;
+    uint32_t bytes = 0;
+#pragma unroll
+    for (int pl = 0; pl < RC::PAIRS; ++pl)
+        if (item * RC::PAIRS + pl <= N / 2) bytes += 2 * RC::ROW_BYTES;
+    mbar_arrive_expect_tx(bar, bytes);
+#pragma unroll
+    for (int pl = 0; pl < RC::PAIRS; ++pl) {
+        const int yp = item * RC::PAIRS + pl;
+        if (yp > N / 2) break;
+        const int yq = (N - yp) & (N - 1);
+        bulk_g2s(ring_stage + (pl * 2 + 0) * N, a.h0 + (size_t)yp * N, RC::ROW_BYTES, bar);
+        bulk_g2s(ring_stage + (pl * 2 + 1) * N, a.h0 + (size_t)yq * N, RC::ROW_BYTES, bar);
+    }
+}
 
 template <int N>
 __global__ void __launch_bounds__(RowCfg<N>::THREADS) k_row_pass(RowArgs a)
 {
     using RC = RowCfg<N>;
     using L  = typename RC::L;
-    extern __shared__ float2 smem[];
+    constexpr int NP = inter_pitch(N), H = inter_rows(N);
+    extern __shared__ unsigned char smem_raw[];
+    float2* smem = align_smem(smem_raw);
     float2* tw_s = smem;
-    for (int i = threadIdx.x; i < N; i += RC::THREADS) tw_s[i] = a.tw[i];
+    float4* ring = reinterpret_cast<float4*>(smem + N);              // [STAGES][PAIRS][2][N]
+    float2* work = smem + N + RC::RING;                              // hy, then line buffers
+    __shared__ __align__(8) uint64_t bars[RC::STAGES];
+    __shared__ int wait_ok;
 
-    const int li = threadIdx.x / L::G, t = threadIdx.x % L::G;
-    const int f  = li % 3;                               // 0: Dx, 1: Dy, 2: Dz
-    const int yp = blockIdx.x * RC::PAIRS + li / 3;      // row y' in [0, N/2]
-    const bool active = yp <= N / 2;
-    const int yq = (N - yp) & (N - 1);                   // row of -k
-    float2 v[L::E];
-#pragma unroll
-    for (int r = 0; r < L::E; ++r) v[r] = make_float2(0.0f, 0.0f);
-    if (active) {
-        const int iz = yp - N / 2, izq = yq - N / 2;
-        const float4* rowp = a.h0 + (size_t)yp * N;
-        const float4* rowq = a.h0 + (size_t)yq * N;
+    const int tid = threadIdx.x;
+    if (tid == 0) {
+        for (int s = 0; s < RC::STAGES; ++s) mbar_init(&bars[s], 1);
+        fence_mbar_init();
+    }
+    for (int i = tid; i < N; i += RC::THREADS) tw_s[i] = a.tw[i];
+    __syncthreads();
+    if (tid == 0)
+        for (int s = 0; s < RC::STAGES; ++s) {
+            const int item = blockIdx.x + s * gridDim.x;
+            if (item < RC::ITEMS) row_issue<N>(a, ring + (size_t)s * RC::PAIRS * 2 * N, &bars[s], item);
+        }
+    // The column pass may start its set-up now; it waits for this grid to finish
+    // before it reads the intermediate.
+    pdl_launch_dependents();
+
+    const int li = tid / L::G, t = tid % L::G;
+    const int f  = li % 3;                                           // 0: Dx, 1: Dy, 2: Dz
+    const int pl_line = li / 3;
+    uint32_t phase_bits = 0;
+
+    for (int k = 0, item = blockIdx.x; item < RC::ITEMS; ++k, item += gridDim.x) {
+        const int s = k & 1;
+        float4* stage = ring + (size_t)s * RC::PAIRS * 2 * N;
+        if (!block_wait(&bars[s], (phase_bits >> s) & 1u, &wait_ok, a.status)) return;
+        phase_bits ^= 1u << s;
+
+        // Prepass: h(k,t) for the pair's two rows, once per mode pair; the
+        // mirror mode (N-x, N-y') shares |k| and so the phase.  hy[pl][0][x] is
+        // the mode (x, y'), hy[pl][1][x] the mode (N-x, N-y').
+        float2* hy = work;
+        for (int i = tid; i < RC::PAIRS * N; i += RC::THREADS) {
+            const int pl = i / N, x = i % N;
+            const int yp = item * RC::PAIRS + pl;
+            if (yp > N / 2) continue;
+            const int ix = x - N / 2, iz = yp - N / 2;
+            float c, sn;
+            mode_phase(ix * ix + iz * iz, a.fc, c, sn);
+            hy[(pl * 2 + 0) * N + x] = evolve(stage[(pl * 2 + 0) * N + x], c, sn, a.literal_conj);
+            hy[(pl * 2 + 1) * N + x] = evolve(stage[(pl * 2 + 1) * N + ((N - x) & (N - 1))], c, sn, a.literal_conj);
+        }
+        __syncthreads();                                   // hy complete, ring stage s consumed
+        if (tid == 0) {
+            const int next = item + RC::STAGES * gridDim.x;
+            if (next < RC::ITEMS) {
+                fence_proxy_async_smem();
+                row_issue<N>(a, stage, &bars[s], next);
+            }
+        }
+
+        // Gather the line inputs: 2 * X_H,f(x) = X_f(x) + conj X_f(-x).
+        const int  yp     = item * RC::PAIRS + pl_line;
+        const bool active = yp <= N / 2;
+        const int  iz = yp - N / 2, izq = ((N - yp) & (N - 1)) - N / 2;
+        float2 v[L::E];
 #pragma unroll
         for (int r = 0; r < L::E; ++r) {
-            const int x  = t + r * (N / L::R1);
-            const int xq = (N - x) & (N - 1);
-            const int ix = x - N / 2;
-            const int m  = ix * ix + iz * iz;
-            float c, s;
-            mode_phase(m, a.fc, c, s);
-            float2 hk = evolve(__ldg(rowp + x), c, s, a.literal_conj);
-            float2 hq = evolve(__ldg(rowq + xq), c, s, a.literal_conj);
-            float2 X, Xq;
-            if (f == 1) {
-                X = hk; Xq = hq;
-            } else {
+            const int x = t + r * (N / L::R1);
+            float2 hk = active ? hy[(pl_line * 2 + 0) * N + x] : make_float2(0.f, 0.f);
+            float2 hq = active ? hy[(pl_line * 2 + 1) * N + x] : make_float2(0.f, 0.f);
+            if (f != 1) {
                 // -i (k/|k|) h (tilde_h0_t_cs.glsl:113-126); the DC mode gets 0
+                const int   ix  = x - N / 2;
+                const int   m   = ix * ix + iz * iz;
                 const float rs  = m ? __frsqrt_rn((float)m) : 0.0f;
                 const float fk  = -(float)(f == 0 ? ix : iz) * rs;
-                const float fkq = -(float)(f == 0 ? (xq - N / 2) : izq) * rs;
-                X  = make_float2(-fk * hk.y, fk * hk.x);
-                Xq = make_float2(-fkq * hq.y, fkq * hq.x);
+                const float fkq = -(float)(f == 0 ? (((N - x) & (N - 1)) - N / 2) : izq) * rs;
+                hk = make_float2(-fk * hk.y, fk * hk.x);
+                hq = make_float2(-fkq * hq.y, fkq * hq.x);
             }
-            v[r] = make_float2(X.x + Xq.x, X.y - Xq.y);  // 2 * X_H
+            v[r] = make_float2(hk.x + hq.x, hk.y - hq.y);
         }
-    }
-    __syncthreads();
-    line_fft<L, +1>(v, smem + N + li * L::NPAD, tw_s, t);
-    if (active) {
-        float2* out = a.inter + ((size_t)f * (N / 2 + 1) + yp) * N;
+        __syncthreads();                                   // hy is read; the line buffers reuse it
+        line_fft<L, +1>(v, work + li * L::NPAD, tw_s, t);
+        if (active) {
+            float2* out = a.inter + ((size_t)f * H + yp) * NP;
 #pragma unroll
-        for (int e = 0; e < L::E; ++e) out[LineOut<L>::pos(t, e)] = v[e];
+            for (int e = 0; e < L::E; ++e) {
+                const int x = LineOut<L>::pos(t, e);
+                out[x + 1] = v[e];
+                if (x == N - 1) out[0] = v[e];             // periodic pad columns
+                if (x == 0) out[N + 1] = v[e];
+            }
+        }
+        // the next prepass overwrites `work`: line_fft ended with a barrier after
+        // its last shared-memory read
     }
 }
 
 // ---------------------------------------------------------------------------
 // Column pass.
 // ---------------------------------------------------------------------------
+constexpr int ceil8(int x) { return (x + 7) / 8 * 8; }
+constexpr int imax(int a, int b) { return a > b ? a : b; }
+
 template <int N>
 struct ColCfg {
     using L = typename LineFor<N>::type;
     static constexpr int C       = N >= 2048 ? 4 : 8;   // output columns per CTA
     static constexpr int CC      = C + 2;               // + one neighbour column each side
-    static constexpr int WL      = CC;                  // Dy + i*Dx lines
-    static constexpr int ZL      = CC / 2;              // Dz(c) + i*Dz(c+1) lines
-    static constexpr int LINES   = WL + ZL;
-    static constexpr int THREADS = LINES * L::G;
-    static constexpr int H       = N / 2 + 1;           // stored half-spectrum rows
-    static constexpr int TS      = CC + 1;              // tile row stride (odd: bank-free)
-    static constexpr int OS      = N + 32 / C;          // output-staging column stride
-    static constexpr size_t TILE = sizeof(float2) * 3 * (size_t)H * TS;
-    static constexpr size_t XBUF = sizeof(float2) * (size_t)LINES * L::NPAD;
-    static constexpr size_t OBUF = sizeof(float) * 3 * (size_t)CC * OS;
-    static constexpr size_t AREG = TILE > XBUF ? (TILE > OBUF ? TILE : OBUF) : (XBUF > OBUF ? XBUF : OBUF);
-    static constexpr size_t SMEM = sizeof(float2) * N + AREG;
+    static constexpr int WL      = CC;                  // round 1: Dy + i*Dx lines, one per column
+    static constexpr int ZL      = CC / 2;              // round 2: Dz(c) + i*Dz(c+1) lines
+    static constexpr int THREADS = WL * L::G;
+    static constexpr int H       = inter_rows(N);
+    // Staged rows per field: at least H, and at least half a line buffer so
+    // that a round's exchange buffers fit in the tile fields it has consumed.
+    static constexpr int HP0     = imax(H, (L::NPAD + 1) / 2);
+    static constexpr int NCHUNK  = (HP0 + 255) / 256;   // TMA boxes per field (<= 256 rows)
+    static constexpr int BR      = ceil8((HP0 + NCHUNK - 1) / NCHUNK);   // 128-byte aligned boxes
+    static constexpr int HP      = NCHUNK * BR;
+    static constexpr int OS      = N + 4;               // staging column stride (floats)
+    static constexpr size_t FIELD = (size_t)HP * CC;    // float2 per tile field
+    static constexpr size_t SMEM = sizeof(float2) * (N + 3 * FIELD) + 128;   // + base alignment slack
     static constexpr int GRID    = N / C;
+    static constexpr uint32_t TILE_BYTES = (uint32_t)(sizeof(float2) * 3 * FIELD);
+    static_assert((size_t)WL * L::NPAD <= 2 * FIELD && (size_t)ZL * L::NPAD <= FIELD, "exchange buffers");
+    static_assert((size_t)CC * OS <= 2 * FIELD, "staging");
 };
 
 template <int N>
-__global__ void __launch_bounds__(ColCfg<N>::THREADS) k_col_pass(ColArgs a)
+__global__ void __launch_bounds__(ColCfg<N>::THREADS) k_col_pass(const __grid_constant__ ColArgs a)
 {
-    using CC_ = ColCfg<N>;
-    using L   = typename CC_::L;
-    constexpr int C = CC_::C, CC = CC_::CC, H = CC_::H, TS = CC_::TS, OS = CC_::OS;
-    extern __shared__ float2 smem[];
+    using CF = ColCfg<N>;
+    using L  = typename CF::L;
+    constexpr int C = CF::C, CC = CF::CC, H = CF::H, HP = CF::HP, OS = CF::OS, WL = CF::WL, ZL = CF::ZL;
+    extern __shared__ unsigned char smem_raw[];
+    float2* smem = align_smem(smem_raw);
     float2* tw_s = smem;
-    float2* tile = smem + N;                                 // [3][H][TS]
-    float2* xbuf = smem + N;                                 // aliases the tile after the gather
-    float*  obuf = reinterpret_cast<float*>(smem + N);       // [3][CC][OS], aliases again
-    const int x0 = blockIdx.x * C;
+    float2* tile = smem + N;                                 // [3][HP][CC]: Dx, Dy, Dz (TMA boxes)
+    // round buffers and staging alias the tile fields once they are consumed
+    float2* xbuf1 = tile;                                    // round 1 exchange: fields Dx, Dy
+    float2* xbuf2 = tile + 2 * CF::FIELD;                    // round 2 exchange: field Dz
+    float*  sx = reinterpret_cast<float*>(tile);             // staged Dx [CC][OS]
+    float*  sy = reinterpret_cast<float*>(tile + CF::FIELD); // staged Dy
+    float*  sz = reinterpret_cast<float*>(tile + 2 * CF::FIELD);
+    __shared__ __align__(8) uint64_t bar;
+    __shared__ int wait_ok;
+    const int x0  = blockIdx.x * C;
+    const int tid = threadIdx.x;
 
-    for (int i = threadIdx.x; i < N; i += CC_::THREADS) tw_s[i] = a.tw[i];
-    // Stage columns x0-1 .. x0+C (periodic) of rows 0..N/2 of the three fields.
-    for (int i = threadIdx.x; i < 3 * H * CC; i += CC_::THREADS) {
-        const int cc = i % CC, row = i / CC;                 // row = f*H + y'
-        const int x  = (x0 - 1 + cc + N) & (N - 1);
-        tile[row * TS + cc] = a.inter[(size_t)row * N + x];
+    if (tid == 0) {
+        mbar_init(&bar, 1);
+        fence_mbar_init();
+        asm volatile("prefetch.tensormap [%0];" ::"l"(&a.map) : "memory");
     }
+    for (int i = tid; i < N; i += CF::THREADS) tw_s[i] = a.tw[i];
+    pdl_wait_prior();                                        // the row pass has finished
     __syncthreads();
-
-    const int li = threadIdx.x / L::G, t = threadIdx.x % L::G;
-    const bool wline = li < CC_::WL;
-    const int  c1 = wline ? li : 2 * (li - CC_::WL);         // tile columns of the two packed reals
-    const int  c2 = wline ? li : c1 + 1;
-    const int  fa = wline ? 1 : 2, fb = wline ? 0 : 2;       // real part: Dy or Dz(c1); imag: Dx or Dz(c2)
-    float2 v[L::E];
+    if (tid == 0) {
+        // Columns x0-1 .. x0+C are padded columns x0 .. x0+C+1 of the intermediate.
+        mbar_arrive_expect_tx(&bar, CF::TILE_BYTES);
 #pragma unroll
-    for (int r = 0; r < L::E; ++r) {
-        const int y = t + r * (N / L::R1);
-        const bool lo = y <= N / 2;
-        const int  ys = lo ? y : N - y;                      // rows N-y are conjugates of rows y
-        float2 p = tile[(fa * H + ys) * TS + c1];
-        float2 q = tile[(fb * H + ys) * TS + c2];
-        if (!lo) { p.y = -p.y; q.y = -q.y; }
-        v[r] = make_float2(p.x - q.y, p.y + q.x);            // p + i*q
+        for (int f = 0; f < 3; ++f)
+#pragma unroll
+            for (int q = 0; q < CF::NCHUNK; ++q)
+                tma_load_2d(tile + f * CF::FIELD + (size_t)q * CF::BR * CC, &a.map, 2 * x0, f * H + q * CF::BR, &bar);
     }
-    __syncthreads();                                         // tile dead; xbuf reuses it
-    line_fft<L, +1>(v, xbuf + li * L::NPAD, tw_s, t);        // ends with a block barrier
+    if (!block_wait(&bar, 0, &wait_ok, a.status)) return;
 
-    // Unpack, apply (-1)^(x+y) * scale (* lambda for Dx, Dz) and stage per column.
+    float2 v[L::E];
+    // ---- round 1: column lines Dy + i*Dx.  Thread -> (column, t) with the
+    // columns fastest across lanes: a warp reads consecutive shared words.
     {
-        const int xa = x0 - 1 + c1, xb = x0 - 1 + c2;        // parity is all that matters
-        const float sa = wline ? a.scale : a.scale * a.lambda;
-        const float sb = a.scale * a.lambda;
-        float* oa = obuf + (fa * CC + c1) * OS;
-        float* ob = obuf + (fb * CC + c2) * OS;
+        const int cc = tid % WL, t = tid / WL;
+#pragma unroll
+        for (int r = 0; r < L::E; ++r) {
+            const int  y  = t + r * (N / L::R1);
+            const bool lo = y <= N / 2;
+            const int  ys = lo ? y : N - y;                  // rows N-y are conjugates of rows y
+            float2 p = tile[CF::FIELD + ys * CC + cc];       // Dy
+            float2 q = tile[ys * CC + cc];                   // Dx
+            if (!lo) { p.y = -p.y; q.y = -q.y; }
+            v[r] = make_float2(p.x - q.y, p.y + q.x);        // p + i*q
+        }
+        __syncthreads();                                     // fields Dx, Dy consumed
+        line_fft<L, +1>(v, xbuf1 + cc * L::NPAD, tw_s, t);   // ends with a block barrier
+        const int   xa = x0 - 1 + cc;                        // parity is all that matters
+        const float sa = a.scale, sb = a.scale * a.lambda;
 #pragma unroll
         for (int e = 0; e < L::E; ++e) {
-            const int y = LineOut<L>::pos(t, e);
-            oa[y] = ((xa + y) & 1) ? -sa * v[e].x : sa * v[e].x;
-            ob[y] = ((xb + y) & 1) ? -sb * v[e].y : sb * v[e].y;
+            const int   y  = LineOut<L>::pos(t, e);
+            const float sg = ((xa + y) & 1) ? -1.0f : 1.0f;
+            sy[cc * OS + y] = sg * sa * v[e].x;
+            sx[cc * OS + y] = sg * sb * v[e].y;
+        }
+    }
+    // ---- round 2: Dz(c) + i*Dz(c+1) lines on the first ZL*G threads.
+    {
+        const bool zact = tid < ZL * L::G;
+        const int  p2 = tid % ZL, t = tid / ZL;
+        if (zact) {
+#pragma unroll
+            for (int r = 0; r < L::E; ++r) {
+                const int  y  = t + r * (N / L::R1);
+                const bool lo = y <= N / 2;
+                const int  ys = lo ? y : N - y;
+                const float4 z2 = *reinterpret_cast<const float4*>(tile + 2 * CF::FIELD + ys * CC + 2 * p2);
+                float2 p = make_float2(z2.x, z2.y), q = make_float2(z2.z, z2.w);
+                if (!lo) { p.y = -p.y; q.y = -q.y; }
+                v[r] = make_float2(p.x - q.y, p.y + q.x);
+            }
+        }
+        __syncthreads();                                     // field Dz consumed
+        line_fft<L, +1>(v, xbuf2 + (zact ? p2 : 0) * L::NPAD, tw_s, t, zact);
+        if (zact) {
+            const int   xa = x0 - 1 + 2 * p2;
+            const float sb = a.scale * a.lambda;
+#pragma unroll
+            for (int e = 0; e < L::E; ++e) {
+                const int   y  = LineOut<L>::pos(t, e);
+                const float sg = ((xa + y) & 1) ? -1.0f : 1.0f;
+                sz[(2 * p2) * OS + y]     = sg * sb * v[e].x;
+                sz[(2 * p2 + 1) * OS + y] = -sg * sb * v[e].y;
+            }
         }
     }
     __syncthreads();
 
-    // Epilogue: outputs, Sobel normal on Dy, Jacobian of x - (Dx, Dz).
-    const float* sx = obuf;
-    const float* sy = obuf + CC * OS;
-    const float* sz = obuf + 2 * CC * OS;
-    for (int i = threadIdx.x; i < C * N; i += CC_::THREADS) {
-        const int c = i % C, y = i / C;
+    // Epilogue: four rows of one column per thread, read as float4 with the
+    // neighbouring rows as scalars; Sobel normal on Dy and the Jacobian of
+    // x - (Dx, Dz).
+    for (int i = tid; i < C * (N / 4); i += CF::THREADS) {
+        const int c = i % C, y0 = 4 * (i / C);
         const int cc = c + 1;
-        const int ym = (y - 1) & (N - 1), yn = (y + 1) & (N - 1);
-        const float z0 = sy[(cc - 1) * OS + ym], z1 = sy[cc * OS + ym], z2 = sy[(cc + 1) * OS + ym];
-        const float z3 = sy[(cc - 1) * OS + y], zc = sy[cc * OS + y], z4 = sy[(cc + 1) * OS + y];
-        const float z5 = sy[(cc - 1) * OS + yn], z6 = sy[cc * OS + yn], z7 = sy[(cc + 1) * OS + yn];
-        const float nz = z0 + 2.0f * z1 + z2 - z5 - 2.0f * z6 - z7;
-        const float nx = z0 + 2.0f * z3 + z5 - z2 - 2.0f * z4 - z7;
-        const float rn = rsqrtf(nx * nx + 1.0f + nz * nz);
-        const float vx = sx[cc * OS + y], vz = sz[cc * OS + y];
-        const float dxx = (sx[(cc + 1) * OS + y] - sx[(cc - 1) * OS + y]) * a.inv2d;
-        const float dxz = (sx[cc * OS + yn] - sx[cc * OS + ym]) * a.inv2d;
-        const float dzx = (sz[(cc + 1) * OS + y] - sz[(cc - 1) * OS + y]) * a.inv2d;
-        const float dzz = (sz[cc * OS + yn] - sz[cc * OS + ym]) * a.inv2d;
-        const size_t o = (size_t)y * N + x0 + c;
-        a.dx[o] = vx;
-        a.dy[o] = zc;
-        a.dz[o] = vz;
-        // J = (1 - dxx)(1 - dzz) - dxz*dzx, formed as 1 + deviation so that the
-        // only rounding at the scale of 1 is the final add
-        const float dJ = (dxx * dzz - dxz * dzx) - dxx - dzz;
-        a.nj[o] = make_float4(nx * rn, rn, nz * rn, 1.0f + dJ);
+        const int ym = (y0 - 1) & (N - 1), yn = (y0 + 4) & (N - 1);
+        float Y[3][6], X[6], Z[6], XL[4], XR[4], ZL4[4], ZR4[4];
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+            const float* col = sy + (cc - 1 + d) * OS;
+            const float4 m4 = *reinterpret_cast<const float4*>(col + y0);
+            Y[d][0] = col[ym]; Y[d][1] = m4.x; Y[d][2] = m4.y; Y[d][3] = m4.z; Y[d][4] = m4.w; Y[d][5] = col[yn];
+        }
+        {
+            const float* col = sx + cc * OS;
+            const float4 m4 = *reinterpret_cast<const float4*>(col + y0);
+            X[0] = col[ym]; X[1] = m4.x; X[2] = m4.y; X[3] = m4.z; X[4] = m4.w; X[5] = col[yn];
+            const float4 l4 = *reinterpret_cast<const float4*>(sx + (cc - 1) * OS + y0);
+            const float4 r4 = *reinterpret_cast<const float4*>(sx + (cc + 1) * OS + y0);
+            XL[0] = l4.x; XL[1] = l4.y; XL[2] = l4.z; XL[3] = l4.w;
+            XR[0] = r4.x; XR[1] = r4.y; XR[2] = r4.z; XR[3] = r4.w;
+        }
+        {
+            const float* col = sz + cc * OS;
+            const float4 m4 = *reinterpret_cast<const float4*>(col + y0);
+            Z[0] = col[ym]; Z[1] = m4.x; Z[2] = m4.y; Z[3] = m4.z; Z[4] = m4.w; Z[5] = col[yn];
+            const float4 l4 = *reinterpret_cast<const float4*>(sz + (cc - 1) * OS + y0);
+            const float4 r4 = *reinterpret_cast<const float4*>(sz + (cc + 1) * OS + y0);
+            ZL4[0] = l4.x; ZL4[1] = l4.y; ZL4[2] = l4.z; ZL4[3] = l4.w;
+            ZR4[0] = r4.x; ZR4[1] = r4.y; ZR4[2] = r4.z; ZR4[3] = r4.w;
+        }
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            // taps z0..z7 (normal_map_cs.glsl:37-44) at rows k (y-1), k+1 (y), k+2 (y+1)
+            const float z0 = Y[0][k], z1 = Y[1][k], z2 = Y[2][k];
+            const float z3 = Y[0][k + 1], z4 = Y[2][k + 1];
+            const float z5 = Y[0][k + 2], z6 = Y[1][k + 2], z7 = Y[2][k + 2];
+            const float nz = z0 + 2.0f * z1 + z2 - z5 - 2.0f * z6 - z7;
+            const float nx = z0 + 2.0f * z3 + z5 - z2 - 2.0f * z4 - z7;
+            const float rn = rsqrtf(nx * nx + 1.0f + nz * nz);
+            const float dxx = (XR[k] - XL[k]) * a.inv2d;
+            const float dxz = (X[k + 2] - X[k]) * a.inv2d;
+            const float dzx = (ZR4[k] - ZL4[k]) * a.inv2d;
+            const float dzz = (Z[k + 2] - Z[k]) * a.inv2d;
+            // J = (1 - dxx)(1 - dzz) - dxz*dzx, formed as 1 + deviation so that the
+            // only rounding at the scale of 1 is the final add
+            const float dJ = (dxx * dzz - dxz * dzx) - dxx - dzz;
+            const size_t o = (size_t)(y0 + k) * N + x0 + c;
+            a.dx[o] = X[k + 1];
+            a.dy[o] = Y[1][k + 1];
+            a.dz[o] = Z[k + 1];
+            a.nj[o] = make_float4(nx * rn, rn, nz * rn, 1.0f + dJ);
+        }
     }
 }
 
@@ -313,75 +413,91 @@ template <int N>
 static cudaError_t row_pass_n(const RowArgs& a, cudaStream_t s)
 {
     using RC = RowCfg<N>;
-    static bool attr = false;
-    if (!attr) {
+    static int grid = 0;
+    if (!grid) {
         cudaError_t e = cudaFuncSetAttribute(k_row_pass<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)RC::SMEM);
         if (e != cudaSuccess) return e;
-        attr = true;
+        int per_sm = 0, dev = 0, sms = 0;
+        if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_row_pass<N>, RC::THREADS, RC::SMEM)) != cudaSuccess)
+            return e;
+        if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+        if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+        if (per_sm < 1) return cudaErrorInvalidConfiguration;
+        grid = per_sm * sms < RC::ITEMS ? per_sm * sms : RC::ITEMS;
     }
-    k_row_pass<N><<<RC::GRID, RC::THREADS, RC::SMEM, s>>>(a);
+    k_row_pass<N><<<grid, RC::THREADS, RC::SMEM, s>>>(a);
     return cudaGetLastError();
 }
 
 template <int N>
-static cudaError_t col_pass_n(const ColArgs& a, cudaStream_t s)
+static cudaError_t col_pass_n(const ColArgs& a, cudaStream_t s, bool pdl)
 {
-    using CC = ColCfg<N>;
+    using CF = ColCfg<N>;
     static bool attr = false;
     if (!attr) {
-        cudaError_t e = cudaFuncSetAttribute(k_col_pass<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)CC::SMEM);
+        cudaError_t e = cudaFuncSetAttribute(k_col_pass<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)CF::SMEM);
         if (e != cudaSuccess) return e;
         attr = true;
     }
-    k_col_pass<N><<<CC::GRID, CC::THREADS, CC::SMEM, s>>>(a);
-    return cudaGetLastError();
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim          = dim3(CF::GRID);
+    cfg.blockDim         = dim3(CF::THREADS);
+    cfg.dynamicSmemBytes = CF::SMEM;
+    cfg.stream           = s;
+    cudaLaunchAttribute at[1];
+    at[0].id                                         = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs    = at;
+    cfg.numAttrs = pdl ? 1 : 0;
+    return cudaLaunchKernelEx(&cfg, k_col_pass<N>, a);
 }
 
-template <int N> struct RowSmem { static constexpr size_t v = RowCfg<N>::SMEM; };
-template <int N> struct ColSmem { static constexpr size_t v = ColCfg<N>::SMEM; };
+template <int N>
+static void col_box_n(unsigned box[2])
+{
+    box[0] = 2 * ColCfg<N>::CC;
+    box[1] = ColCfg<N>::BR;
+}
+
+#define OCEAN_FOR_EACH_N(M) M(32) M(64) M(128) M(256) M(512) M(1024) M(2048)
 
 cudaError_t launch_row_pass(int N, const RowArgs& a, cudaStream_t s)
 {
-#define ROWCALL(n) row_pass_n<n>(a, s)
     switch (N) {
-    case 32: return ROWCALL(32);
-    case 64: return ROWCALL(64);
-    case 128: return ROWCALL(128);
-    case 256: return ROWCALL(256);
-    case 512: return ROWCALL(512);
-    case 1024: return ROWCALL(1024);
-    case 2048: return ROWCALL(2048);
+#define CASE(n) case n: return row_pass_n<n>(a, s);
+        OCEAN_FOR_EACH_N(CASE)
+#undef CASE
     default: return cudaErrorInvalidValue;
     }
-#undef ROWCALL
 }
 
-cudaError_t launch_col_pass(int N, const ColArgs& a, cudaStream_t s)
+cudaError_t launch_col_pass(int N, const ColArgs& a, cudaStream_t s, bool pdl)
 {
-#define COLCALL(n) col_pass_n<n>(a, s)
     switch (N) {
-    case 32: return COLCALL(32);
-    case 64: return COLCALL(64);
-    case 128: return COLCALL(128);
-    case 256: return COLCALL(256);
-    case 512: return COLCALL(512);
-    case 1024: return COLCALL(1024);
-    case 2048: return COLCALL(2048);
+#define CASE(n) case n: return col_pass_n<n>(a, s, pdl);
+        OCEAN_FOR_EACH_N(CASE)
+#undef CASE
     default: return cudaErrorInvalidValue;
     }
-#undef COLCALL
+}
+
+void col_pass_box(int N, unsigned box[2])
+{
+    box[0] = box[1] = 0;
+    switch (N) {
+#define CASE(n) case n: col_box_n<n>(box); break;
+        OCEAN_FOR_EACH_N(CASE)
+#undef CASE
+    default: break;
+    }
 }
 
 size_t row_pass_smem(int N)
 {
     switch (N) {
-    case 32: return RowSmem<32>::v;
-    case 64: return RowSmem<64>::v;
-    case 128: return RowSmem<128>::v;
-    case 256: return RowSmem<256>::v;
-    case 512: return RowSmem<512>::v;
-    case 1024: return RowSmem<1024>::v;
-    case 2048: return RowSmem<2048>::v;
+#define CASE(n) case n: return RowCfg<n>::SMEM;
+        OCEAN_FOR_EACH_N(CASE)
+#undef CASE
     default: return 0;
     }
 }
@@ -389,13 +505,9 @@ size_t row_pass_smem(int N)
 size_t col_pass_smem(int N)
 {
     switch (N) {
-    case 32: return ColSmem<32>::v;
-    case 64: return ColSmem<64>::v;
-    case 128: return ColSmem<128>::v;
-    case 256: return ColSmem<256>::v;
-    case 512: return ColSmem<512>::v;
-    case 1024: return ColSmem<1024>::v;
-    case 2048: return ColSmem<2048>::v;
+#define CASE(n) case n: return ColCfg<n>::SMEM;
+        OCEAN_FOR_EACH_N(CASE)
+#undef CASE
     default: return 0;
     }
 }

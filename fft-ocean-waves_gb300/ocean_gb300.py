@@ -25,6 +25,7 @@ OCEAN_ERR_INVALID = -1
 OCEAN_ERR_CUDA = -2
 OCEAN_ERR_NOMEM = -3
 OCEAN_ERR_UNSUPPORTED = -4
+OCEAN_ERR_TIMEOUT = -5
 OCEAN_FLAG_LITERAL_CONJ = 1
 
 # Every entry point include/ocean.h declares (checked by the CPU tests).
@@ -33,8 +34,9 @@ EXPORTS = [
     "ocean_update_columns", "ocean_get_outputs",
     "ocean_set_params", "ocean_get_params", "ocean_get_h0", "ocean_set_h0", "ocean_compute_h0",
     "ocean_fill_noise", "ocean_bit_reversed_indices", "ocean_butterfly_table", "ocean_last_error",
-    "ocean_version",
+    "ocean_version", "ocean_backward", "ocean_device_status",
 ]
+OCEAN_GRAD_ACCUMULATE = 1
 
 
 class OceanError(RuntimeError):
@@ -51,6 +53,11 @@ class ocean_params(C.Structure):
 
 class ocean_outputs(C.Structure):
     _fields_ = [("dx", C.c_void_p), ("dy", C.c_void_p), ("dz", C.c_void_p), ("normal_j", C.c_void_p)]
+
+
+class ocean_grads(C.Structure):
+    _fields_ = [("dA", C.c_double), ("dV", C.c_double), ("dtheta", C.c_double), ("dlambda", C.c_double),
+                ("dh0", C.c_void_p)]
 
 
 @dataclasses.dataclass
@@ -108,6 +115,8 @@ def load() -> C.CDLL:
     L.ocean_fill_noise.argtypes = [C.c_uint64, C.c_int32, P(C.c_float)]
     L.ocean_bit_reversed_indices.argtypes = [C.c_int32, P(C.c_int32)]
     L.ocean_butterfly_table.argtypes = [C.c_int32, P(C.c_float)]
+    L.ocean_backward.argtypes = [vp, P(C.c_double), C.c_int32, vp, vp, vp, C.c_uint32, P(ocean_grads), vp]
+    L.ocean_device_status.argtypes = [vp, vp]
     L.ocean_last_error.restype = C.c_char_p
     for name in EXPORTS:
         if name not in ("ocean_destroy", "ocean_last_error"):
@@ -205,6 +214,20 @@ class Ocean:
             return
         o = ocean_outputs(_addr(dx), _addr(dy), _addr(dz), _addr(normal_j))
         check(load().ocean_update_columns(self._h, C.byref(o), _stream(stream)))
+
+    def backward(self, times, g_dx=None, g_dy=None, g_dz=None, dh0=None, accumulate=False, stream=None) -> dict:
+        """Gradients for upstream dL/d(dx, dy, dz) of shape (T, N, N) (device
+        tensors or addresses; None = zero).  dh0 (device N*N*4) receives
+        dL/dh0 when given.  Returns dA, dV, dtheta, dlambda."""
+        ts = (C.c_double * len(times))(*[float(t) for t in times])
+        g = ocean_grads(0.0, 0.0, 0.0, 0.0, _addr(dh0))
+        check(load().ocean_backward(self._h, ts, len(times), _addr(g_dx), _addr(g_dy), _addr(g_dz),
+                                    OCEAN_GRAD_ACCUMULATE if accumulate else 0, C.byref(g), _stream(stream)))
+        return {"dA": g.dA, "dV": g.dV, "dtheta": g.dtheta, "dlambda": g.dlambda}
+
+    def device_status(self, stream=None) -> None:
+        """Synchronise and raise if a kernel reported a bounded-wait time-out."""
+        check(load().ocean_device_status(self._h, _stream(stream)))
 
     def outputs(self) -> dict:
         o = ocean_outputs()

@@ -37,6 +37,7 @@ extern "C" {
 #define OCEAN_ERR_CUDA -2        /* a CUDA runtime call or launch failed   */
 #define OCEAN_ERR_NOMEM -3       /* device or host allocation failed       */
 #define OCEAN_ERR_UNSUPPORTED -4 /* no kernel for this device / size       */
+#define OCEAN_ERR_TIMEOUT -5     /* a kernel's bounded wait timed out       */
 
 #define OCEAN_MIN_N 32
 #define OCEAN_MAX_N 2048
@@ -106,6 +107,12 @@ OCEAN_API int ocean_update(ocean_t* ocean, double t, const ocean_outputs* out, v
 OCEAN_API int ocean_update_rows(ocean_t* ocean, double t, void* stream);
 OCEAN_API int ocean_update_columns(ocean_t* ocean, const ocean_outputs* out, void* stream);
 
+/* Synchronise `stream` and report (and clear) the handle's device status:
+ * OCEAN_ERR_TIMEOUT if a kernel gave up a bounded wait for its TMA copies
+ * (its outputs for that frame are incomplete), else OCEAN_OK.  The reference
+ * never checks its dispatches. */
+OCEAN_API int ocean_device_status(ocean_t* ocean, void* stream);
+
 /* Handle-owned output buffers (allocated on first use); the headless
  * stand-ins for the reference's GL textures m_dx/m_dy/m_dz/m_normal_map. */
 OCEAN_API int ocean_get_outputs(ocean_t* ocean, ocean_outputs* out);
@@ -139,6 +146,37 @@ OCEAN_API int ocean_fill_noise(uint64_t seed, int32_t N, float* host_out);
  * twiddles and do not need either. */
 OCEAN_API int ocean_bit_reversed_indices(int32_t N, int32_t* host_out);
 OCEAN_API int ocean_butterfly_table(int32_t N, float* host_out);
+
+/* ---- Adjoint --------------------------------------------------------- */
+
+/* Flags for ocean_backward */
+#define OCEAN_GRAD_ACCUMULATE 1u /* add into *grads and dh0 instead of overwriting */
+
+/* Gradients of a scalar loss L with respect to the spectrum parameters and,
+ * optionally, the per-mode spectrum state.  Complex gradients use the
+ * convention dL/dRe + i dL/dIm. */
+typedef struct ocean_grads {
+    double dA;       /* dL/d amplitude                                            */
+    double dV;       /* dL/d wind speed                                           */
+    double dtheta;   /* dL/d wind direction angle (w = (cos theta, sin theta))    */
+    double dlambda;  /* dL/d choppiness                                           */
+    float* dh0;      /* optional device N*N*4 (layout of ocean_get_h0), or NULL   */
+} ocean_grads;
+
+/* Adjoint of ocean_update's displacement outputs over T frames: given
+ * dL/d(dx, dy, dz) for frame times[j] (device, T*N*N floats each, frame-major;
+ * NULL = zero gradient for that field), compute the gradients above.  The
+ * frames are not stored or recomputed: the adjoint reads only h0 (forward
+ * DFT as the transpose of the inverse butterfly network, conjugate phase
+ * rotation, transpose of the choppy multiply, chain through the Phillips
+ * amplitude).  Parameter gradients hold l, L and g fixed, exclude modes on the
+ * +-4000 clamp and assume h0 was built from the current parameters (not set
+ * with ocean_set_h0).  The normal/Jacobian map carries no gradient.
+ * Two kernel launches per chunk of <= 64 frames; scratch is allocated on
+ * first use (at most 512 MiB).  Returns after the scalar gradients are on the
+ * host (synchronises `stream`). No counterpart in the reference. */
+OCEAN_API int ocean_backward(ocean_t* ocean, const double* times, int32_t T, const float* g_dx, const float* g_dy,
+                             const float* g_dz, uint32_t flags, ocean_grads* grads, void* stream);
 
 OCEAN_API const char* ocean_last_error(void);
 OCEAN_API int ocean_version(void);
