@@ -18,7 +18,7 @@
 #include <string>
 #include <vector>
 
-#include "../../include/ocean.h"
+#include "ocean.h"
 #include "ocean_internal.h"
 
 namespace {

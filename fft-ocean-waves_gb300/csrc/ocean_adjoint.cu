@@ -130,9 +130,11 @@ struct AdjRowCfg {
     static constexpr int THREADS = LINES * L::G;
     static constexpr int H       = N / 2 + 1;
     static constexpr int LS      = L::NPAD + 1;
-    // tw | line buffers | h0 rows [PAIRS][2][N] | accumulators [PAIRS][2][N]
-    static constexpr size_t SMEM = sizeof(float2) * (N + (size_t)LINES * LS) + sizeof(float4) * 4 * (size_t)PAIRS * N;
-    static constexpr int GRID    = (H + PAIRS - 1) / PAIRS;
+    // tw | line buffers | h0 rows [PAIRS][2][N] | accumulators [PAIRS][2][N];
+    // the float4 arrays start on a 128-byte boundary (LS is odd, LINES may be)
+    static constexpr size_t F4OFF = ((size_t)(N + LINES * LS) + 15) / 16 * 16;   // in float2
+    static constexpr size_t SMEM  = sizeof(float2) * F4OFF + sizeof(float4) * 4 * (size_t)PAIRS * N + 128;
+    static constexpr int GRID     = (H + PAIRS - 1) / PAIRS;
 };
 
 __device__ __forceinline__ double block_sum(double v, double* red)
@@ -155,10 +157,11 @@ __global__ void __launch_bounds__(AdjRowCfg<N>::THREADS) k_adj_row_pass(AdjRowAr
     using CF = AdjRowCfg<N>;
     using L  = typename CF::L;
     constexpr int H = CF::H, LS = CF::LS, PAIRS = CF::PAIRS;
-    extern __shared__ float2 smem[];
+    extern __shared__ unsigned char smem_raw[];
+    float2* smem = reinterpret_cast<float2*>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
     float2* tw_s = smem;
     float2* buf  = smem + N;
-    float4* h0s  = reinterpret_cast<float4*>(buf + CF::LINES * LS);   // [PAIRS][2][N]
+    float4* h0s  = reinterpret_cast<float4*>(smem + CF::F4OFF);          // [PAIRS][2][N], 128-byte aligned
     float4* acc  = h0s + 2 * PAIRS * N;                                // [PAIRS][2][N]
     __shared__ double red[32];
 
