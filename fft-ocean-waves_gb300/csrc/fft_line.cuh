@@ -132,9 +132,11 @@ template <> struct LineFor<32>   { using type = LineCfg<32, 8, 4>; };
 template <> struct LineFor<64>   { using type = LineCfg<64, 8, 8>; };
 template <> struct LineFor<128>  { using type = LineCfg<128, 16, 8>; };
 template <> struct LineFor<256>  { using type = LineCfg<256, 16, 16>; };
-template <> struct LineFor<512>  { using type = LineCfg<512, 32, 16>; };
-template <> struct LineFor<1024> { using type = LineCfg<1024, 32, 32>; };
-template <> struct LineFor<2048> { using type = LineCfg<2048, 32, 8, 8>; };
+// 16-point first passes from N = 512 up: ~95 registers per thread instead of
+// ~168 for 32-point ones, so twice the threads per line fit on an SM.
+template <> struct LineFor<512>  { using type = LineCfg<512, 16, 16, 2>; };
+template <> struct LineFor<1024> { using type = LineCfg<1024, 16, 16, 4>; };
+template <> struct LineFor<2048> { using type = LineCfg<2048, 16, 16, 8>; };
 
 // One exchange + pass: the registers hold the outputs of a pass of radix RP
 // with stride NSP; they are written to `buf`, re-read as the inputs of a pass

@@ -151,19 +151,30 @@ __global__ void __launch_bounds__(RowCfg<N>::THREADS) k_row_pass(RowArgs a)
         if (!block_wait(&bars[s], (phase_bits >> s) & 1u, &wait_ok, a.status)) return;
         phase_bits ^= 1u << s;
 
-        // Prepass: h(k,t) for the pair's two rows, once per mode pair; the
-        // mirror mode (N-x, N-y') shares |k| and so the phase.  hy[pl][0][x] is
-        // the mode (x, y'), hy[pl][1][x] the mode (N-x, N-y').
+        // Prepass: h(k,t) for the pair's two rows.  hy[pl][0][x] is the mode
+        // (x, y'), hy[pl][1][x] the mode (N-x, N-y').  The four modes (x, y'),
+        // (N-x, y'), (N-x, N-y'), (x, N-y') share |k| (ix^2 and iz^2 are even)
+        // and so the phase, which is computed once for all four.
         float2* hy = work;
-        for (int i = tid; i < RC::PAIRS * N; i += RC::THREADS) {
-            const int pl = i / N, x = i % N;
+        constexpr int HX = N / 2 + 1;
+        for (int i = tid; i < RC::PAIRS * HX; i += RC::THREADS) {
+            const int pl = i / HX, x = i % HX;
             const int yp = item * RC::PAIRS + pl;
             if (yp > N / 2) continue;
+            const int xm = (N - x) & (N - 1);
             const int ix = x - N / 2, iz = yp - N / 2;
             float c, sn;
             mode_phase(ix * ix + iz * iz, a.fc, c, sn);
-            hy[(pl * 2 + 0) * N + x] = evolve(stage[(pl * 2 + 0) * N + x], c, sn, a.literal_conj);
-            hy[(pl * 2 + 1) * N + x] = evolve(stage[(pl * 2 + 1) * N + ((N - x) & (N - 1))], c, sn, a.literal_conj);
+            const float4* r0 = stage + (pl * 2 + 0) * N;
+            const float4* r1 = stage + (pl * 2 + 1) * N;
+            float2*       h0r = hy + (pl * 2 + 0) * N;
+            float2*       h1r = hy + (pl * 2 + 1) * N;
+            h0r[x] = evolve(r0[x], c, sn, a.literal_conj);
+            h1r[x] = evolve(r1[xm], c, sn, a.literal_conj);
+            if (xm != x) {
+                h0r[xm] = evolve(r0[xm], c, sn, a.literal_conj);
+                h1r[xm] = evolve(r1[x], c, sn, a.literal_conj);
+            }
         }
         __syncthreads();                                   // hy complete, ring stage s consumed
         if (tid == 0) {
@@ -284,10 +295,10 @@ __global__ void __launch_bounds__(ColCfg<N>::THREADS) k_col_pass(const __grid_co
     if (!block_wait(&bar, 0, &wait_ok, a.status)) return;
 
     float2 v[L::E];
-    // ---- round 1: column lines Dy + i*Dx.  Thread -> (column, t) with the
-    // columns fastest across lanes: a warp reads consecutive shared words.
+    // ---- round 1: column lines Dy + i*Dx, one line per G consecutive threads
+    // (a warp never spans two lines' exchange buffers).
     {
-        const int cc = tid % WL, t = tid / WL;
+        const int cc = tid / L::G, t = tid % L::G;
 #pragma unroll
         for (int r = 0; r < L::E; ++r) {
             const int  y  = t + r * (N / L::R1);
@@ -313,7 +324,7 @@ __global__ void __launch_bounds__(ColCfg<N>::THREADS) k_col_pass(const __grid_co
     // ---- round 2: Dz(c) + i*Dz(c+1) lines on the first ZL*G threads.
     {
         const bool zact = tid < ZL * L::G;
-        const int  p2 = tid % ZL, t = tid / ZL;
+        const int  p2 = tid / L::G, t = tid % L::G;
         if (zact) {
 #pragma unroll
             for (int r = 0; r < L::E; ++r) {
@@ -342,59 +353,64 @@ __global__ void __launch_bounds__(ColCfg<N>::THREADS) k_col_pass(const __grid_co
     }
     __syncthreads();
 
-    // Epilogue: four rows of one column per thread, read as float4 with the
-    // neighbouring rows as scalars; Sobel normal on Dy and the Jacobian of
-    // x - (Dx, Dz).
-    for (int i = tid; i < C * (N / 4); i += CF::THREADS) {
-        const int c = i % C, y0 = 4 * (i / C);
-        const int cc = c + 1;
+    // Epilogue: a 4-row x 2-column block per thread (float4 shared reads down
+    // the staged columns, float2 global stores across them); Sobel normal on Dy
+    // and the Jacobian of x - (Dx, Dz).
+    for (int i = tid; i < (C / 2) * (N / 4); i += CF::THREADS) {
+        const int cp = i % (C / 2), y0 = 4 * (i / (C / 2));
+        const int cb = 2 * cp + 1;                                // staged column of output column 2cp
         const int ym = (y0 - 1) & (N - 1), yn = (y0 + 4) & (N - 1);
-        float Y[3][6], X[6], Z[6], XL[4], XR[4], ZL4[4], ZR4[4];
+        // Y[d][k]: Dy at staged column cb-1+d, rows y0-1+k (d < 4, k < 6)
+        float Y[4][6], X[2][6], Z[2][6], XS[2][4], ZS[2][4];
 #pragma unroll
-        for (int d = 0; d < 3; ++d) {
-            const float* col = sy + (cc - 1 + d) * OS;
+        for (int d = 0; d < 4; ++d) {
+            const float* col = sy + (cb - 1 + d) * OS;
             const float4 m4 = *reinterpret_cast<const float4*>(col + y0);
             Y[d][0] = col[ym]; Y[d][1] = m4.x; Y[d][2] = m4.y; Y[d][3] = m4.z; Y[d][4] = m4.w; Y[d][5] = col[yn];
         }
-        {
-            const float* col = sx + cc * OS;
-            const float4 m4 = *reinterpret_cast<const float4*>(col + y0);
-            X[0] = col[ym]; X[1] = m4.x; X[2] = m4.y; X[3] = m4.z; X[4] = m4.w; X[5] = col[yn];
-            const float4 l4 = *reinterpret_cast<const float4*>(sx + (cc - 1) * OS + y0);
-            const float4 r4 = *reinterpret_cast<const float4*>(sx + (cc + 1) * OS + y0);
-            XL[0] = l4.x; XL[1] = l4.y; XL[2] = l4.z; XL[3] = l4.w;
-            XR[0] = r4.x; XR[1] = r4.y; XR[2] = r4.z; XR[3] = r4.w;
-        }
-        {
-            const float* col = sz + cc * OS;
-            const float4 m4 = *reinterpret_cast<const float4*>(col + y0);
-            Z[0] = col[ym]; Z[1] = m4.x; Z[2] = m4.y; Z[3] = m4.z; Z[4] = m4.w; Z[5] = col[yn];
-            const float4 l4 = *reinterpret_cast<const float4*>(sz + (cc - 1) * OS + y0);
-            const float4 r4 = *reinterpret_cast<const float4*>(sz + (cc + 1) * OS + y0);
-            ZL4[0] = l4.x; ZL4[1] = l4.y; ZL4[2] = l4.z; ZL4[3] = l4.w;
-            ZR4[0] = r4.x; ZR4[1] = r4.y; ZR4[2] = r4.z; ZR4[3] = r4.w;
+#pragma unroll
+        for (int d = 0; d < 2; ++d) {
+            const float* cx = sx + (cb + d) * OS;
+            const float4 mx = *reinterpret_cast<const float4*>(cx + y0);
+            X[d][0] = cx[ym]; X[d][1] = mx.x; X[d][2] = mx.y; X[d][3] = mx.z; X[d][4] = mx.w; X[d][5] = cx[yn];
+            const float* cz = sz + (cb + d) * OS;
+            const float4 mz = *reinterpret_cast<const float4*>(cz + y0);
+            Z[d][0] = cz[ym]; Z[d][1] = mz.x; Z[d][2] = mz.y; Z[d][3] = mz.z; Z[d][4] = mz.w; Z[d][5] = cz[yn];
+            // the outer x-neighbours: staged columns cb-1 (d = 0) and cb+2 (d = 1)
+            const float4 ox = *reinterpret_cast<const float4*>(sx + (cb - 1 + 3 * d) * OS + y0);
+            const float4 oz = *reinterpret_cast<const float4*>(sz + (cb - 1 + 3 * d) * OS + y0);
+            XS[d][0] = ox.x; XS[d][1] = ox.y; XS[d][2] = ox.z; XS[d][3] = ox.w;
+            ZS[d][0] = oz.x; ZS[d][1] = oz.y; ZS[d][2] = oz.z; ZS[d][3] = oz.w;
         }
 #pragma unroll
         for (int k = 0; k < 4; ++k) {
-            // taps z0..z7 (normal_map_cs.glsl:37-44) at rows k (y-1), k+1 (y), k+2 (y+1)
-            const float z0 = Y[0][k], z1 = Y[1][k], z2 = Y[2][k];
-            const float z3 = Y[0][k + 1], z4 = Y[2][k + 1];
-            const float z5 = Y[0][k + 2], z6 = Y[1][k + 2], z7 = Y[2][k + 2];
-            const float nz = z0 + 2.0f * z1 + z2 - z5 - 2.0f * z6 - z7;
-            const float nx = z0 + 2.0f * z3 + z5 - z2 - 2.0f * z4 - z7;
-            const float rn = rsqrtf(nx * nx + 1.0f + nz * nz);
-            const float dxx = (XR[k] - XL[k]) * a.inv2d;
-            const float dxz = (X[k + 2] - X[k]) * a.inv2d;
-            const float dzx = (ZR4[k] - ZL4[k]) * a.inv2d;
-            const float dzz = (Z[k + 2] - Z[k]) * a.inv2d;
-            // J = (1 - dxx)(1 - dzz) - dxz*dzx, formed as 1 + deviation so that the
-            // only rounding at the scale of 1 is the final add
-            const float dJ = (dxx * dzz - dxz * dzx) - dxx - dzz;
-            const size_t o = (size_t)(y0 + k) * N + x0 + c;
-            a.dx[o] = X[k + 1];
-            a.dy[o] = Y[1][k + 1];
-            a.dz[o] = Z[k + 1];
-            a.nj[o] = make_float4(nx * rn, rn, nz * rn, 1.0f + dJ);
+            float4 njv[2];
+#pragma unroll
+            for (int d = 0; d < 2; ++d) {
+                // taps z0..z7 (normal_map_cs.glsl:37-44) around (column d, row k+1)
+                const float z0 = Y[d][k], z1 = Y[d + 1][k], z2 = Y[d + 2][k];
+                const float z3 = Y[d][k + 1], z4 = Y[d + 2][k + 1];
+                const float z5 = Y[d][k + 2], z6 = Y[d + 1][k + 2], z7 = Y[d + 2][k + 2];
+                const float nz = z0 + 2.0f * z1 + z2 - z5 - 2.0f * z6 - z7;
+                const float nx = z0 + 2.0f * z3 + z5 - z2 - 2.0f * z4 - z7;
+                const float rn = rsqrtf(nx * nx + 1.0f + nz * nz);
+                const float xl = d == 0 ? XS[0][k] : X[0][k + 1], xr = d == 0 ? X[1][k + 1] : XS[1][k];
+                const float zl = d == 0 ? ZS[0][k] : Z[0][k + 1], zr = d == 0 ? Z[1][k + 1] : ZS[1][k];
+                const float dxx = (xr - xl) * a.inv2d;
+                const float dxz = (X[d][k + 2] - X[d][k]) * a.inv2d;
+                const float dzx = (zr - zl) * a.inv2d;
+                const float dzz = (Z[d][k + 2] - Z[d][k]) * a.inv2d;
+                // J = (1 - dxx)(1 - dzz) - dxz*dzx, formed as 1 + deviation so that
+                // the only rounding at the scale of 1 is the final add
+                const float dJ = (dxx * dzz - dxz * dzx) - dxx - dzz;
+                njv[d] = make_float4(nx * rn, rn, nz * rn, 1.0f + dJ);
+            }
+            const size_t o = (size_t)(y0 + k) * N + x0 + 2 * cp;
+            *reinterpret_cast<float2*>(a.dx + o) = make_float2(X[0][k + 1], X[1][k + 1]);
+            *reinterpret_cast<float2*>(a.dy + o) = make_float2(Y[1][k + 1], Y[2][k + 1]);
+            *reinterpret_cast<float2*>(a.dz + o) = make_float2(Z[0][k + 1], Z[1][k + 1]);
+            a.nj[o]     = njv[0];
+            a.nj[o + 1] = njv[1];
         }
     }
 }

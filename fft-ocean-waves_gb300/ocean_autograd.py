@@ -54,8 +54,9 @@ class OceanParamFrames(torch.autograd.Function):
 
     @staticmethod
     def backward(ctx, gD):
-        gD = gD.contiguous()
-        r = ctx.oc.backward(ctx.times, gD[:, 0], gD[:, 1], gD[:, 2], stream=torch.cuda.current_stream())
+        # ocean_backward takes each field's gradients frame-major and contiguous
+        g = [gD[:, f].contiguous() for f in range(3)]
+        r = ctx.oc.backward(ctx.times, g[0], g[1], g[2], stream=torch.cuda.current_stream())
         g = torch.tensor([r["dA"], r["dV"], r["dtheta"], r["dlambda"]], dtype=torch.float64)
         return g, None, None
 
@@ -94,7 +95,7 @@ class OceanH0Loss(torch.autograd.Function):
         for j, t in enumerate(ctx.times):
             _frames(oc, [t], D)                        # recomputed from h0
             _frames(target, [t], Dt)
-            G = (D - Dt) * scale
-            oc.backward([t], G[:, 0], G[:, 1], G[:, 2], dh0=dh0, accumulate=j > 0,
+            G = (D - Dt) * scale                       # one frame: each field slice is contiguous
+            oc.backward([t], G[0, 0], G[0, 1], G[0, 2], dh0=dh0, accumulate=j > 0,
                         stream=torch.cuda.current_stream())
         return dh0, None, None, None

@@ -136,6 +136,8 @@ def _addr(x) -> int | None:
     if isinstance(x, int):
         return x
     if hasattr(x, "data_ptr"):
+        if hasattr(x, "is_contiguous") and not x.is_contiguous():
+            raise ValueError("device buffers passed to the C ABI must be contiguous")
         return x.data_ptr()
     raise TypeError(f"cannot take a device address of {type(x)}")
 

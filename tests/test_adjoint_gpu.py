@@ -98,13 +98,18 @@ def test_backward_null_fields(torch_cuda, ocean_lib, oracle_mod):
     with ocean_lib.Ocean(lp, seed=d["seed"]) as oc:
         r = oc.backward(times, None, torch_cuda.tensor(gy, device=dev), None, dh0=dh0)
     assert rel_l2(dh0.cpu().numpy(), dh0_ref) < 1e-5
-    assert r["dlambda"] == 0.0
+    # no Dx/Dz loss: dlambda is zero up to the FP32 residue of unpacking two
+    # real fields from one complex transform
+    assert abs(r["dlambda"]) < 1e-5 * max(abs(ref["dA"]), abs(ref["dV"]), abs(ref["dtheta"]))
     _check_params({k: r[k] for k in ("dA", "dV", "dtheta")} | {"dlambda": 0.0}, ref | {"dlambda": 0.0}, 1e-4)
 
 
 def test_parameter_gradients_vs_finite_differences(torch_cuda, ocean_lib, oracle_mod):
-    """Central differences (h = 1e-3 relative) of L = sum_t <g_t, D_t> with
-    the FP64 forward, against the GPU adjoint: 1e-4 relative."""
+    """Central differences (h = 1e-3 relative for A, V, lambda) of
+    L = sum_t <g_t, D_t> with the FP64 forward, against the GPU adjoint: 1e-4
+    relative.  theta uses an absolute step of 1e-5 rad: the amplitude goes
+    as |k^.w|, which has a kink where k^.w = 0, and a larger step straddles
+    the kinks of the modes near it."""
     N = 128
     d, op, lp = _setup(N)
     times = [0.4, 2.2]
@@ -133,7 +138,7 @@ def test_parameter_gradients_vs_finite_differences(torch_cuda, ocean_lib, oracle
         b[key] -= e
         fd[name] = (loss(a) - loss(b)) / (2 * e)
     th = math.atan2(base["wind_y"], base["wind_x"])
-    e = 1e-3 * th
+    e = 1e-5
     a, b = dict(base), dict(base)
     a["wind_x"], a["wind_y"] = math.cos(th + e), math.sin(th + e)
     b["wind_x"], b["wind_y"] = math.cos(th - e), math.sin(th - e)

@@ -82,7 +82,8 @@ def test_h0_loss_gradient_matches_oracle(torch_cuda, ocean_lib, oracle_mod):
 
 
 def test_parameter_fit_converges(torch_cuda, ocean_lib):
-    """200 Adam steps of the N=512 fit reduce the MSE by orders of magnitude."""
+    """200 Adam steps of the N=512 fit reach the noise floor of the target
+    (MSE = sigma^2 = 4e-4) from an initial MSE about 18x higher."""
     import ocean_autograd as oa
     torch = torch_cuda
     N, T = 512, 32
@@ -107,4 +108,6 @@ def test_parameter_fit_converges(torch_cuda, ocean_lib):
         opt.step()
         losses.append(float(loss))
     model.close()
-    assert losses[-1] < 0.05 * losses[0], (losses[0], losses[-1])
+    sigma2 = 0.02 ** 2
+    assert losses[0] > 10 * sigma2
+    assert losses[-1] < 1.05 * sigma2, (losses[0], losses[-1])
