@@ -302,10 +302,135 @@ def run_gpu(args, world, rank, local):
         "clocks": clocks,
         "wall_s_timed_region": round(wall, 4),
     }
+    if not args.no_extra:
+        out["adjoint"] = bench_adjoint(torch, og, dev, stream)
+        out["batched"] = bench_batched(torch, og, dev, stream, flush)
     if not args.no_cpu:
         out["cpu_baseline"] = cpu_baseline(N, args.cpu_seconds)
         out["err_vs_fp64"] = parity_check(N, frame, t_chk)
     return out
+
+
+def c4_params(og, A=3.0, V=22.0, theta_deg=50.0, lam=1.1):
+    import numpy as np
+    f = lambda v: float(np.float32(v))
+    a = math.radians(theta_deg)
+    return og.Params(N=512, L=1500.0, amplitude=A, wind_speed=V, wind_dir_x=f(math.cos(a)), wind_dir_y=f(math.sin(a)),
+                     choppiness=f(lam), suppression=f(0.1), gravity=f(9.81))
+
+
+def bench_adjoint(torch, og, dev, stream, reps=5):
+    """Parameter-fit workload: N=512, T=32 frames at dt=0.1 s.  Forward = the
+    32 frames into a (T, 3, N, N) buffer; backward = ocean_backward over the
+    32 frames' upstream gradients (one call, no stored or recomputed frames)."""
+    N, T = 512, 32
+    times = [0.1 * j for j in range(T)]
+    oc = og.Ocean(c4_params(og), seed=3)
+    D = torch.empty((T, 3, N, N), device=dev)
+    nj = torch.empty((N, N, 4), device=dev)
+    G = torch.randn((3, T, N, N), device=dev)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+    fw, bw = [], []
+    with torch.cuda.stream(stream):
+        for rep in range(reps + 2):
+            ev[0].record(stream)
+            for j, t in enumerate(times):
+                oc.update(t, D[j, 0], D[j, 1], D[j, 2], nj, stream=stream)
+            ev[1].record(stream)
+            oc.backward(times, G[0], G[1], G[2], stream=stream)
+            ev[2].record(stream)
+            torch.cuda.synchronize()
+            if rep >= 2:
+                fw.append(ev[0].elapsed_time(ev[1]))
+                bw.append(ev[1].elapsed_time(ev[2]))
+    oc.close()
+    f, b = sum(fw) / len(fw), sum(bw) / len(bw)
+    return {"workload": "N=512, T=32 frames, dt=0.1 s (parameter-fit config)", "forward_ms": round(f, 4),
+            "backward_ms": round(b, 4), "fwd_frames_per_s": round(T / (f * 1e-3), 1),
+            "fwd_adj_frames_per_s": round(T / ((f + b) * 1e-3), 1), "adj_over_fwd": round((f + b) / f, 3),
+            "gpu_launches_per_step": 2 * T + 2}
+
+
+def batched_tiles(og, n_tiles=64, seed=2):
+    """64 tiles: N uniform in {128..2048}, L~U(100,4000), A~U(0.5,8),
+    V~U(5,40), theta~U(0,2pi), lambda~U(0,2), own noise; numpy seed 2."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    f = lambda v: float(np.float32(v))
+    tiles, seeds = [], []
+    for i in range(n_tiles):
+        N = int(rng.choice([128, 256, 512, 1024, 2048]))
+        th = rng.uniform(0, 2 * math.pi)
+        tiles.append(og.Params(N=N, L=f(rng.uniform(100, 4000)), amplitude=f(rng.uniform(0.5, 8)),
+                               wind_speed=f(rng.uniform(5, 40)), wind_dir_x=f(math.cos(th)), wind_dir_y=f(math.sin(th)),
+                               choppiness=f(rng.uniform(0, 2)), suppression=f(0.1), gravity=f(9.81)))
+        seeds.append(1000 + i)
+    return tiles, seeds, rng
+
+
+def bench_batched(torch, og, dev, stream, flush, S=8, reps=3):
+    """Batched mixed-size launch vs looping the plain per-tile update over the
+    same 64 tiles x 8 time samples (t ~ U(0, 600) s)."""
+    tiles, seeds, rng = batched_tiles(og)
+    n = len(tiles)
+    times = rng.uniform(0, 600, size=n * S).tolist()
+    outs = []
+    bufs = []
+    for p in tiles:
+        N = p.N
+        b3 = torch.empty((S, 3, N, N), device=dev)
+        b4 = torch.empty((S, N, N, 4), device=dev)
+        bufs += [b3, b4]
+        for s in range(S):
+            outs.append((b3[s, 0], b3[s, 1], b3[s, 2], b4[s]))
+    texels = sum(p.N * p.N for p in tiles) * S
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+    bt, lt = [], []
+    with og.OceanBatch(tiles, seeds, S) as b, torch.cuda.stream(stream):
+        singles = [og.Ocean(p, seed=sd) for p, sd in zip(tiles, seeds)]
+        for rep in range(reps + 1):
+            flush()
+            ev[0].record(stream)
+            b.update(times, outs, stream=stream)
+            ev[1].record(stream)
+            torch.cuda.synchronize()
+            if rep:
+                bt.append(ev[0].elapsed_time(ev[1]))
+            flush()
+            ev[0].record(stream)
+            for i, oc in enumerate(singles):
+                for s in range(S):
+                    oc.update(times[i * S + s], *outs[i * S + s], stream=stream)
+            ev[1].record(stream)
+            torch.cuda.synchronize()
+            if rep:
+                lt.append(ev[0].elapsed_time(ev[1]))
+        # the same loop captured in a CUDA graph (no host launch overhead)
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g, stream=stream):
+            for i, oc in enumerate(singles):
+                for s in range(S):
+                    oc.update(times[i * S + s], *outs[i * S + s], stream=stream)
+        gt = []
+        for rep in range(reps + 1):
+            flush()
+            ev[0].record(stream)
+            g.replay()
+            ev[1].record(stream)
+            torch.cuda.synchronize()
+            if rep:
+                gt.append(ev[0].elapsed_time(ev[1]))
+        del g
+        b.device_status()
+        for oc in singles:
+            oc.close()
+    bms, lms, gms = sum(bt) / len(bt), sum(lt) / len(lt), sum(gt) / len(gt)
+    return {"workload": f"{n} tiles, N in {{128..2048}} (seed 2), {S} samples each, t~U(0,600) s",
+            "tile_frames": n * S, "texels_per_launch": texels, "batched_ms": round(bms, 3),
+            "loop_ms": round(lms, 3), "batched_tile_frames_per_s": round(n * S / (bms * 1e-3), 1),
+            "loop_tile_frames_per_s": round(n * S / (lms * 1e-3), 1), "speedup_vs_loop": round(lms / bms, 3),
+            "loop_graph_ms": round(gms, 3), "speedup_vs_graphed_loop": round(gms / bms, 3),
+            "batched_effective_GBps": round(92 * texels / (bms * 1e-3) / 1e9, 1)}
 
 
 def run_reference(args, world, rank):
@@ -352,6 +477,7 @@ def main():
     ap.add_argument("--size", type=int, default=1024)
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-extra", action="store_true", help="skip the adjoint and batched measurements")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

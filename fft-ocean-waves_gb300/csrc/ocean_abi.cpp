@@ -19,11 +19,14 @@
 #include <vector>
 
 #include "ocean.h"
+#include "ocean_host.h"
 #include "ocean_internal.h"
 
-namespace {
+namespace ocean {
+namespace host {
 
 thread_local std::string g_err;
+
 
 int fail(int code, const std::string& msg)
 {
@@ -88,10 +91,63 @@ ocean::H0Args h0_args(const ocean_params& p)
     return a;
 }
 
-}  // namespace
+int check_device()
+{
+    int         dev = 0;
+    cudaError_t e   = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
+    int major = 0, minor = 0;
+    cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev);
+    cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, dev);
+    if (major != 10 || minor != 3)
+        return fail(OCEAN_ERR_UNSUPPORTED, "kernels are built for sm_103a only; device is sm_" + std::to_string(major) +
+                                               std::to_string(minor));
+    return OCEAN_OK;
+}
+
+int upload_twiddles(float2** d, int N)
+{
+    std::vector<float2> tw((size_t)N);
+    for (int k = 0; k < N; ++k) {
+        const double a = 2.0 * M_PI * (double)k / (double)N;
+        tw[k]          = make_float2((float)std::cos(a), (float)std::sin(a));
+    }
+    cudaError_t e;
+    if ((e = cudaMalloc(d, N * sizeof(float2))) != cudaSuccess) {
+        *d = nullptr;
+        return fail(OCEAN_ERR_NOMEM, std::string("device allocation failed: ") + cudaGetErrorString(e));
+    }
+    if ((e = cudaMemcpy(*d, tw.data(), N * sizeof(float2), cudaMemcpyHostToDevice)) != cudaSuccess)
+        return cuda_fail(e, "twiddle upload");
+    return OCEAN_OK;
+}
+
+int encode_inter_map(CUtensorMap* map, float2* inter, int N, int units)
+{
+    PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
+    if (!enc) return fail(OCEAN_ERR_UNSUPPORTED, "cuTensorMapEncodeTiled is not available from the driver");
+    const cuuint64_t H = (cuuint64_t)inter_rows(N), NP = (cuuint64_t)inter_pitch(N);
+    unsigned box[2];
+    col_pass_box(N, box);
+    // the intermediates as floats [units*3*H rows][2*NP]
+    cuuint64_t dims[2]    = {2 * NP, (cuuint64_t)units * 3 * H};
+    cuuint64_t strides[1] = {2 * NP * sizeof(float)};
+    cuuint32_t boxd[2]    = {box[0], box[1]};
+    cuuint32_t estr[2]    = {1, 1};
+    CUresult   r = enc(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, inter, dims, strides, boxd, estr,
+                       CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                       CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return fail(OCEAN_ERR_CUDA, "cuTensorMapEncodeTiled failed: " + std::to_string((int)r));
+    return OCEAN_OK;
+}
+
+}  // namespace host
+}  // namespace ocean
+
+using namespace ocean::host;
 
 // splitmix64 (Steele, Lea & Flood 2014): i-th draw uses state seed + (i+1)*gamma.
-static inline uint64_t splitmix64_at(uint64_t seed, uint64_t i)
+uint64_t ocean::host::splitmix64_at(uint64_t seed, uint64_t i)
 {
     uint64_t z = seed + (i + 1) * 0x9E3779B97F4A7C15ull;
     z          = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
@@ -143,7 +199,22 @@ struct ocean_s {
         fc.kt_lo        = (float)(kt - (double)fc.kt_hi);
         const double dc = w_dc * t / (2.0 * M_PI);
         fc.dc_cycles    = (float)(dc - std::nearbyint(dc));
+        fc.literal_conj = (p.flags & OCEAN_FLAG_LITERAL_CONJ) ? 1 : 0;
         return fc;
+    }
+
+    ocean::ColUnit col_unit(const ocean_outputs& out) const
+    {
+        ocean::ColUnit u;
+        u.dx     = out.dx;
+        u.dy     = out.dy;
+        u.dz     = out.dz;
+        u.nj     = reinterpret_cast<float4*>(out.normal_j);
+        u.scale  = (float)(0.5 / ((double)N * N));
+        u.lambda = p.choppiness;
+        u.inv2d  = (float)((double)N / (2.0 * (double)p.L));
+        u.pad_   = 0.0f;
+        return u;
     }
 
     int build_h0(cudaStream_t s)
@@ -232,15 +303,8 @@ int ocean_create(const ocean_params* params, const float* noise_host, ocean_t** 
     int rc = validate(params);
     if (rc) return rc;
     if (!noise_host) return fail(OCEAN_ERR_INVALID, "noise_host is NULL");
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
-    int major = 0, minor = 0;
-    cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev);
-    cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, dev);
-    if (major != 10 || minor != 3)
-        return fail(OCEAN_ERR_UNSUPPORTED, "kernels are built for sm_103a only; device is sm_" +
-                                               std::to_string(major) + std::to_string(minor));
+    if ((rc = check_device()) != OCEAN_OK) return rc;
+    cudaError_t e;
 
     ocean_s* o = new (std::nothrow) ocean_s();
     if (!o) return fail(OCEAN_ERR_NOMEM, "host allocation failed");
@@ -252,7 +316,6 @@ int ocean_create(const ocean_params* params, const float* noise_host, ocean_t** 
     if ((e = cudaMalloc(&o->h0, N * N * sizeof(float4))) != cudaSuccess ||
         (e = cudaMalloc(&o->inter, 3 * H * NP * sizeof(float2))) != cudaSuccess ||
         (e = cudaMalloc(&o->status, sizeof(unsigned))) != cudaSuccess ||
-        (e = cudaMalloc(&o->tw, N * sizeof(float2))) != cudaSuccess ||
         (e = cudaMalloc(&o->noise, 4 * N * N * sizeof(float))) != cudaSuccess) {
         delete o;
         return fail(OCEAN_ERR_NOMEM, std::string("device allocation failed: ") + cudaGetErrorString(e));
@@ -261,34 +324,15 @@ int ocean_create(const ocean_params* params, const float* noise_host, ocean_t** 
         delete o;
         return cuda_fail(e, "status clear");
     }
-    {
-        // Column-pass tensor map: the intermediate as floats [3*H rows][2*NP].
-        PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
-        if (!enc) {
-            delete o;
-            return fail(OCEAN_ERR_UNSUPPORTED, "cuTensorMapEncodeTiled is not available from the driver");
-        }
-        unsigned box[2];
-        ocean::col_pass_box(o->N, box);
-        cuuint64_t dims[2]    = {2 * NP, 3 * H};
-        cuuint64_t strides[1] = {2 * NP * sizeof(float)};
-        cuuint32_t boxd[2]    = {box[0], box[1]};
-        cuuint32_t estr[2]    = {1, 1};
-        CUresult   r = enc(&o->inter_map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, o->inter, dims, strides, boxd, estr,
-                           CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
-                           CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-        if (r != CUDA_SUCCESS) {
-            delete o;
-            return fail(OCEAN_ERR_CUDA, "cuTensorMapEncodeTiled failed: " + std::to_string((int)r));
-        }
+    if ((rc = encode_inter_map(&o->inter_map, o->inter, o->N, 1)) != OCEAN_OK) {
+        delete o;
+        return rc;
     }
-    std::vector<float2> tw(N);
-    for (size_t k = 0; k < N; ++k) {
-        const double a = 2.0 * M_PI * (double)k / (double)N;
-        tw[k]          = make_float2((float)std::cos(a), (float)std::sin(a));
+    if ((rc = upload_twiddles(&o->tw, o->N)) != OCEAN_OK) {
+        delete o;
+        return rc;
     }
-    if ((e = cudaMemcpy(o->tw, tw.data(), N * sizeof(float2), cudaMemcpyHostToDevice)) != cudaSuccess ||
-        (e = cudaMemcpy(o->noise, noise_host, 4 * N * N * sizeof(float), cudaMemcpyHostToDevice)) != cudaSuccess) {
+    if ((e = cudaMemcpy(o->noise, noise_host, 4 * N * N * sizeof(float), cudaMemcpyHostToDevice)) != cudaSuccess) {
         delete o;
         return cuda_fail(e, "upload");
     }
@@ -379,13 +423,15 @@ int ocean_update_rows(ocean_t* o, double t, void* stream)
     if (!o) return fail(OCEAN_ERR_INVALID, "ocean is NULL");
     if (!std::isfinite(t)) return fail(OCEAN_ERR_INVALID, "time is not finite");
     ocean::RowArgs ra;
-    ra.h0           = o->h0;
-    ra.inter        = o->inter;
-    ra.tw           = o->tw;
-    ra.status       = o->status;
-    ra.fc           = o->frame(t);
-    ra.literal_conj = (o->p.flags & OCEAN_FLAG_LITERAL_CONJ) ? 1 : 0;
-    cudaError_t e   = ocean::launch_row_pass(o->N, ra, static_cast<cudaStream_t>(stream));
+    ra.h0         = o->h0;
+    ra.inter      = o->inter;
+    ra.tw         = o->tw;
+    ra.status     = o->status;
+    ra.fcs        = nullptr;
+    ra.fc0        = o->frame(t);
+    ra.tiles      = 1;
+    ra.S          = 1;
+    cudaError_t e = ocean::launch_row_pass(o->N, ra, static_cast<cudaStream_t>(stream));
     if (e != cudaSuccess) return cuda_fail(e, "row pass launch");
     return OCEAN_OK;
 }
@@ -407,14 +453,9 @@ int ocean_update_columns(ocean_t* o, const ocean_outputs* out, void* stream)
     ca.map        = o->inter_map;
     ca.status     = o->status;
     ca.tw         = o->tw;
-    ca.dx         = out->dx;
-    ca.dy         = out->dy;
-    ca.dz         = out->dz;
-    ca.nj         = reinterpret_cast<float4*>(out->normal_j);
-    ca.scale      = (float)(0.5 / ((double)o->N * o->N));
-    ca.lambda     = o->p.choppiness;
-    ca.inv2d      = (float)((double)o->N / (2.0 * (double)o->p.L));
-    cudaError_t e = ocean::launch_col_pass(o->N, ca, static_cast<cudaStream_t>(stream), o->pdl_next);
+    ca.units      = nullptr;
+    ca.u0         = o->col_unit(*out);
+    cudaError_t e = ocean::launch_col_pass(o->N, 1, ca, static_cast<cudaStream_t>(stream), o->pdl_next);
     o->pdl_next   = false;
     if (e != cudaSuccess) return cuda_fail(e, "column pass launch");
     return OCEAN_OK;

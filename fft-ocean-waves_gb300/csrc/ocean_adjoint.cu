@@ -95,7 +95,7 @@ __global__ void __launch_bounds__(AdjColCfg<N>::THREADS) k_adj_col_pass(AdjColAr
     }
     __syncthreads();
     float2* lb = buf + li * LS;
-    line_fft<L, -1>(v, lb, tw_s, t);
+    line_fft<L, -1>(v, lb, tw_s, t, li);
 #pragma unroll
     for (int e = 0; e < L::E; ++e) lb[L::pad(LineOut<L>::pos(t, e))] = v[e];
     __syncthreads();
@@ -189,7 +189,7 @@ __global__ void __launch_bounds__(AdjRowCfg<N>::THREADS) k_adj_row_pass(AdjRowAr
             v[r] = lactive ? __ldg(in + t + r * (N / L::R1)) : make_float2(0.f, 0.f);
         __syncthreads();                                   // previous frame's mode loop is done with buf
         float2* lb = buf + li * LS;
-        line_fft<L, -1>(v, lb, tw_s, t);
+        line_fft<L, -1>(v, lb, tw_s, t, li);
 #pragma unroll
         for (int e = 0; e < L::E; ++e) lb[L::pad(LineOut<L>::pos(t, e))] = v[e];
         __syncthreads();

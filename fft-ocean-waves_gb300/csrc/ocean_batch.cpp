@@ -1,0 +1,285 @@
+// ocean_batch.cpp -- batches of independent tiles (ocean_batch_* in
+// include/ocean.h).  No counterpart in the reference, which renders one tile.
+//
+// Tiles are grouped by N.  Per group: h0 of every tile back to back, one
+// intermediate per (tile, time sample) back to back, one tensor map over all
+// of them, and one twiddle table.  An update is a CUDA graph of
+//   H2D copy of the per-unit constants (pinned staging -> device)
+//   per group: k_row_pass (persistent; each h0 row pair is staged once and
+//              serves all samples of its tile) -> k_col_pass (grid: column
+//              tiles x units, programmatic dependent of the row pass)
+// captured at creation and replayed by ocean_batch_update.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <map>
+#include <vector>
+
+#include "ocean.h"
+#include "ocean_host.h"
+#include "ocean_internal.h"
+
+using namespace ocean::host;
+
+struct ocean_batch_s {
+    struct Group {
+        int              N = 0;
+        std::vector<int> tiles;          // batch tile indices, in slot order
+        float4*          h0    = nullptr;
+        float2*          inter = nullptr;
+        float2*          tw    = nullptr;
+        CUtensorMap      map;
+        size_t           first_unit = 0; // this group's units start here in the unit arrays
+    };
+    int                       n_tiles = 0, S = 0;
+    std::vector<ocean_params> params;
+    std::vector<double>       K, w_dc;
+    std::vector<Group>        groups;
+    unsigned*                 status = nullptr;
+    // per-unit constants, in group order: FrameConsts[units] | ColUnit[units]
+    size_t                    units = 0, desc_bytes = 0;
+    void*                     d_desc = nullptr;
+    void*                     h_desc = nullptr;   // pinned
+    cudaStream_t              cap    = nullptr;
+    cudaGraph_t               graph  = nullptr;
+    cudaGraphExec_t           exec   = nullptr;
+    cudaEvent_t               done   = nullptr;
+    bool                      launched = false;
+
+    ~ocean_batch_s()
+    {
+        if (launched) cudaEventSynchronize(done);
+        if (exec) cudaGraphExecDestroy(exec);
+        if (graph) cudaGraphDestroy(graph);
+        if (done) cudaEventDestroy(done);
+        if (cap) cudaStreamDestroy(cap);
+        for (Group& g : groups) {
+            cudaFree(g.h0);
+            cudaFree(g.inter);
+            cudaFree(g.tw);
+        }
+        cudaFree(status);
+        cudaFree(d_desc);
+        cudaFreeHost(h_desc);
+    }
+
+    ocean::FrameConsts* h_fc() { return static_cast<ocean::FrameConsts*>(h_desc); }
+    ocean::ColUnit*     h_units()
+    {
+        return reinterpret_cast<ocean::ColUnit*>(static_cast<char*>(h_desc) + units * sizeof(ocean::FrameConsts));
+    }
+    ocean::FrameConsts* d_fc() { return static_cast<ocean::FrameConsts*>(d_desc); }
+    ocean::ColUnit*     d_units()
+    {
+        return reinterpret_cast<ocean::ColUnit*>(static_cast<char*>(d_desc) + units * sizeof(ocean::FrameConsts));
+    }
+};
+
+namespace {
+
+int capture(ocean_batch_s* b)
+{
+    cudaError_t e;
+    if ((e = cudaStreamBeginCapture(b->cap, cudaStreamCaptureModeRelaxed)) != cudaSuccess)
+        return cuda_fail(e, "batch graph capture");
+    e = cudaMemcpyAsync(b->d_desc, b->h_desc, b->desc_bytes, cudaMemcpyHostToDevice, b->cap);
+    for (size_t gi = 0; gi < b->groups.size() && e == cudaSuccess; ++gi) {
+        ocean_batch_s::Group& g = b->groups[gi];
+        ocean::RowArgs ra;
+        ra.h0     = g.h0;
+        ra.inter  = g.inter;
+        ra.tw     = g.tw;
+        ra.status = b->status;
+        ra.fcs    = b->d_fc() + g.first_unit;
+        ra.fc0    = ocean::FrameConsts{};
+        ra.tiles  = (int)g.tiles.size();
+        ra.S      = b->S;
+        if ((e = ocean::launch_row_pass(g.N, ra, b->cap)) != cudaSuccess) break;
+        ocean::ColArgs ca;
+        ca.map    = g.map;
+        ca.status = b->status;
+        ca.tw     = g.tw;
+        ca.units  = b->d_units() + g.first_unit;
+        ca.u0     = ocean::ColUnit{};
+        e = ocean::launch_col_pass(g.N, (int)g.tiles.size() * b->S, ca, b->cap, true);
+    }
+    cudaGraph_t graph = nullptr;
+    cudaError_t e2    = cudaStreamEndCapture(b->cap, &graph);
+    if (e != cudaSuccess) {
+        if (graph) cudaGraphDestroy(graph);
+        return cuda_fail(e, "batch graph launch capture");
+    }
+    if (e2 != cudaSuccess) return cuda_fail(e2, "batch graph capture");
+    b->graph = graph;
+    if ((e = cudaGraphInstantiate(&b->exec, b->graph, 0)) != cudaSuccess) return cuda_fail(e, "batch graph instantiate");
+    return OCEAN_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int ocean_batch_create(const ocean_params* params, const uint64_t* seeds, int32_t n_tiles, int32_t samples,
+                       ocean_batch_t** out)
+{
+    if (!out) return fail(OCEAN_ERR_INVALID, "out is NULL");
+    *out = nullptr;
+    if (!params || !seeds) return fail(OCEAN_ERR_INVALID, "NULL argument");
+    if (n_tiles < 1 || samples < 1) return fail(OCEAN_ERR_INVALID, "n_tiles and samples must be >= 1");
+    for (int i = 0; i < n_tiles; ++i) {
+        int rc = validate(&params[i]);
+        if (rc) return fail(rc, "tile " + std::to_string(i) + ": " + ocean_last_error());
+    }
+    int rc = check_device();
+    if (rc) return rc;
+
+    ocean_batch_s* b = new (std::nothrow) ocean_batch_s();
+    if (!b) return fail(OCEAN_ERR_NOMEM, "host allocation failed");
+    b->n_tiles = n_tiles;
+    b->S       = samples;
+    b->params.assign(params, params + n_tiles);
+    for (const ocean_params& p : b->params) {
+        const double g = gravity_of(p);
+        b->K.push_back(std::sqrt(g / (2.0 * M_PI * (double)p.L)));
+        b->w_dc.push_back(std::sqrt(g * 0.00001));
+    }
+    // groups, largest N first (its kernels take longest)
+    std::map<int, std::vector<int>, std::greater<int>> byN;
+    for (int i = 0; i < n_tiles; ++i) byN[params[i].N].push_back(i);
+    cudaError_t e;
+    size_t      unit0 = 0;
+    for (auto& kv : byN) {
+        ocean_batch_s::Group g;
+        g.N          = kv.first;
+        g.tiles      = kv.second;
+        g.first_unit = unit0;
+        unit0 += g.tiles.size() * (size_t)samples;
+        b->groups.push_back(g);
+    }
+    b->units      = unit0;
+    b->desc_bytes = b->units * (sizeof(ocean::FrameConsts) + sizeof(ocean::ColUnit));
+    std::vector<float> noise;
+    float*             d_noise = nullptr;
+    const int          maxN    = b->groups.front().N;
+    if ((e = cudaMalloc(&b->status, sizeof(unsigned))) != cudaSuccess ||
+        (e = cudaMemset(b->status, 0, sizeof(unsigned))) != cudaSuccess ||
+        (e = cudaMalloc(&b->d_desc, b->desc_bytes)) != cudaSuccess ||
+        (e = cudaMallocHost(&b->h_desc, b->desc_bytes)) != cudaSuccess ||
+        (e = cudaMalloc(&d_noise, 4 * (size_t)maxN * maxN * sizeof(float))) != cudaSuccess) {
+        cudaFree(d_noise);
+        delete b;
+        return fail(OCEAN_ERR_NOMEM, std::string("batch allocation failed: ") + cudaGetErrorString(e));
+    }
+    for (ocean_batch_s::Group& g : b->groups) {
+        const size_t N = (size_t)g.N, NN = N * N, T = g.tiles.size();
+        const size_t H = (size_t)ocean::inter_rows(g.N), NP = (size_t)ocean::inter_pitch(g.N);
+        if ((e = cudaMalloc(&g.h0, T * NN * sizeof(float4))) != cudaSuccess ||
+            (e = cudaMalloc(&g.inter, T * samples * 3 * H * NP * sizeof(float2))) != cudaSuccess) {
+            cudaFree(d_noise);
+            delete b;
+            return fail(OCEAN_ERR_NOMEM, std::string("batch allocation failed: ") + cudaGetErrorString(e));
+        }
+        if ((rc = upload_twiddles(&g.tw, g.N)) != OCEAN_OK ||
+            (rc = encode_inter_map(&g.map, g.inter, g.N, (int)(T * samples))) != OCEAN_OK) {
+            cudaFree(d_noise);
+            delete b;
+            return rc;
+        }
+        noise.resize(4 * NN);
+        for (size_t j = 0; j < T; ++j) {
+            const int t = g.tiles[j];
+            ocean_fill_noise(seeds[t], g.N, noise.data());
+            if ((e = cudaMemcpy(d_noise, noise.data(), 4 * NN * sizeof(float), cudaMemcpyHostToDevice)) != cudaSuccess ||
+                (e = ocean::launch_h0(h0_args(params[t]), d_noise, g.h0 + j * NN, 0)) != cudaSuccess ||
+                (e = cudaStreamSynchronize(0)) != cudaSuccess) {
+                cudaFree(d_noise);
+                delete b;
+                return cuda_fail(e, "batch h0 init");
+            }
+        }
+    }
+    cudaFree(d_noise);
+    if ((e = cudaStreamCreateWithFlags(&b->cap, cudaStreamNonBlocking)) != cudaSuccess ||
+        (e = cudaEventCreateWithFlags(&b->done, cudaEventDisableTiming)) != cudaSuccess) {
+        delete b;
+        return cuda_fail(e, "batch stream");
+    }
+    if ((rc = capture(b)) != OCEAN_OK) {
+        delete b;
+        return rc;
+    }
+    *out = b;
+    return OCEAN_OK;
+}
+
+int ocean_batch_update(ocean_batch_t* b, const double* times, const ocean_outputs* outs, void* stream)
+{
+    if (!b || !times || !outs) return fail(OCEAN_ERR_INVALID, "NULL argument");
+    const size_t n = (size_t)b->n_tiles * b->S;
+    for (size_t i = 0; i < n; ++i) {
+        if (!std::isfinite(times[i])) return fail(OCEAN_ERR_INVALID, "time is not finite");
+        const ocean_outputs& o = outs[i];
+        if (!o.dx || !o.dy || !o.dz || !o.normal_j) return fail(OCEAN_ERR_INVALID, "NULL output pointer");
+        const uintptr_t al = reinterpret_cast<uintptr_t>(o.dx) | reinterpret_cast<uintptr_t>(o.dy) |
+                             reinterpret_cast<uintptr_t>(o.dz) | reinterpret_cast<uintptr_t>(o.normal_j);
+        if (al % 16) return fail(OCEAN_ERR_INVALID, "output pointers must be 16-byte aligned");
+    }
+    cudaError_t e;
+    // the previous replay's H2D copy must have read the staging buffer
+    if (b->launched && (e = cudaEventSynchronize(b->done)) != cudaSuccess) return cuda_fail(e, "batch wait");
+    ocean::FrameConsts* fc = b->h_fc();
+    ocean::ColUnit*     cu = b->h_units();
+    for (const ocean_batch_s::Group& g : b->groups) {
+        for (size_t j = 0; j < g.tiles.size(); ++j) {
+            const int           t = g.tiles[j];
+            const ocean_params& p = b->params[t];
+            for (int s = 0; s < b->S; ++s) {
+                const size_t   u  = g.first_unit + j * b->S + s;
+                const double   tt = times[(size_t)t * b->S + s];
+                const double   kt = b->K[t] * tt;
+                ocean::FrameConsts f;
+                f.kt_hi          = (float)kt;
+                f.kt_lo          = (float)(kt - (double)f.kt_hi);
+                const double dc  = b->w_dc[t] * tt / (2.0 * M_PI);
+                f.dc_cycles      = (float)(dc - std::nearbyint(dc));
+                f.literal_conj   = (p.flags & OCEAN_FLAG_LITERAL_CONJ) ? 1 : 0;
+                fc[u]            = f;
+                const ocean_outputs& o = outs[(size_t)t * b->S + s];
+                ocean::ColUnit       c;
+                c.dx     = o.dx;
+                c.dy     = o.dy;
+                c.dz     = o.dz;
+                c.nj     = reinterpret_cast<float4*>(o.normal_j);
+                c.scale  = (float)(0.5 / ((double)g.N * g.N));
+                c.lambda = p.choppiness;
+                c.inv2d  = (float)((double)g.N / (2.0 * (double)p.L));
+                c.pad_   = 0.0f;
+                cu[u]    = c;
+            }
+        }
+    }
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    if ((e = cudaGraphLaunch(b->exec, s)) != cudaSuccess) return cuda_fail(e, "batch graph launch");
+    if ((e = cudaEventRecord(b->done, s)) != cudaSuccess) return cuda_fail(e, "batch event");
+    b->launched = true;
+    return OCEAN_OK;
+}
+
+int ocean_batch_device_status(ocean_batch_t* b, void* stream)
+{
+    if (!b) return fail(OCEAN_ERR_INVALID, "batch is NULL");
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    unsigned     h = 0;
+    cudaError_t  e;
+    if ((e = cudaMemcpyAsync(&h, b->status, sizeof(h), cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
+        (e = cudaMemsetAsync(b->status, 0, sizeof(unsigned), s)) != cudaSuccess ||
+        (e = cudaStreamSynchronize(s)) != cudaSuccess)
+        return cuda_fail(e, "device status");
+    if (h) return fail(OCEAN_ERR_TIMEOUT, "a kernel's bounded wait for its TMA copies timed out");
+    return OCEAN_OK;
+}
+
+void ocean_batch_destroy(ocean_batch_t* b) { delete b; }
+
+}  // extern "C"

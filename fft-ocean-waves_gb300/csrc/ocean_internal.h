@@ -7,10 +7,24 @@
 
 namespace ocean {
 
-// Per-frame constants computed on the host in double precision.
+// Per-frame constants of one (tile, time sample), computed on the host in
+// double precision.
 struct FrameConsts {
     float kt_hi, kt_lo;  // K*t as a double-float, K = sqrt(g/(2*pi*L)): phase in cycles = K*t*m^(1/4)
     float dc_cycles;     // reduced phase (cycles) of the DC mode, whose |k| is floored at 1e-5
+    int   literal_conj;  // the tile's OCEAN_FLAG_LITERAL_CONJ
+};
+
+// Column-pass epilogue parameters and outputs of one (tile, time sample).
+struct ColUnit {
+    float*  dx;
+    float*  dy;
+    float*  dz;
+    float4* nj;
+    float   scale;   // 0.5/N^2: Hermitian average and inversion_cs.glsl's 1/N^2
+    float   lambda;
+    float   inv2d;   // N/(2L): central-difference factor
+    float   pad_;
 };
 
 struct H0Args {
@@ -30,26 +44,26 @@ struct H0Args {
 __host__ __device__ constexpr int inter_pitch(int N) { return N + 2; }
 __host__ __device__ constexpr int inter_rows(int N) { return N / 2 + 1; }
 
+// A launch covers `tiles` tiles of the same N, each advanced to S time
+// samples: unit u = tile*S + s.  h0 of tile t starts at h0 + t*N*N; the
+// intermediate of unit u at inter + u*3*(N/2+1)*(N+2).  Per-unit constants come
+// from `fcs` (device, [tiles*S]) or, for a single unit, from `fc0`.
 struct RowArgs {
-    const float4* h0;      // [N][N]
-    float2*       inter;   // [3][N/2+1][N+2]
-    const float2* tw;      // [N] exp(+2*pi*i*k/N)
-    unsigned*     status;  // device status word (bounded-wait time-outs)
-    FrameConsts   fc;
-    int           literal_conj;
+    const float4*      h0;
+    float2*            inter;
+    const float2*      tw;      // [N] exp(+2*pi*i*k/N)
+    unsigned*          status;  // device status word (bounded-wait time-outs)
+    const FrameConsts* fcs;
+    FrameConsts        fc0;
+    int                tiles, S;
 };
 
 struct ColArgs {
-    CUtensorMap   map;     // 2-D tensor map over inter: floats [3*(N/2+1)][2*(N+2)]
-    unsigned*     status;
-    const float2* tw;
-    float*        dx;
-    float*        dy;
-    float*        dz;
-    float4*       nj;
-    float         scale;   // 0.5/N^2: Hermitian average and inversion_cs.glsl's 1/N^2
-    float         lambda;
-    float         inv2d;   // N/(2L): central-difference factor
+    CUtensorMap    map;     // 2-D tensor map over inter: floats [units*3*(N/2+1)][2*(N+2)]
+    unsigned*      status;
+    const float2*  tw;
+    const ColUnit* units;   // device [units], or NULL: u0 for the single unit
+    ColUnit        u0;
 };
 
 // ---------------------------------------------------------------------------
@@ -87,7 +101,7 @@ cudaError_t launch_adj_row(int N, const AdjRowArgs& a, cudaStream_t s);
 cudaError_t launch_h0(const H0Args& a, const float* noise, float4* h0, cudaStream_t s);
 cudaError_t launch_row_pass(int N, const RowArgs& a, cudaStream_t s);
 // pdl: launch as a programmatic dependent of the preceding kernel in `s`.
-cudaError_t launch_col_pass(int N, const ColArgs& a, cudaStream_t s, bool pdl);
+cudaError_t launch_col_pass(int N, int units, const ColArgs& a, cudaStream_t s, bool pdl);
 // Box of the column-pass tensor map at size N: {inner floats, rows}.
 void col_pass_box(int N, unsigned box[2]);
 // Shared memory the two passes need at size N (bytes), for validation.

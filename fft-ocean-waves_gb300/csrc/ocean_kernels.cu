@@ -79,7 +79,7 @@ struct RowCfg {
     static constexpr int PAIRS   = L::G >= 32 ? 1 : 32 / L::G;  // row pairs per work item
     static constexpr int LINES   = 3 * PAIRS;
     static constexpr int THREADS = LINES * L::G;
-    static constexpr int ITEMS   = (N / 2 + 1 + PAIRS - 1) / PAIRS;
+    static constexpr int ITEMS   = (N / 2 + 1 + PAIRS - 1) / PAIRS;  // work items per tile
     static constexpr int STAGES  = 2;
     // shared memory (float2 units): tw[N] | h0 ring [STAGES][PAIRS][2][N] float4 |
     // work area = max(hy [PAIRS][2][N], line buffers [LINES][NPAD])
@@ -91,26 +91,33 @@ struct RowCfg {
     static constexpr uint32_t ROW_BYTES = N * sizeof(float4);
 };
 
+// Fetch the h0 rows of work item `item` (tile item/ITEMS, row pairs
+// (item%ITEMS)*PAIRS ...) into a ring stage with 1-D bulk copies.
 template <int N>
 __device__ __forceinline__ void row_issue(const RowArgs& a, float4* ring_stage, uint64_t* bar, int item)
 {
     using RC = RowCfg<N>;
+    const int     tile = item / RC::ITEMS, pi = item % RC::ITEMS;
+    const float4* h0t  = a.h0 + (size_t)tile * N * N;
     uint32_t bytes = 0;
 #pragma unroll
     for (int pl = 0; pl < RC::PAIRS; ++pl)
-        if (item * RC::PAIRS + pl <= N / 2) bytes += 2 * RC::ROW_BYTES;
+        if (pi * RC::PAIRS + pl <= N / 2) bytes += 2 * RC::ROW_BYTES;
     mbar_arrive_expect_tx(bar, bytes);
 #pragma unroll
     for (int pl = 0; pl < RC::PAIRS; ++pl) {
-        const int yp = item * RC::PAIRS + pl;
+        const int yp = pi * RC::PAIRS + pl;
         if (yp > N / 2) break;
         const int yq = (N - yp) & (N - 1);
-        bulk_g2s(ring_stage + (pl * 2 + 0) * N, a.h0 + (size_t)yp * N, RC::ROW_BYTES, bar);
-        bulk_g2s(ring_stage + (pl * 2 + 1) * N, a.h0 + (size_t)yq * N, RC::ROW_BYTES, bar);
+        bulk_g2s(ring_stage + (pl * 2 + 0) * N, h0t + (size_t)yp * N, RC::ROW_BYTES, bar);
+        bulk_g2s(ring_stage + (pl * 2 + 1) * N, h0t + (size_t)yq * N, RC::ROW_BYTES, bar);
     }
 }
 
-template <int N>
+// MULTI: more than one (tile, sample) unit per launch (batches).  The single
+// unit instantiation keeps the per-element choppy factors out of a runtime
+// sample loop, which the compiler would otherwise hoist into registers.
+template <int N, bool MULTI>
 __global__ void __launch_bounds__(RowCfg<N>::THREADS) k_row_pass(RowArgs a)
 {
     using RC = RowCfg<N>;
@@ -131,10 +138,11 @@ __global__ void __launch_bounds__(RowCfg<N>::THREADS) k_row_pass(RowArgs a)
     }
     for (int i = tid; i < N; i += RC::THREADS) tw_s[i] = a.tw[i];
     __syncthreads();
+    const int n_items = a.tiles * RC::ITEMS;
     if (tid == 0)
         for (int s = 0; s < RC::STAGES; ++s) {
             const int item = blockIdx.x + s * gridDim.x;
-            if (item < RC::ITEMS) row_issue<N>(a, ring + (size_t)s * RC::PAIRS * 2 * N, &bars[s], item);
+            if (item < n_items) row_issue<N>(a, ring + (size_t)s * RC::PAIRS * 2 * N, &bars[s], item);
         }
     // The column pass may start its set-up now; it waits for this grid to finish
     // before it reads the intermediate.
@@ -145,82 +153,90 @@ __global__ void __launch_bounds__(RowCfg<N>::THREADS) k_row_pass(RowArgs a)
     const int pl_line = li / 3;
     uint32_t phase_bits = 0;
 
-    for (int k = 0, item = blockIdx.x; item < RC::ITEMS; ++k, item += gridDim.x) {
+    for (int k = 0, item = blockIdx.x; item < n_items; ++k, item += gridDim.x) {
         const int s = k & 1;
         float4* stage = ring + (size_t)s * RC::PAIRS * 2 * N;
         if (!block_wait(&bars[s], (phase_bits >> s) & 1u, &wait_ok, a.status)) return;
         phase_bits ^= 1u << s;
+        const int tile = item / RC::ITEMS, pi = item % RC::ITEMS;
 
-        // Prepass: h(k,t) for the pair's two rows.  hy[pl][0][x] is the mode
-        // (x, y'), hy[pl][1][x] the mode (N-x, N-y').  The four modes (x, y'),
-        // (N-x, y'), (N-x, N-y'), (x, N-y') share |k| (ix^2 and iz^2 are even)
-        // and so the phase, which is computed once for all four.
-        float2* hy = work;
-        constexpr int HX = N / 2 + 1;
-        for (int i = tid; i < RC::PAIRS * HX; i += RC::THREADS) {
-            const int pl = i / HX, x = i % HX;
-            const int yp = item * RC::PAIRS + pl;
-            if (yp > N / 2) continue;
-            const int xm = (N - x) & (N - 1);
-            const int ix = x - N / 2, iz = yp - N / 2;
-            float c, sn;
-            mode_phase(ix * ix + iz * iz, a.fc, c, sn);
-            const float4* r0 = stage + (pl * 2 + 0) * N;
-            const float4* r1 = stage + (pl * 2 + 1) * N;
-            float2*       h0r = hy + (pl * 2 + 0) * N;
-            float2*       h1r = hy + (pl * 2 + 1) * N;
-            h0r[x] = evolve(r0[x], c, sn, a.literal_conj);
-            h1r[x] = evolve(r1[xm], c, sn, a.literal_conj);
-            if (xm != x) {
-                h0r[xm] = evolve(r0[xm], c, sn, a.literal_conj);
-                h1r[xm] = evolve(r1[x], c, sn, a.literal_conj);
+        // The staged rows serve every time sample of the tile.
+        const int nsmp = MULTI ? a.S : 1;
+        for (int smp = 0; smp < nsmp; ++smp) {
+            const int         unit = MULTI ? tile * a.S + smp : 0;
+            const FrameConsts fc   = MULTI ? a.fcs[unit] : a.fc0;
+            // Prepass: h(k,t) for the pair's two rows.  hy[pl][0][x] is the mode
+            // (x, y'), hy[pl][1][x] the mode (N-x, N-y').  The four modes (x, y'),
+            // (N-x, y'), (N-x, N-y'), (x, N-y') share |k| (ix^2 and iz^2 are
+            // even) and so the phase, which is computed once for all four.
+            float2* hy = work;
+            constexpr int HX = N / 2 + 1;
+            for (int i = tid; i < RC::PAIRS * HX; i += RC::THREADS) {
+                const int pl = i / HX, x = i % HX;
+                const int yp = pi * RC::PAIRS + pl;
+                if (yp > N / 2) continue;
+                const int xm = (N - x) & (N - 1);
+                const int ix = x - N / 2, iz = yp - N / 2;
+                float c, sn;
+                mode_phase(ix * ix + iz * iz, fc, c, sn);
+                const float4* r0  = stage + (pl * 2 + 0) * N;
+                const float4* r1  = stage + (pl * 2 + 1) * N;
+                float2*       h0r = hy + (pl * 2 + 0) * N;
+                float2*       h1r = hy + (pl * 2 + 1) * N;
+                h0r[x] = evolve(r0[x], c, sn, fc.literal_conj);
+                h1r[x] = evolve(r1[xm], c, sn, fc.literal_conj);
+                if (xm != x) {
+                    h0r[xm] = evolve(r0[xm], c, sn, fc.literal_conj);
+                    h1r[xm] = evolve(r1[x], c, sn, fc.literal_conj);
+                }
             }
-        }
-        __syncthreads();                                   // hy complete, ring stage s consumed
-        if (tid == 0) {
-            const int next = item + RC::STAGES * gridDim.x;
-            if (next < RC::ITEMS) {
-                fence_proxy_async_smem();
-                row_issue<N>(a, stage, &bars[s], next);
+            __syncthreads();                               // hy complete
+            if (smp == nsmp - 1 && tid == 0) {             // ring stage consumed: refill it
+                const int next = item + RC::STAGES * gridDim.x;
+                if (next < n_items) {
+                    fence_proxy_async_smem();
+                    row_issue<N>(a, stage, &bars[s], next);
+                }
             }
-        }
 
-        // Gather the line inputs: 2 * X_H,f(x) = X_f(x) + conj X_f(-x).
-        const int  yp     = item * RC::PAIRS + pl_line;
-        const bool active = yp <= N / 2;
-        const int  iz = yp - N / 2, izq = ((N - yp) & (N - 1)) - N / 2;
-        float2 v[L::E];
+            // Gather the line inputs: 2 * X_H,f(x) = X_f(x) + conj X_f(-x).
+            const int  yp     = pi * RC::PAIRS + pl_line;
+            const bool active = yp <= N / 2;
+            const int  iz = yp - N / 2, izq = ((N - yp) & (N - 1)) - N / 2;
+            float2 v[L::E];
 #pragma unroll
-        for (int r = 0; r < L::E; ++r) {
-            const int x = t + r * (N / L::R1);
-            float2 hk = active ? hy[(pl_line * 2 + 0) * N + x] : make_float2(0.f, 0.f);
-            float2 hq = active ? hy[(pl_line * 2 + 1) * N + x] : make_float2(0.f, 0.f);
-            if (f != 1) {
-                // -i (k/|k|) h (tilde_h0_t_cs.glsl:113-126); the DC mode gets 0
-                const int   ix  = x - N / 2;
-                const int   m   = ix * ix + iz * iz;
-                const float rs  = m ? __frsqrt_rn((float)m) : 0.0f;
-                const float fk  = -(float)(f == 0 ? ix : iz) * rs;
-                const float fkq = -(float)(f == 0 ? (((N - x) & (N - 1)) - N / 2) : izq) * rs;
-                hk = make_float2(-fk * hk.y, fk * hk.x);
-                hq = make_float2(-fkq * hq.y, fkq * hq.x);
+            for (int r = 0; r < L::E; ++r) {
+                const int x = t + r * (N / L::R1);
+                float2 hk = active ? hy[(pl_line * 2 + 0) * N + x] : make_float2(0.f, 0.f);
+                float2 hq = active ? hy[(pl_line * 2 + 1) * N + x] : make_float2(0.f, 0.f);
+                if (f != 1) {
+                    // -i (k/|k|) h (tilde_h0_t_cs.glsl:113-126); the DC mode gets 0
+                    const int   ix  = x - N / 2;
+                    const int   m   = ix * ix + iz * iz;
+                    const float rs  = m ? __frsqrt_rn((float)m) : 0.0f;
+                    const float fk  = -(float)(f == 0 ? ix : iz) * rs;
+                    const float fkq = -(float)(f == 0 ? (((N - x) & (N - 1)) - N / 2) : izq) * rs;
+                    hk = make_float2(-fk * hk.y, fk * hk.x);
+                    hq = make_float2(-fkq * hq.y, fkq * hq.x);
+                }
+                v[r] = make_float2(hk.x + hq.x, hk.y - hq.y);
             }
-            v[r] = make_float2(hk.x + hq.x, hk.y - hq.y);
-        }
-        __syncthreads();                                   // hy is read; the line buffers reuse it
-        line_fft<L, +1>(v, work + li * L::NPAD, tw_s, t);
-        if (active) {
-            float2* out = a.inter + ((size_t)f * H + yp) * NP;
+            __syncthreads();                               // hy is read; the line buffers reuse it
+            line_fft<L, +1>(v, work + li * L::NPAD, tw_s, t, li);
+            if (active) {
+                float2* out = a.inter + (((size_t)unit * 3 + f) * H + yp) * NP;
 #pragma unroll
-            for (int e = 0; e < L::E; ++e) {
-                const int x = LineOut<L>::pos(t, e);
-                out[x + 1] = v[e];
-                if (x == N - 1) out[0] = v[e];             // periodic pad columns
-                if (x == 0) out[N + 1] = v[e];
+                for (int e = 0; e < L::E; ++e) {
+                    const int x = LineOut<L>::pos(t, e);
+                    out[x + 1] = v[e];
+                    if (x == N - 1) out[0] = v[e];         // periodic pad columns
+                    if (x == 0) out[N + 1] = v[e];
+                }
             }
+            // the next prepass overwrites `work`: every line has finished
+            // reading its buffer
+            __syncthreads();
         }
-        // the next prepass overwrites `work`: line_fft ended with a barrier after
-        // its last shared-memory read
     }
 }
 
@@ -230,9 +246,15 @@ __global__ void __launch_bounds__(RowCfg<N>::THREADS) k_row_pass(RowArgs a)
 constexpr int ceil8(int x) { return (x + 7) / 8 * 8; }
 constexpr int imax(int a, int b) { return a > b ? a : b; }
 
+// Column-pass line decomposition: as LineFor except at N = 2048, where the
+// column CTA's 6 lines x 64 threads (32-point first pass) keep 168 registers
+// per thread without spilling (16-point lines would need 768 threads).
+template <int N> struct ColLineFor { using type = typename LineFor<N>::type; };
+template <> struct ColLineFor<2048> { using type = LineCfg<2048, 32, 8, 8>; };
+
 template <int N>
 struct ColCfg {
-    using L = typename LineFor<N>::type;
+    using L = typename ColLineFor<N>::type;
     static constexpr int C       = N >= 2048 ? 4 : 8;   // output columns per CTA
     static constexpr int CC      = C + 2;               // + one neighbour column each side
     static constexpr int WL      = CC;                  // round 1: Dy + i*Dx lines, one per column
@@ -259,7 +281,7 @@ __global__ void __launch_bounds__(ColCfg<N>::THREADS) k_col_pass(const __grid_co
 {
     using CF = ColCfg<N>;
     using L  = typename CF::L;
-    constexpr int C = CF::C, CC = CF::CC, H = CF::H, HP = CF::HP, OS = CF::OS, WL = CF::WL, ZL = CF::ZL;
+    constexpr int C = CF::C, CC = CF::CC, H = CF::H, OS = CF::OS, ZL = CF::ZL;
     extern __shared__ unsigned char smem_raw[];
     float2* smem = align_smem(smem_raw);
     float2* tw_s = smem;
@@ -272,8 +294,12 @@ __global__ void __launch_bounds__(ColCfg<N>::THREADS) k_col_pass(const __grid_co
     float*  sz = reinterpret_cast<float*>(tile + 2 * CF::FIELD);
     __shared__ __align__(8) uint64_t bar;
     __shared__ int wait_ok;
-    const int x0  = blockIdx.x * C;
-    const int tid = threadIdx.x;
+    const int x0   = blockIdx.x * C;
+    const int unit = blockIdx.y;
+    const int tid  = threadIdx.x;
+    // read the unit's fields where they are used (a struct copy would stay
+    // live in registers across the FFTs)
+    const ColUnit* cu = a.units ? a.units + unit : &a.u0;
 
     if (tid == 0) {
         mbar_init(&bar, 1);
@@ -290,7 +316,8 @@ __global__ void __launch_bounds__(ColCfg<N>::THREADS) k_col_pass(const __grid_co
         for (int f = 0; f < 3; ++f)
 #pragma unroll
             for (int q = 0; q < CF::NCHUNK; ++q)
-                tma_load_2d(tile + f * CF::FIELD + (size_t)q * CF::BR * CC, &a.map, 2 * x0, f * H + q * CF::BR, &bar);
+                tma_load_2d(tile + f * CF::FIELD + (size_t)q * CF::BR * CC, &a.map, 2 * x0,
+                            (unit * 3 + f) * H + q * CF::BR, &bar);
     }
     if (!block_wait(&bar, 0, &wait_ok, a.status)) return;
 
@@ -310,9 +337,10 @@ __global__ void __launch_bounds__(ColCfg<N>::THREADS) k_col_pass(const __grid_co
             v[r] = make_float2(p.x - q.y, p.y + q.x);        // p + i*q
         }
         __syncthreads();                                     // fields Dx, Dy consumed
-        line_fft<L, +1>(v, xbuf1 + cc * L::NPAD, tw_s, t);   // ends with a block barrier
+        line_fft<L, +1>(v, xbuf1 + cc * L::NPAD, tw_s, t, cc);
+        __syncthreads();                                     // every line done with xbuf1
         const int   xa = x0 - 1 + cc;                        // parity is all that matters
-        const float sa = a.scale, sb = a.scale * a.lambda;
+        const float sa = cu->scale, sb = cu->scale * cu->lambda;
 #pragma unroll
         for (int e = 0; e < L::E; ++e) {
             const int   y  = LineOut<L>::pos(t, e);
@@ -338,10 +366,11 @@ __global__ void __launch_bounds__(ColCfg<N>::THREADS) k_col_pass(const __grid_co
             }
         }
         __syncthreads();                                     // field Dz consumed
-        line_fft<L, +1>(v, xbuf2 + (zact ? p2 : 0) * L::NPAD, tw_s, t, zact);
+        if (zact || L::G < 32) line_fft<L, +1>(v, xbuf2 + (zact ? p2 : 0) * L::NPAD, tw_s, t, zact ? p2 : 0, zact);
+        __syncthreads();                                     // every line done with xbuf2
         if (zact) {
             const int   xa = x0 - 1 + 2 * p2;
-            const float sb = a.scale * a.lambda;
+            const float sb = cu->scale * cu->lambda;
 #pragma unroll
             for (int e = 0; e < L::E; ++e) {
                 const int   y  = LineOut<L>::pos(t, e);
@@ -356,6 +385,11 @@ __global__ void __launch_bounds__(ColCfg<N>::THREADS) k_col_pass(const __grid_co
     // Epilogue: a 4-row x 2-column block per thread (float4 shared reads down
     // the staged columns, float2 global stores across them); Sobel normal on Dy
     // and the Jacobian of x - (Dx, Dz).
+    float* const  odx = cu->dx;
+    float* const  ody = cu->dy;
+    float* const  odz = cu->dz;
+    float4* const onj = cu->nj;
+    const float   inv2d = cu->inv2d;
     for (int i = tid; i < (C / 2) * (N / 4); i += CF::THREADS) {
         const int cp = i % (C / 2), y0 = 4 * (i / (C / 2));
         const int cb = 2 * cp + 1;                                // staged column of output column 2cp
@@ -396,21 +430,21 @@ __global__ void __launch_bounds__(ColCfg<N>::THREADS) k_col_pass(const __grid_co
                 const float rn = rsqrtf(nx * nx + 1.0f + nz * nz);
                 const float xl = d == 0 ? XS[0][k] : X[0][k + 1], xr = d == 0 ? X[1][k + 1] : XS[1][k];
                 const float zl = d == 0 ? ZS[0][k] : Z[0][k + 1], zr = d == 0 ? Z[1][k + 1] : ZS[1][k];
-                const float dxx = (xr - xl) * a.inv2d;
-                const float dxz = (X[d][k + 2] - X[d][k]) * a.inv2d;
-                const float dzx = (zr - zl) * a.inv2d;
-                const float dzz = (Z[d][k + 2] - Z[d][k]) * a.inv2d;
+                const float dxx = (xr - xl) * inv2d;
+                const float dxz = (X[d][k + 2] - X[d][k]) * inv2d;
+                const float dzx = (zr - zl) * inv2d;
+                const float dzz = (Z[d][k + 2] - Z[d][k]) * inv2d;
                 // J = (1 - dxx)(1 - dzz) - dxz*dzx, formed as 1 + deviation so that
                 // the only rounding at the scale of 1 is the final add
                 const float dJ = (dxx * dzz - dxz * dzx) - dxx - dzz;
                 njv[d] = make_float4(nx * rn, rn, nz * rn, 1.0f + dJ);
             }
             const size_t o = (size_t)(y0 + k) * N + x0 + 2 * cp;
-            *reinterpret_cast<float2*>(a.dx + o) = make_float2(X[0][k + 1], X[1][k + 1]);
-            *reinterpret_cast<float2*>(a.dy + o) = make_float2(Y[1][k + 1], Y[2][k + 1]);
-            *reinterpret_cast<float2*>(a.dz + o) = make_float2(Z[0][k + 1], Z[1][k + 1]);
-            a.nj[o]     = njv[0];
-            a.nj[o + 1] = njv[1];
+            *reinterpret_cast<float2*>(odx + o) = make_float2(X[0][k + 1], X[1][k + 1]);
+            *reinterpret_cast<float2*>(ody + o) = make_float2(Y[1][k + 1], Y[2][k + 1]);
+            *reinterpret_cast<float2*>(odz + o) = make_float2(Z[0][k + 1], Z[1][k + 1]);
+            onj[o]     = njv[0];
+            onj[o + 1] = njv[1];
         }
     }
 }
@@ -425,28 +459,37 @@ cudaError_t launch_h0(const H0Args& a, const float* noise, float4* h0, cudaStrea
     return cudaGetLastError();
 }
 
-template <int N>
-static cudaError_t row_pass_n(const RowArgs& a, cudaStream_t s)
+template <int N, bool MULTI>
+static cudaError_t row_pass_nm(const RowArgs& a, cudaStream_t s)
 {
     using RC = RowCfg<N>;
-    static int grid = 0;
+    static int grid = 0;   // persistent grid: resident CTAs per SM x SMs
     if (!grid) {
-        cudaError_t e = cudaFuncSetAttribute(k_row_pass<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)RC::SMEM);
+        cudaError_t e =
+            cudaFuncSetAttribute(k_row_pass<N, MULTI>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)RC::SMEM);
         if (e != cudaSuccess) return e;
         int per_sm = 0, dev = 0, sms = 0;
-        if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_row_pass<N>, RC::THREADS, RC::SMEM)) != cudaSuccess)
+        if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_row_pass<N, MULTI>, RC::THREADS, RC::SMEM)) !=
+            cudaSuccess)
             return e;
         if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
         if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
         if (per_sm < 1) return cudaErrorInvalidConfiguration;
-        grid = per_sm * sms < RC::ITEMS ? per_sm * sms : RC::ITEMS;
+        grid = per_sm * sms;
     }
-    k_row_pass<N><<<grid, RC::THREADS, RC::SMEM, s>>>(a);
+    const int items = a.tiles * RC::ITEMS;
+    k_row_pass<N, MULTI><<<grid < items ? grid : items, RC::THREADS, RC::SMEM, s>>>(a);
     return cudaGetLastError();
 }
 
 template <int N>
-static cudaError_t col_pass_n(const ColArgs& a, cudaStream_t s, bool pdl)
+static cudaError_t row_pass_n(const RowArgs& a, cudaStream_t s)
+{
+    return (a.tiles == 1 && a.S == 1 && !a.fcs) ? row_pass_nm<N, false>(a, s) : row_pass_nm<N, true>(a, s);
+}
+
+template <int N>
+static cudaError_t col_pass_n(int units, const ColArgs& a, cudaStream_t s, bool pdl)
 {
     using CF = ColCfg<N>;
     static bool attr = false;
@@ -456,7 +499,7 @@ static cudaError_t col_pass_n(const ColArgs& a, cudaStream_t s, bool pdl)
         attr = true;
     }
     cudaLaunchConfig_t cfg = {};
-    cfg.gridDim          = dim3(CF::GRID);
+    cfg.gridDim          = dim3(CF::GRID, units);
     cfg.blockDim         = dim3(CF::THREADS);
     cfg.dynamicSmemBytes = CF::SMEM;
     cfg.stream           = s;
@@ -487,10 +530,10 @@ cudaError_t launch_row_pass(int N, const RowArgs& a, cudaStream_t s)
     }
 }
 
-cudaError_t launch_col_pass(int N, const ColArgs& a, cudaStream_t s, bool pdl)
+cudaError_t launch_col_pass(int N, int units, const ColArgs& a, cudaStream_t s, bool pdl)
 {
     switch (N) {
-#define CASE(n) case n: return col_pass_n<n>(a, s, pdl);
+#define CASE(n) case n: return col_pass_n<n>(units, a, s, pdl);
         OCEAN_FOR_EACH_N(CASE)
 #undef CASE
     default: return cudaErrorInvalidValue;

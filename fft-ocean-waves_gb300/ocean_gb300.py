@@ -34,7 +34,8 @@ EXPORTS = [
     "ocean_update_columns", "ocean_get_outputs",
     "ocean_set_params", "ocean_get_params", "ocean_get_h0", "ocean_set_h0", "ocean_compute_h0",
     "ocean_fill_noise", "ocean_bit_reversed_indices", "ocean_butterfly_table", "ocean_last_error",
-    "ocean_version", "ocean_backward", "ocean_device_status",
+    "ocean_version", "ocean_backward", "ocean_device_status", "ocean_batch_create", "ocean_batch_update",
+    "ocean_batch_device_status", "ocean_batch_destroy",
 ]
 OCEAN_GRAD_ACCUMULATE = 1
 
@@ -117,9 +118,14 @@ def load() -> C.CDLL:
     L.ocean_butterfly_table.argtypes = [C.c_int32, P(C.c_float)]
     L.ocean_backward.argtypes = [vp, P(C.c_double), C.c_int32, vp, vp, vp, C.c_uint32, P(ocean_grads), vp]
     L.ocean_device_status.argtypes = [vp, vp]
+    L.ocean_batch_create.argtypes = [P(ocean_params), P(C.c_uint64), C.c_int32, C.c_int32, P(vp)]
+    L.ocean_batch_update.argtypes = [vp, P(C.c_double), P(ocean_outputs), vp]
+    L.ocean_batch_device_status.argtypes = [vp, vp]
+    L.ocean_batch_destroy.argtypes = [vp]
+    L.ocean_batch_destroy.restype = None
     L.ocean_last_error.restype = C.c_char_p
     for name in EXPORTS:
-        if name not in ("ocean_destroy", "ocean_last_error"):
+        if name not in ("ocean_destroy", "ocean_last_error", "ocean_batch_destroy"):
             getattr(L, name).restype = C.c_int
     _lib = L
     return L
@@ -250,6 +256,53 @@ class Ocean:
     def close(self) -> None:
         if self._h and self._h.value:
             load().ocean_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class OceanBatch:
+    """Independent tiles (any mix of N) advanced `samples` time samples per
+    update in one CUDA-graph replay (ocean_batch_* of include/ocean.h)."""
+
+    def __init__(self, params_list, seeds, samples: int):
+        L = load()
+        n = len(params_list)
+        if len(seeds) != n:
+            raise ValueError("one seed per tile")
+        self.params = list(params_list)
+        self.samples = int(samples)
+        ps = (ocean_params * n)(*[p.c() for p in params_list])
+        ss = (C.c_uint64 * n)(*[int(x) for x in seeds])
+        self._h = C.c_void_p()
+        check(L.ocean_batch_create(ps, ss, n, self.samples, C.byref(self._h)))
+
+    def update(self, times, outputs, stream=None) -> None:
+        """times: n_tiles*samples values (tile-major); outputs: as many
+        (dx, dy, dz, normal_j) tuples of device buffers."""
+        n = len(self.params) * self.samples
+        if len(times) != n or len(outputs) != n:
+            raise ValueError(f"need {n} times and output sets")
+        ts = (C.c_double * n)(*[float(t) for t in times])
+        os_ = (ocean_outputs * n)(*[ocean_outputs(*[_addr(b) for b in o]) for o in outputs])
+        check(load().ocean_batch_update(self._h, ts, os_, _stream(stream)))
+
+    def device_status(self, stream=None) -> None:
+        check(load().ocean_batch_device_status(self._h, _stream(stream)))
+
+    def close(self) -> None:
+        if self._h and self._h.value:
+            load().ocean_batch_destroy(self._h)
             self._h = C.c_void_p()
 
     def __enter__(self):

@@ -147,6 +147,30 @@ OCEAN_API int ocean_fill_noise(uint64_t seed, int32_t N, float* host_out);
 OCEAN_API int ocean_bit_reversed_indices(int32_t N, int32_t* host_out);
 OCEAN_API int ocean_butterfly_table(int32_t N, float* host_out);
 
+/* ---- Batched tiles ---------------------------------------------------- */
+
+typedef struct ocean_batch_s ocean_batch_t;
+
+/* A batch of n_tiles independent tiles, each with its own parameters (any
+ * supported N; tiles of equal N are grouped) and its own seeded noise
+ * (ocean_fill_noise(seeds[i], N)), advanced `samples` time samples per
+ * ocean_batch_update.  h0 is built at creation.  Synchronous. */
+OCEAN_API int ocean_batch_create(const ocean_params* params, const uint64_t* seeds, int32_t n_tiles,
+                                 int32_t samples, ocean_batch_t** out);
+
+/* Advance every tile to its `samples` times: times[tile*samples + s] (host),
+ * outputs into outs[tile*samples + s] (device pointers, 16-byte aligned).
+ * All launches (per distinct N: one persistent row pass reading each h0 row
+ * once for all samples, one column pass) replay as one CUDA graph on
+ * `stream`.  The host-side constants go through a pinned staging buffer: a
+ * call first waits for the previous call's graph to finish. */
+OCEAN_API int ocean_batch_update(ocean_batch_t* batch, const double* times, const ocean_outputs* outs, void* stream);
+
+/* As ocean_device_status, for the batch's kernels. */
+OCEAN_API int ocean_batch_device_status(ocean_batch_t* batch, void* stream);
+
+OCEAN_API void ocean_batch_destroy(ocean_batch_t* batch);
+
 /* ---- Adjoint --------------------------------------------------------- */
 
 /* Flags for ocean_backward */
