@@ -138,13 +138,15 @@ template <> struct LineFor<512>  { using type = LineCfg<512, 16, 16, 2>; };
 template <> struct LineFor<1024> { using type = LineCfg<1024, 16, 16, 4>; };
 template <> struct LineFor<2048> { using type = LineCfg<2048, 16, 16, 8>; };
 
-// Barrier among the threads of one line.  Lines of >= 32 threads (whole
-// warps) use named barrier 1 + li, so lines progress independently; smaller
-// lines share warps and fall back to the block barrier.
-template <class C>
+// Barrier among the threads of one line.  With NAMED, lines of >= 32 threads
+// use named barrier 1 + li, so lines progress independently; this requires
+// every warp to belong to a single line (threads of one warp must not wait on
+// different barriers).  Smaller lines, or kernels whose warps mix lines, use
+// the block barrier.
+template <class C, bool NAMED>
 __device__ __forceinline__ void line_sync(int li)
 {
-    if constexpr (C::G >= 32)
+    if constexpr (NAMED && C::G >= 32)
         asm volatile("bar.sync %0, %1;" ::"r"(1 + li), "n"(C::G) : "memory");
     else
         __syncthreads();
@@ -154,7 +156,7 @@ __device__ __forceinline__ void line_sync(int li)
 // with stride NSP; they are written to `buf`, re-read as the inputs of a pass
 // of radix RN (stride NSP*RP), twiddled and transformed.  Contains two line
 // barriers (see line_sync).
-template <class C, int RP, int NSP, int RN, int SIGN>
+template <class C, int RP, int NSP, int RN, int SIGN, bool NAMED>
 __device__ __forceinline__ void stockham_pass(float2* v, float2* buf, const float2* tw, int t, bool active, int li)
 {
     constexpr int N   = C::N;
@@ -168,7 +170,7 @@ __device__ __forceinline__ void stockham_pass(float2* v, float2* buf, const floa
             for (int r = 0; r < RP; ++r) buf[C::pad(idxD + r * NSP)] = v[b * RP + r];
         }
     }
-    line_sync<C>(li);
+    line_sync<C, NAMED>(li);
     if (active) {
 #pragma unroll
         for (int b = 0; b < C::R1 / RN; ++b) {
@@ -177,7 +179,7 @@ __device__ __forceinline__ void stockham_pass(float2* v, float2* buf, const floa
             for (int r = 0; r < RN; ++r) v[b * RN + r] = buf[C::pad(j + r * (N / RN))];
         }
     }
-    line_sync<C>(li);
+    line_sync<C, NAMED>(li);
     if (!active) return;
 #pragma unroll
     for (int b = 0; b < C::R1 / RN; ++b) {
@@ -218,19 +220,20 @@ __device__ __forceinline__ void stockham_pass(float2* v, float2* buf, const floa
     }
 }
 
-// Full line transform of line `li` (barrier id 1 + li, so li < 15).  On entry
+// Full line transform of line `li` (barrier id 1 + li, so li < 15; NAMED as
+// in line_sync).  On entry
 // v[r] = x[t + r*N/R1]; on exit v[b*RL + r] = X[(t + b*G) + r*(N/RL)] with RL
 // the last radix.  tw: N-entry table tw[i] = exp(+2*pi*i*i/N) (conjugated here
 // for SIGN < 0).  On return every thread of the line has finished reading
 // `buf`.  Threads with active == false do no work; for lines of >= 32 threads
 // they may skip the call entirely, for smaller lines they must call it (the
 // barrier is then the block's).
-template <class C, int SIGN>
+template <class C, int SIGN, bool NAMED = true>
 __device__ __forceinline__ void line_fft(float2* v, float2* buf, const float2* tw, int t, int li, bool active = true)
 {
     if (active) dft<C::R1, SIGN>(v);
-    stockham_pass<C, C::R1, 1, C::R2, SIGN>(v, buf, tw, t, active, li);
-    if constexpr (C::R3 > 1) stockham_pass<C, C::R2, C::R1, C::R3, SIGN>(v, buf, tw, t, active, li);
+    stockham_pass<C, C::R1, 1, C::R2, SIGN, NAMED>(v, buf, tw, t, active, li);
+    if constexpr (C::R3 > 1) stockham_pass<C, C::R2, C::R1, C::R3, SIGN, NAMED>(v, buf, tw, t, active, li);
 }
 
 template <class C>

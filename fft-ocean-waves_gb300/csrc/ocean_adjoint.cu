@@ -95,7 +95,8 @@ __global__ void __launch_bounds__(AdjColCfg<N>::THREADS) k_adj_col_pass(AdjColAr
     }
     __syncthreads();
     float2* lb = buf + li * LS;
-    line_fft<L, -1>(v, lb, tw_s, t, li);
+    // columns-fastest lanes put several lines in one warp: block barriers
+    line_fft<L, -1, false>(v, lb, tw_s, t, li);
 #pragma unroll
     for (int e = 0; e < L::E; ++e) lb[L::pad(LineOut<L>::pos(t, e))] = v[e];
     __syncthreads();
