@@ -1,0 +1,154 @@
+// ocean_static.cu -- ocean_update_noalloc: one ocean frame without any device
+// allocation, for callers that cannot call cudaMalloc.
+//
+// Some callers of this library cannot allocate device memory on their own:
+// plug-in hosts that own the CUDA context and forbid allocation from plug-in
+// code, code that runs while the application's allocator is locked or its
+// memory pool is exhausted, and callers that must hold a fixed memory budget
+// decided at load time.  For them this entry point takes the spectrum h0 and
+// the output maps from the caller and keeps the one piece of scratch the frame
+// needs -- the row-pass intermediate -- in a fixed array compiled into this
+// library, instead of in a handle's cudaMalloc'd buffer.
+//
+// The array is a file-scope `static __device__` array sized for N <= 1024
+// (12,632,112 bytes); every GPU that loads the library holds it until the
+// process exits.  In host code its name is only a stand-in: the device address
+// is obtained with cudaGetSymbolAddress once per device, with that device
+// current, on the first call made on that device.
+#include <cuda.h>
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <mutex>
+#include <string>
+
+#include "ocean.h"
+#include "ocean_host.h"
+#include "ocean_internal.h"
+
+namespace {
+
+constexpr int    kStaticMaxN     = 1024;
+constexpr size_t kStaticInterLen = 3 * (size_t)(kStaticMaxN / 2 + 1) * (kStaticMaxN + 2);  // float2
+
+// The frame's scratch: row-pass intermediate, twiddle table, device status word.
+static __device__ __align__(256) float2   g_static_inter[kStaticInterLen];
+static __device__ __align__(256) float2   g_static_tw[kStaticMaxN];
+static __device__ __align__(256) unsigned g_static_status;
+
+constexpr int kMaxDevices = 64;
+
+struct DeviceScratch {
+    bool        ready   = false;
+    float2*     inter   = nullptr;   // device addresses of the arrays above
+    float2*     tw      = nullptr;
+    unsigned*   status  = nullptr;
+    int         tw_N    = 0;         // N whose twiddles the table holds
+    int         map_N   = 0;         // N the tensor map was encoded for
+    CUtensorMap map;
+};
+
+// exp(+2*pi*i*k/N) for k < N, from double-precision sincospi.
+__global__ void k_static_twiddles(float2* tw, int N)
+{
+    const int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= N) return;
+    double sn, cs;
+    sincospi(2.0 * (double)k / (double)N, &sn, &cs);
+    tw[k] = make_float2((float)cs, (float)sn);
+}
+
+std::mutex    g_mu;
+DeviceScratch g_dev[kMaxDevices];
+
+// Per-device set-up: resolve the arrays' device addresses (cudaGetSymbolAddress
+// with this device current) and clear the status word.
+int setup(int dev, DeviceScratch& d, cudaStream_t s)
+{
+    cudaError_t e;
+    if ((e = cudaGetSymbolAddress(reinterpret_cast<void**>(&d.inter), g_static_inter)) != cudaSuccess ||
+        (e = cudaGetSymbolAddress(reinterpret_cast<void**>(&d.tw), g_static_tw)) != cudaSuccess ||
+        (e = cudaGetSymbolAddress(reinterpret_cast<void**>(&d.status), g_static_status)) != cudaSuccess)
+        return ocean::host::cuda_fail(e, "cudaGetSymbolAddress of the static scratch");
+    if ((e = cudaMemsetAsync(d.status, 0, sizeof(unsigned), s)) != cudaSuccess)
+        return ocean::host::cuda_fail(e, "static status clear");
+    (void)dev;
+    d.ready = true;
+    return OCEAN_OK;
+}
+
+}  // namespace
+
+using namespace ocean::host;
+
+extern "C" int ocean_update_noalloc(const ocean_params* params, const float* h0_dev, double t,
+                                    const ocean_outputs* out, void* stream)
+{
+    int rc = validate(params);
+    if (rc) return rc;
+    if (params->N > kStaticMaxN)
+        return fail(OCEAN_ERR_INVALID, "ocean_update_noalloc supports N <= " + std::to_string(kStaticMaxN) +
+                                           " (its static scratch is sized for that), got N = " +
+                                           std::to_string(params->N));
+    if (!h0_dev || !out) return fail(OCEAN_ERR_INVALID, "NULL argument");
+    if (!std::isfinite(t)) return fail(OCEAN_ERR_INVALID, "time is not finite");
+    if (!out->dx || !out->dy || !out->dz || !out->normal_j) return fail(OCEAN_ERR_INVALID, "NULL output pointer");
+    const uintptr_t al = reinterpret_cast<uintptr_t>(h0_dev) | reinterpret_cast<uintptr_t>(out->dx) |
+                         reinterpret_cast<uintptr_t>(out->dy) | reinterpret_cast<uintptr_t>(out->dz) |
+                         reinterpret_cast<uintptr_t>(out->normal_j);
+    if (al % 16) return fail(OCEAN_ERR_INVALID, "h0 and output pointers must be 16-byte aligned");
+    if ((rc = check_device()) != OCEAN_OK) return rc;
+    int         dev = 0;
+    cudaError_t e   = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
+    if (dev < 0 || dev >= kMaxDevices) return fail(OCEAN_ERR_UNSUPPORTED, "device ordinal out of range");
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    const int    N = params->N;
+
+    std::lock_guard<std::mutex> lock(g_mu);
+    DeviceScratch&              d = g_dev[dev];
+    if (!d.ready && (rc = setup(dev, d, s)) != OCEAN_OK) return rc;
+    if (d.tw_N != N) {                 // the table holds another size's twiddles
+        k_static_twiddles<<<(N + 255) / 256, 256, 0, s>>>(d.tw, N);
+        if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(e, "static twiddle launch");
+        d.tw_N = N;
+    }
+    if (d.map_N != N) {
+        if ((rc = encode_inter_map(&d.map, d.inter, N, 1)) != OCEAN_OK) return rc;
+        d.map_N = N;
+    }
+
+    // one frame: the same two kernels as ocean_update, scratch from the arrays
+    const double g  = gravity_of(*params);
+    const double K  = std::sqrt(g / (2.0 * M_PI * (double)params->L));
+    const double kt = K * t;
+    ocean::RowArgs ra;
+    ra.h0              = reinterpret_cast<const float4*>(h0_dev);
+    ra.inter           = d.inter;
+    ra.tw              = d.tw;
+    ra.status          = d.status;
+    ra.fcs             = nullptr;
+    ra.fc0.kt_hi       = (float)kt;
+    ra.fc0.kt_lo       = (float)(kt - (double)ra.fc0.kt_hi);
+    const double dc    = std::sqrt(g * 0.00001) * t / (2.0 * M_PI);
+    ra.fc0.dc_cycles   = (float)(dc - std::nearbyint(dc));
+    ra.fc0.literal_conj = (params->flags & OCEAN_FLAG_LITERAL_CONJ) ? 1 : 0;
+    ra.tiles           = 1;
+    ra.S               = 1;
+    if ((e = ocean::launch_row_pass(N, ra, s)) != cudaSuccess) return cuda_fail(e, "row pass launch");
+    ocean::ColArgs ca;
+    ca.map       = d.map;
+    ca.status    = d.status;
+    ca.tw        = d.tw;
+    ca.units     = nullptr;
+    ca.u0.dx     = out->dx;
+    ca.u0.dy     = out->dy;
+    ca.u0.dz     = out->dz;
+    ca.u0.nj     = reinterpret_cast<float4*>(out->normal_j);
+    ca.u0.scale  = (float)(0.5 / ((double)N * N));
+    ca.u0.lambda = params->choppiness;
+    ca.u0.inv2d  = (float)((double)N / (2.0 * (double)params->L));
+    ca.u0.pad_   = 0.0f;
+    if ((e = ocean::launch_col_pass(N, 1, ca, s, true)) != cudaSuccess) return cuda_fail(e, "column pass launch");
+    return OCEAN_OK;
+}

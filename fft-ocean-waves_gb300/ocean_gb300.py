@@ -35,7 +35,7 @@ EXPORTS = [
     "ocean_set_params", "ocean_get_params", "ocean_get_h0", "ocean_set_h0", "ocean_compute_h0",
     "ocean_fill_noise", "ocean_bit_reversed_indices", "ocean_butterfly_table", "ocean_last_error",
     "ocean_version", "ocean_backward", "ocean_device_status", "ocean_batch_create", "ocean_batch_update",
-    "ocean_batch_device_status", "ocean_batch_destroy",
+    "ocean_batch_device_status", "ocean_batch_destroy", "ocean_update_noalloc",
 ]
 OCEAN_GRAD_ACCUMULATE = 1
 
@@ -123,6 +123,7 @@ def load() -> C.CDLL:
     L.ocean_batch_device_status.argtypes = [vp, vp]
     L.ocean_batch_destroy.argtypes = [vp]
     L.ocean_batch_destroy.restype = None
+    L.ocean_update_noalloc.argtypes = [P(ocean_params), vp, C.c_double, P(ocean_outputs), vp]
     L.ocean_last_error.restype = C.c_char_p
     for name in EXPORTS:
         if name not in ("ocean_destroy", "ocean_last_error", "ocean_batch_destroy"):
@@ -176,6 +177,14 @@ def butterfly_table(N: int):
     out = np.empty((lg, N, 4), dtype=np.float32)
     check(load().ocean_butterfly_table(N, out.ctypes.data_as(C.POINTER(C.c_float))))
     return out
+
+
+def update_noalloc(params: Params, h0_dev, t: float, dx, dy, dz, normal_j, stream=None) -> None:
+    """One frame from a caller-held h0 without any device allocation
+    (ocean_update_noalloc: static scratch, N <= 1024)."""
+    cp = params.c()
+    o = ocean_outputs(_addr(dx), _addr(dy), _addr(dz), _addr(normal_j))
+    check(load().ocean_update_noalloc(C.byref(cp), _addr(h0_dev), float(t), C.byref(o), _stream(stream)))
 
 
 def compute_h0(params: Params, noise_dev, h0_dev, stream=None) -> None:

@@ -171,6 +171,26 @@ OCEAN_API int ocean_batch_device_status(ocean_batch_t* batch, void* stream);
 
 OCEAN_API void ocean_batch_destroy(ocean_batch_t* batch);
 
+/* ---- Frame update without device allocation ------------------------ */
+
+/* One frame, like ocean_update, for callers that cannot call cudaMalloc:
+ * plug-in hosts that own the CUDA context and forbid allocation from plug-in
+ * code, code running while the application's allocator is locked or its pool
+ * exhausted, and callers held to a memory budget fixed at load time.  No
+ * handle: the caller passes the parameters, the spectrum h0 (device,
+ * N*N*4 floats, the layout of ocean_get_h0 / ocean_compute_h0) and the output
+ * maps.  The frame's scratch (the row-pass intermediate, 12,632,112 bytes,
+ * plus a twiddle table and a status word) lives in static device arrays
+ * compiled into the library, sized for N <= 1024; every GPU that loads the
+ * library holds them until the process exits.  N > 1024 is rejected with
+ * OCEAN_ERR_INVALID.  The first call on a device resolves the arrays' addresses
+ * (cudaGetSymbolAddress) and clears the status word: make that first call
+ * before any stream capture.  Every call uses the same arrays, so calls whose
+ * work overlaps on the GPU (other streams, other threads) race: serialise
+ * them.  Calls no cudaMalloc/cudaFree.  No counterpart in the reference. */
+OCEAN_API int ocean_update_noalloc(const ocean_params* params, const float* h0_dev, double t,
+                                   const ocean_outputs* out, void* stream);
+
 /* ---- Adjoint --------------------------------------------------------- */
 
 /* Flags for ocean_backward */
