@@ -242,7 +242,10 @@ struct LineOut {
     static constexpr int B  = C::R1 / RL;          // butterflies per thread in the last pass
     static constexpr int NS = C::N / RL;           // output stride of the last pass
     // position of register e = b*RL + r after line_fft
-    __device__ __forceinline__ static int pos(int t, int e) { return (t + (e / RL) * C::G) + (e % RL) * NS; }
+    __host__ __device__ __forceinline__ static constexpr int pos(int t, int e)
+    {
+        return (t + (e / RL) * C::G) + (e % RL) * NS;
+    }
 };
 
 }  // namespace ocean

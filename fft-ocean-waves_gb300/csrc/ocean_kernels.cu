@@ -226,12 +226,12 @@ __global__ void __launch_bounds__(RowCfg<N>::THREADS) k_row_pass(RowArgs a)
             if (active) {
                 float2* out = a.inter + (((size_t)unit * 3 + f) * H + yp) * NP;
 #pragma unroll
-                for (int e = 0; e < L::E; ++e) {
-                    const int x = LineOut<L>::pos(t, e);
-                    out[x + 1] = v[e];
-                    if (x == N - 1) out[0] = v[e];         // periodic pad columns
-                    if (x == 0) out[N + 1] = v[e];
-                }
+                for (int e = 0; e < L::E; ++e) out[LineOut<L>::pos(t, e) + 1] = v[e];
+                // periodic pad columns: x = 0 is thread 0's first output and
+                // x = N-1 the last thread's last one
+                static_assert(LineOut<L>::pos(0, 0) == 0 && LineOut<L>::pos(L::G - 1, L::E - 1) == N - 1, "pad");
+                if (t == 0) out[N + 1] = v[0];
+                if (t == L::G - 1) out[0] = v[L::E - 1];
             }
             // the next prepass overwrites `work`: every line has finished
             // reading its buffer
