@@ -159,6 +159,7 @@ struct ocean_s {
     ocean_params p{};
     int          N = 0;
     float4*      h0     = nullptr;  // [N][N]
+    float2*      spec   = nullptr;  // combined spectrum read by the row pass [spec_len(N)]
     float2*      inter  = nullptr;  // [3][N/2+1][N+2] (periodic pad column each side)
     unsigned*    status = nullptr;  // device status word (bounded-wait time-outs)
     CUtensorMap  inter_map;         // column-pass view of inter
@@ -175,6 +176,7 @@ struct ocean_s {
     ~ocean_s()
     {
         cudaFree(h0);
+        cudaFree(spec);
         cudaFree(inter);
         cudaFree(status);
         cudaFree(tw);
@@ -221,6 +223,15 @@ struct ocean_s {
     {
         cudaError_t e = ocean::launch_h0(h0_args(p), noise, h0, s);
         if (e != cudaSuccess) return cuda_fail(e, "h0 init launch");
+        return build_spec(s);
+    }
+
+    // The row pass's combined spectrum, after every change of h0 or of the
+    // conjugation flag.
+    int build_spec(cudaStream_t s)
+    {
+        cudaError_t e = ocean::launch_spec_combine(N, 1, h0, (p.flags & OCEAN_FLAG_LITERAL_CONJ) ? 1 : 0, spec, s);
+        if (e != cudaSuccess) return cuda_fail(e, "spectrum combine launch");
         return OCEAN_OK;
     }
 };
@@ -314,6 +325,7 @@ int ocean_create(const ocean_params* params, const float* noise_host, ocean_t** 
     const size_t N = (size_t)o->N;
     const size_t H = (size_t)ocean::inter_rows(o->N), NP = (size_t)ocean::inter_pitch(o->N);
     if ((e = cudaMalloc(&o->h0, N * N * sizeof(float4))) != cudaSuccess ||
+        (e = cudaMalloc(&o->spec, ocean::spec_len(o->N) * sizeof(float2))) != cudaSuccess ||
         (e = cudaMalloc(&o->inter, 3 * H * NP * sizeof(float2))) != cudaSuccess ||
         (e = cudaMalloc(&o->status, sizeof(unsigned))) != cudaSuccess ||
         (e = cudaMalloc(&o->noise, 4 * N * N * sizeof(float))) != cudaSuccess) {
@@ -397,7 +409,7 @@ int ocean_set_h0(ocean_t* o, const float* src, void* stream)
     cudaError_t e = cudaMemcpyAsync(o->h0, src, (size_t)o->N * o->N * sizeof(float4), cudaMemcpyDefault,
                                     static_cast<cudaStream_t>(stream));
     if (e != cudaSuccess) return cuda_fail(e, "ocean_set_h0");
-    return OCEAN_OK;
+    return o->build_spec(static_cast<cudaStream_t>(stream));
 }
 
 int ocean_get_outputs(ocean_t* o, ocean_outputs* out)
@@ -423,6 +435,7 @@ int ocean_update_rows(ocean_t* o, double t, void* stream)
     if (!o) return fail(OCEAN_ERR_INVALID, "ocean is NULL");
     if (!std::isfinite(t)) return fail(OCEAN_ERR_INVALID, "time is not finite");
     ocean::RowArgs ra;
+    ra.spec       = o->spec;
     ra.h0         = o->h0;
     ra.inter      = o->inter;
     ra.tw         = o->tw;

@@ -1,11 +1,12 @@
 // ocean_batch.cpp -- batches of independent tiles (ocean_batch_* in
 // include/ocean.h).  No counterpart in the reference, which renders one tile.
 //
-// Tiles are grouped by N.  Per group: h0 of every tile back to back, one
+// Tiles are grouped by N.  Per group: the combined spectrum (G, D) of every
+// tile back to back (h0 itself is only a creation-time temporary), one
 // intermediate per (tile, time sample) back to back, one tensor map over all
 // of them, and one twiddle table.  An update is a CUDA graph of
 //   H2D copy of the per-unit constants (pinned staging -> device)
-//   per group: k_row_pass (persistent; each h0 row pair is staged once and
+//   per group: k_row_pass (persistent; each spectrum row pair is staged once and
 //              serves all samples of its tile) -> k_col_pass (grid: column
 //              tiles x units, programmatic dependent of the row pass)
 // captured at creation and replayed by ocean_batch_update.
@@ -26,7 +27,7 @@ struct ocean_batch_s {
     struct Group {
         int              N = 0;
         std::vector<int> tiles;          // batch tile indices, in slot order
-        float4*          h0    = nullptr;
+        float2*          spec  = nullptr;
         float2*          inter = nullptr;
         float2*          tw    = nullptr;
         CUtensorMap      map;
@@ -55,7 +56,7 @@ struct ocean_batch_s {
         if (done) cudaEventDestroy(done);
         if (cap) cudaStreamDestroy(cap);
         for (Group& g : groups) {
-            cudaFree(g.h0);
+            cudaFree(g.spec);
             cudaFree(g.inter);
             cudaFree(g.tw);
         }
@@ -87,7 +88,8 @@ int capture(ocean_batch_s* b)
     for (size_t gi = 0; gi < b->groups.size() && e == cudaSuccess; ++gi) {
         ocean_batch_s::Group& g = b->groups[gi];
         ocean::RowArgs ra;
-        ra.h0     = g.h0;
+        ra.spec   = g.spec;
+        ra.h0     = nullptr;
         ra.inter  = g.inter;
         ra.tw     = g.tw;
         ra.status = b->status;
@@ -161,28 +163,33 @@ int ocean_batch_create(const ocean_params* params, const uint64_t* seeds, int32_
     b->desc_bytes = b->units * (sizeof(ocean::FrameConsts) + sizeof(ocean::ColUnit));
     std::vector<float> noise;
     float*             d_noise = nullptr;
+    float4*            d_h0    = nullptr;
     const int          maxN    = b->groups.front().N;
     if ((e = cudaMalloc(&b->status, sizeof(unsigned))) != cudaSuccess ||
         (e = cudaMemset(b->status, 0, sizeof(unsigned))) != cudaSuccess ||
         (e = cudaMalloc(&b->d_desc, b->desc_bytes)) != cudaSuccess ||
         (e = cudaMallocHost(&b->h_desc, b->desc_bytes)) != cudaSuccess ||
-        (e = cudaMalloc(&d_noise, 4 * (size_t)maxN * maxN * sizeof(float))) != cudaSuccess) {
+        (e = cudaMalloc(&d_noise, 4 * (size_t)maxN * maxN * sizeof(float))) != cudaSuccess ||
+        (e = cudaMalloc(&d_h0, (size_t)maxN * maxN * sizeof(float4))) != cudaSuccess) {
         cudaFree(d_noise);
+        cudaFree(d_h0);
         delete b;
         return fail(OCEAN_ERR_NOMEM, std::string("batch allocation failed: ") + cudaGetErrorString(e));
     }
     for (ocean_batch_s::Group& g : b->groups) {
         const size_t N = (size_t)g.N, NN = N * N, T = g.tiles.size();
         const size_t H = (size_t)ocean::inter_rows(g.N), NP = (size_t)ocean::inter_pitch(g.N);
-        if ((e = cudaMalloc(&g.h0, T * NN * sizeof(float4))) != cudaSuccess ||
+        if ((e = cudaMalloc(&g.spec, T * ocean::spec_len(g.N) * sizeof(float2))) != cudaSuccess ||
             (e = cudaMalloc(&g.inter, T * samples * 3 * H * NP * sizeof(float2))) != cudaSuccess) {
             cudaFree(d_noise);
+            cudaFree(d_h0);
             delete b;
             return fail(OCEAN_ERR_NOMEM, std::string("batch allocation failed: ") + cudaGetErrorString(e));
         }
         if ((rc = upload_twiddles(&g.tw, g.N)) != OCEAN_OK ||
             (rc = encode_inter_map(&g.map, g.inter, g.N, (int)(T * samples))) != OCEAN_OK) {
             cudaFree(d_noise);
+            cudaFree(d_h0);
             delete b;
             return rc;
         }
@@ -191,15 +198,19 @@ int ocean_batch_create(const ocean_params* params, const uint64_t* seeds, int32_
             const int t = g.tiles[j];
             ocean_fill_noise(seeds[t], g.N, noise.data());
             if ((e = cudaMemcpy(d_noise, noise.data(), 4 * NN * sizeof(float), cudaMemcpyHostToDevice)) != cudaSuccess ||
-                (e = ocean::launch_h0(h0_args(params[t]), d_noise, g.h0 + j * NN, 0)) != cudaSuccess ||
+                (e = ocean::launch_h0(h0_args(params[t]), d_noise, d_h0, 0)) != cudaSuccess ||
+                (e = ocean::launch_spec_combine(g.N, 1, d_h0, (params[t].flags & OCEAN_FLAG_LITERAL_CONJ) ? 1 : 0,
+                                                g.spec + j * ocean::spec_len(g.N), 0)) != cudaSuccess ||
                 (e = cudaStreamSynchronize(0)) != cudaSuccess) {
                 cudaFree(d_noise);
+                cudaFree(d_h0);
                 delete b;
                 return cuda_fail(e, "batch h0 init");
             }
         }
     }
     cudaFree(d_noise);
+    cudaFree(d_h0);
     if ((e = cudaStreamCreateWithFlags(&b->cap, cudaStreamNonBlocking)) != cudaSuccess ||
         (e = cudaEventCreateWithFlags(&b->done, cudaEventDisableTiming)) != cudaSuccess) {
         delete b;

@@ -11,55 +11,44 @@ namespace ocean {
 // Phase w*t in double-float arithmetic.
 // w = sqrt(g*|k|), |k| = (2*pi/L)*sqrt(m), m = ix^2 + iz^2 (exact integer), so
 // w*t/(2*pi) = K*t*m^(1/4) with K = sqrt(g/(2*pi*L)).  K*t comes from the host
-// as a double-float; m^(1/4) is formed by two double-float square roots
-// (Dekker 1971: one Newton correction on the FP32 root with an exact FMA
-// residual) and the product by Dekker's two-product via FMA.  The integer
+// as a double-float; m^(1/4) is formed by two double-float square roots, each
+// a hardware reciprocal-square-root estimate refined by one Newton step on the
+// exact FMA residual (Dekker 1971; Karp & Markstein 1997): relative error
+// ~2^-44.  The product with K*t is Dekker's two-product via FMA.  The integer
 // number of cycles is dropped before sincospi, so the reduced phase keeps
-// ~1e-7 absolute accuracy at any t the double can carry.
+// ~1e-7 absolute accuracy while K*t*m^(1/4) stays below ~2^20 cycles.
 // ---------------------------------------------------------------------------
-struct dfl {
-    float hi, lo;
-};
-
-__device__ __forceinline__ dfl df_sqrt_int(float a)  // a >= 1, an exact integer
-{
-    float s = __fsqrt_rn(a);
-    float e = __fmaf_rn(-s, s, a);
-    return {s, __fmul_rn(e, 0.5f * __frcp_rn(s))};
-}
-
-__device__ __forceinline__ dfl df_sqrt(dfl a)
-{
-    float s = __fsqrt_rn(a.hi);
-    float e = __fadd_rn(__fmaf_rn(-s, s, a.hi), a.lo);
-    float c = __fmul_rn(e, 0.5f * __frcp_rn(s));
-    float r = __fadd_rn(s, c);
-    return {r, __fadd_rn(c, -__fadd_rn(r, -s))};
-}
-
-__device__ __forceinline__ dfl df_mul(dfl a, dfl b)
-{
-    float p = __fmul_rn(a.hi, b.hi);
-    float e = __fmaf_rn(a.hi, b.hi, -p);
-    e       = __fmaf_rn(a.hi, b.lo, e);
-    e       = __fmaf_rn(a.lo, b.hi, e);
-    return {p, e};
-}
-
-// cos/sin of the phase of mode m (m = ix^2 + iz^2) at the frame's time.
-__device__ __forceinline__ void mode_phase(int m, const FrameConsts& fc, float& c, float& s)
+// cos/sin of the phase of mode m at the frame's time, and r = 1/sqrt(m)
+// (0 for m = 0) to the accuracy of rsqrtf.
+__device__ __forceinline__ void mode_phase_r(int m, const FrameConsts& fc, float& c, float& s, float& r)
 {
     float f;
     if (m == 0) {
         f = fc.dc_cycles;
+        r = 0.0f;
     } else {
-        dfl q   = df_sqrt(df_sqrt_int((float)m));
-        dfl cyc = df_mul(dfl{fc.kt_hi, fc.kt_lo}, q);
-        float n = rintf(cyc.hi);
-        f       = __fadd_rn(__fadd_rn(cyc.hi, -n), cyc.lo);
-        f       = __fadd_rn(f, -rintf(f));
+        const float mf  = (float)m;                            // exact: m < 2^24
+        const float r1  = rsqrtf(mf);
+        const float s1  = mf * r1;                             // sqrt(m), a few ulp
+        const float s1l = __fmaf_rn(-s1, s1, mf) * (0.5f * r1);
+        const float r2  = rsqrtf(s1);
+        const float q   = s1 * r2;                             // m^(1/4), a few ulp
+        const float ql  = __fadd_rn(__fmaf_rn(-q, q, s1), s1l) * (0.5f * r2);
+        const float p   = __fmul_rn(fc.kt_hi, q);
+        float       e   = __fmaf_rn(fc.kt_hi, q, -p);
+        e               = __fmaf_rn(fc.kt_hi, ql, e);
+        e               = __fmaf_rn(fc.kt_lo, q, e);
+        f               = __fadd_rn(__fadd_rn(p, -rintf(p)), e);
+        f               = __fadd_rn(f, -rintf(f));
+        r               = r1;
     }
     sincospif(2.0f * f, &s, &c);
+}
+
+__device__ __forceinline__ void mode_phase(int m, const FrameConsts& fc, float& c, float& s)
+{
+    float r;
+    mode_phase_r(m, fc, c, s, r);
 }
 
 // h(k,t) = h0(k) e^{iwt} + conj(h0(-k)) e^{-iwt} (tilde_h0_t_cs.glsl:110);

@@ -44,11 +44,20 @@ struct H0Args {
 __host__ __device__ constexpr int inter_pitch(int N) { return N + 2; }
 __host__ __device__ constexpr int inter_rows(int N) { return N / 2 + 1; }
 
+// Combined spectrum read by the row pass, per tile: G[N][N] (G(k) = h0k(k) +
+// sigma(h0m(-k))), then D of column 0 [N], then D of row 0 [N]
+// (D(k) = h0k(k) - sigma(h0m(-k))); sigma = conj, or the identity under
+// OCEAN_FLAG_LITERAL_CONJ.
+__host__ __device__ constexpr size_t spec_len(int N) { return (size_t)N * N + 2 * (size_t)N; }
+
 // A launch covers `tiles` tiles of the same N, each advanced to S time
-// samples: unit u = tile*S + s.  h0 of tile t starts at h0 + t*N*N; the
-// intermediate of unit u at inter + u*3*(N/2+1)*(N+2).  Per-unit constants come
-// from `fcs` (device, [tiles*S]) or, for a single unit, from `fc0`.
+// samples: unit u = tile*S + s.  The spectrum of tile t is spec + t*spec_len(N)
+// or, with spec NULL (single unit only), it is formed on the fly from h0
+// ([N][N] float4 (h0k, h0m)).  The intermediate of unit u starts at
+// inter + u*3*(N/2+1)*(N+2).  Per-unit constants come from `fcs` (device,
+// [tiles*S]) or, for a single unit, from `fc0`.
 struct RowArgs {
+    const float2*      spec;
     const float4*      h0;
     float2*            inter;
     const float2*      tw;      // [N] exp(+2*pi*i*k/N)
@@ -100,6 +109,8 @@ cudaError_t launch_adj_row(int N, const AdjRowArgs& a, cudaStream_t s);
 
 cudaError_t launch_h0(const H0Args& a, const float* noise, float4* h0, cudaStream_t s);
 cudaError_t launch_row_pass(int N, const RowArgs& a, cudaStream_t s);
+// spec[t] from h0[t] for `tiles` consecutive tiles of size N.
+cudaError_t launch_spec_combine(int N, int tiles, const float4* h0, int literal_conj, float2* spec, cudaStream_t s);
 // pdl: launch as a programmatic dependent of the preceding kernel in `s`.
 cudaError_t launch_col_pass(int N, int units, const ColArgs& a, cudaStream_t s, bool pdl);
 // Box of the column-pass tensor map at size N: {inner floats, rows}.

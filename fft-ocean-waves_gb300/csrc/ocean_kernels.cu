@@ -73,7 +73,57 @@ __device__ __forceinline__ float2* align_smem(unsigned char* raw)
 // ---------------------------------------------------------------------------
 // Row pass.
 // ---------------------------------------------------------------------------
-template <int N>
+// The spectrum the row pass reads.  With h(k,t) = h0(k) e^{iwt} +
+// sigma(h0m(k)) e^{-iwt} (tilde_h0_t_cs.glsl:110; sigma = conj, or the
+// identity for the shader's literal conjugate() :42-48) and the index mirror
+// k' = (-k) mod N, the Hermitian line input of Dy is
+//     h(k) + conj h(k') = e^{iwt} G(k) + e^{-iwt} conj G(k'),
+//     G(k) = h0(k) + sigma(h0m(k')),
+// and those of Dx and Dz are -i (kx/|k|) and -i (kz/|k|) times it, except on
+// the Nyquist column (x = 0) for Dx and the Nyquist row (y = 0) for Dz, where
+// k and k' carry the same kx (resp. kz) and the input is -i (k./|k|) times
+//     h(k) - conj h(k') = e^{iwt} D(k) - e^{-iwt} conj D(k'),
+//     D(k) = h0(k) - sigma(h0m(k')).
+// k_spec_combine stores G, then D of column 0, then D of row 0: spec_len(N)
+// complex values per tile.  The row pass then reads 8 bytes per mode instead of
+// h0's 16.
+__global__ void k_spec_combine(int N, const float4* __restrict__ h0, int literal_conj, float2* __restrict__ spec)
+{
+    const size_t NN = (size_t)N * N;
+    const float4* h = h0 + (size_t)blockIdx.y * NN;
+    float2*       o = spec + (size_t)blockIdx.y * spec_len(N);
+    const int     i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= N * N + 2 * N) return;
+    const float sg = literal_conj ? -1.0f : 1.0f;   // sigma(z) = (z.x, sg * z.y)
+    int x, y, sign;
+    size_t at;
+    if (i < N * N) {
+        x = i % N, y = i / N, sign = 1, at = i;
+    } else if (i < N * N + N) {
+        x = 0, y = i - N * N, sign = -1, at = i;
+    } else {
+        x = i - N * N - N, y = 0, sign = -1, at = i;
+    }
+    const int    xm = (N - x) & (N - 1), ym = (N - y) & (N - 1);
+    const float4 a  = h[(size_t)y * N + x];
+    const float4 b  = h[(size_t)ym * N + xm];
+    o[at] = make_float2(a.x + sign * b.z, a.y + sign * sg * b.w);
+}
+
+// e^{iwt} g + e^{-iwt} conj(g2), with e^{iwt} = (c, s)
+__device__ __forceinline__ float2 herm_sum(float2 g, float2 g2, float c, float s)
+{
+    return make_float2(c * (g.x + g2.x) - s * (g.y + g2.y), c * (g.y - g2.y) + s * (g.x - g2.x));
+}
+// e^{iwt} d - e^{-iwt} conj(d2)
+__device__ __forceinline__ float2 herm_diff(float2 d, float2 d2, float c, float s)
+{
+    return make_float2(c * (d.x - d2.x) - s * (d.y - d2.y), c * (d.y + d2.y) + s * (d.x + d2.x));
+}
+// -i * f * z
+__device__ __forceinline__ float2 mul_mi(float f, float2 z) { return make_float2(f * z.y, -f * z.x); }
+
+template <int N, bool FROM_H0>
 struct RowCfg {
     using L = typename LineFor<N>::type;
     static constexpr int PAIRS   = L::G >= 32 ? 1 : 32 / L::G;  // row pairs per work item
@@ -81,24 +131,24 @@ struct RowCfg {
     static constexpr int THREADS = LINES * L::G;
     static constexpr int ITEMS   = (N / 2 + 1 + PAIRS - 1) / PAIRS;  // work items per tile
     static constexpr int STAGES  = 2;
-    // shared memory (float2 units): tw[N] | h0 ring [STAGES][PAIRS][2][N] float4 |
-    // work area = max(hy [PAIRS][2][N], line buffers [LINES][NPAD])
-    static constexpr size_t RING  = (size_t)STAGES * PAIRS * 2 * N * 2;
-    static constexpr size_t HY    = (size_t)PAIRS * 2 * N;
-    static constexpr size_t XB    = (size_t)LINES * L::NPAD;
-    static constexpr size_t WORK  = HY > XB ? HY : XB;
+    static constexpr int EW      = FROM_H0 ? 2 : 1;   // float2 per staged mode (h0: float4, G: float2)
+    // shared memory (float2 units): tw[N] | ring [STAGES][PAIRS][2 rows][N modes] |
+    // line buffers [LINES][NPAD] (line inputs in natural order, then the FFT's exchanges)
+    static constexpr size_t RING  = (size_t)STAGES * PAIRS * 2 * N * EW;
+    static constexpr size_t WORK  = (size_t)LINES * L::NPAD;
     static constexpr size_t SMEM  = sizeof(float2) * (N + RING + WORK) + 128;   // + base alignment slack
-    static constexpr uint32_t ROW_BYTES = N * sizeof(float4);
+    static constexpr uint32_t ROW_BYTES = (uint32_t)(N * EW * sizeof(float2));
 };
 
-// Fetch the h0 rows of work item `item` (tile item/ITEMS, row pairs
+// Fetch the spectrum rows of work item `item` (tile item/ITEMS, row pairs
 // (item%ITEMS)*PAIRS ...) into a ring stage with 1-D bulk copies.
-template <int N>
-__device__ __forceinline__ void row_issue(const RowArgs& a, float4* ring_stage, uint64_t* bar, int item)
+template <int N, bool FROM_H0>
+__device__ __forceinline__ void row_issue(const RowArgs& a, float2* ring_stage, uint64_t* bar, int item)
 {
-    using RC = RowCfg<N>;
-    const int     tile = item / RC::ITEMS, pi = item % RC::ITEMS;
-    const float4* h0t  = a.h0 + (size_t)tile * N * N;
+    using RC = RowCfg<N, FROM_H0>;
+    const int    tile = item / RC::ITEMS, pi = item % RC::ITEMS;
+    const float2* src = FROM_H0 ? reinterpret_cast<const float2*>(a.h0 + (size_t)tile * N * N)
+                                : a.spec + (size_t)tile * spec_len(N);
     uint32_t bytes = 0;
 #pragma unroll
     for (int pl = 0; pl < RC::PAIRS; ++pl)
@@ -109,25 +159,66 @@ __device__ __forceinline__ void row_issue(const RowArgs& a, float4* ring_stage, 
         const int yp = pi * RC::PAIRS + pl;
         if (yp > N / 2) break;
         const int yq = (N - yp) & (N - 1);
-        bulk_g2s(ring_stage + (pl * 2 + 0) * N, h0t + (size_t)yp * N, RC::ROW_BYTES, bar);
-        bulk_g2s(ring_stage + (pl * 2 + 1) * N, h0t + (size_t)yq * N, RC::ROW_BYTES, bar);
+        bulk_g2s(ring_stage + (pl * 2 + 0) * N * RC::EW, src + (size_t)yp * N * RC::EW, RC::ROW_BYTES, bar);
+        bulk_g2s(ring_stage + (pl * 2 + 1) * N * RC::EW, src + (size_t)yq * N * RC::EW, RC::ROW_BYTES, bar);
+    }
+}
+
+// The four combined-spectrum values of one position pair (x, xm = N-x) of row
+// pair (yp, yq = N-yp): g0 = G(x,yp), g1 = G(xm,yq), g2 = G(xm,yp),
+// g3 = G(x,yq), and the D values at the same places where a Nyquist line needs
+// them (d0..d3, valid when x == 0 or yp == 0).
+template <int N, bool FROM_H0>
+__device__ __forceinline__ void row_modes(const RowArgs& a, const float2* rA, const float2* rB, int tile, int x,
+                                          int xm, int yp, int yq, int literal, float2 (&g)[4], float2 (&d)[4])
+{
+    if constexpr (FROM_H0) {
+        // G and D from h0 = (h0k, h0m): G(k) = h0k(k) + sigma h0m(k'), k' the mirror
+        const float4 a0 = reinterpret_cast<const float4*>(rA)[x], a1 = reinterpret_cast<const float4*>(rA)[xm];
+        const float4 b0 = reinterpret_cast<const float4*>(rB)[xm], b1 = reinterpret_cast<const float4*>(rB)[x];
+        const float  sg = literal ? -1.0f : 1.0f;
+        g[0] = make_float2(a0.x + b0.z, a0.y + sg * b0.w);
+        g[1] = make_float2(b0.x + a0.z, b0.y + sg * a0.w);
+        g[2] = make_float2(a1.x + b1.z, a1.y + sg * b1.w);
+        g[3] = make_float2(b1.x + a1.z, b1.y + sg * a1.w);
+        d[0] = make_float2(a0.x - b0.z, a0.y - sg * b0.w);
+        d[1] = make_float2(b0.x - a0.z, b0.y - sg * a0.w);
+        d[2] = make_float2(a1.x - b1.z, a1.y - sg * b1.w);
+        d[3] = make_float2(b1.x - a1.z, b1.y - sg * a1.w);
+    } else {
+        g[0] = rA[x];
+        g[1] = rB[xm];
+        g[2] = rA[xm];
+        g[3] = rB[x];
+        const float2* sp = a.spec + (size_t)tile * spec_len(N);
+        if (x == 0) {                                   // column 0: D(0, yp), D(0, yq)
+            d[0] = __ldg(sp + (size_t)N * N + yp);
+            d[1] = __ldg(sp + (size_t)N * N + yq);
+        }
+        if (yp == 0) {                                  // row 0: D(x, 0), D(xm, 0)
+            d[0] = __ldg(sp + (size_t)N * N + N + x);
+            d[1] = __ldg(sp + (size_t)N * N + N + xm);
+            d[2] = d[1];
+            d[3] = d[0];
+        }
     }
 }
 
 // MULTI: more than one (tile, sample) unit per launch (batches).  The single
-// unit instantiation keeps the per-element choppy factors out of a runtime
-// sample loop, which the compiler would otherwise hoist into registers.
-template <int N, bool MULTI>
-__global__ void __launch_bounds__(RowCfg<N>::THREADS) k_row_pass(RowArgs a)
+// unit instantiation keeps the per-element constants out of a runtime sample
+// loop, which the compiler would otherwise hoist into registers.  FROM_H0: the
+// ring holds h0 rows and G, D are formed on the fly (ocean_update_noalloc).
+template <int N, bool MULTI, bool FROM_H0>
+__global__ void __launch_bounds__(RowCfg<N, FROM_H0>::THREADS) k_row_pass(RowArgs a)
 {
-    using RC = RowCfg<N>;
+    using RC = RowCfg<N, FROM_H0>;
     using L  = typename RC::L;
     constexpr int NP = inter_pitch(N), H = inter_rows(N);
     extern __shared__ unsigned char smem_raw[];
     float2* smem = align_smem(smem_raw);
     float2* tw_s = smem;
-    float4* ring = reinterpret_cast<float4*>(smem + N);              // [STAGES][PAIRS][2][N]
-    float2* work = smem + N + RC::RING;                              // hy, then line buffers
+    float2* ring = smem + N;                                         // [STAGES][PAIRS][2][N*EW]
+    float2* work = smem + N + RC::RING;                              // line buffers
     __shared__ __align__(8) uint64_t bars[RC::STAGES];
     __shared__ int wait_ok;
 
@@ -142,7 +233,7 @@ __global__ void __launch_bounds__(RowCfg<N>::THREADS) k_row_pass(RowArgs a)
     if (tid == 0)
         for (int s = 0; s < RC::STAGES; ++s) {
             const int item = blockIdx.x + s * gridDim.x;
-            if (item < n_items) row_issue<N>(a, ring + (size_t)s * RC::PAIRS * 2 * N, &bars[s], item);
+            if (item < n_items) row_issue<N, FROM_H0>(a, ring + (size_t)s * RC::PAIRS * 2 * N * RC::EW, &bars[s], item);
         }
     // The column pass may start its set-up now; it waits for this grid to finish
     // before it reads the intermediate.
@@ -155,7 +246,7 @@ __global__ void __launch_bounds__(RowCfg<N>::THREADS) k_row_pass(RowArgs a)
 
     for (int k = 0, item = blockIdx.x; item < n_items; ++k, item += gridDim.x) {
         const int s = k & 1;
-        float4* stage = ring + (size_t)s * RC::PAIRS * 2 * N;
+        float2* stage = ring + (size_t)s * RC::PAIRS * 2 * N * RC::EW;
         if (!block_wait(&bars[s], (phase_bits >> s) & 1u, &wait_ok, a.status)) return;
         phase_bits ^= 1u << s;
         const int tile = item / RC::ITEMS, pi = item % RC::ITEMS;
@@ -165,64 +256,60 @@ __global__ void __launch_bounds__(RowCfg<N>::THREADS) k_row_pass(RowArgs a)
         for (int smp = 0; smp < nsmp; ++smp) {
             const int         unit = MULTI ? tile * a.S + smp : 0;
             const FrameConsts fc   = MULTI ? a.fcs[unit] : a.fc0;
-            // Prepass: h(k,t) for the pair's two rows.  hy[pl][0][x] is the mode
-            // (x, y'), hy[pl][1][x] the mode (N-x, N-y').  The four modes (x, y'),
-            // (N-x, y'), (N-x, N-y'), (x, N-y') share |k| (ix^2 and iz^2 are
-            // even) and so the phase, which is computed once for all four.
-            float2* hy = work;
+            // Line inputs of the pair's row yp for the three fields, position
+            // pairs (x, N-x): the modes (x, yp), (N-x, yp), (N-x, N-yp), (x, N-yp)
+            // share |k| (ix^2 and iz^2 are even) and so the phase.
             constexpr int HX = N / 2 + 1;
             for (int i = tid; i < RC::PAIRS * HX; i += RC::THREADS) {
-                const int pl = i / HX, x = i % HX;
+                const int pl = i / HX, x = i - pl * HX;
                 const int yp = pi * RC::PAIRS + pl;
                 if (yp > N / 2) continue;
-                const int xm = (N - x) & (N - 1);
+                const int yq = (N - yp) & (N - 1), xm = (N - x) & (N - 1);
                 const int ix = x - N / 2, iz = yp - N / 2;
-                float c, sn;
-                mode_phase(ix * ix + iz * iz, fc, c, sn);
-                const float4* r0  = stage + (pl * 2 + 0) * N;
-                const float4* r1  = stage + (pl * 2 + 1) * N;
-                float2*       h0r = hy + (pl * 2 + 0) * N;
-                float2*       h1r = hy + (pl * 2 + 1) * N;
-                h0r[x] = evolve(r0[x], c, sn, fc.literal_conj);
-                h1r[x] = evolve(r1[xm], c, sn, fc.literal_conj);
-                if (xm != x) {
-                    h0r[xm] = evolve(r0[xm], c, sn, fc.literal_conj);
-                    h1r[xm] = evolve(r1[x], c, sn, fc.literal_conj);
+                float c, sn, r;
+                mode_phase_r(ix * ix + iz * iz, fc, c, sn, r);
+                float2 g[4], d[4];
+                const float2* rA = stage + (pl * 2 + 0) * N * RC::EW;
+                const float2* rB = stage + (pl * 2 + 1) * N * RC::EW;
+                row_modes<N, FROM_H0>(a, rA, rB, tile, x, xm, yp, yq, fc.literal_conj, g, d);
+                const float2 y0 = herm_sum(g[0], g[1], c, sn);
+                const float2 y1 = herm_sum(g[2], g[3], c, sn);
+                float2 ux0 = y0, uz0 = y0, uz1 = y1;
+                if (x == 0) ux0 = herm_diff(d[0], d[1], c, sn);
+                if (yp == 0) {
+                    uz0 = herm_diff(d[0], d[1], c, sn);
+                    uz1 = herm_diff(d[2], d[3], c, sn);
+                }
+                const float sx = (float)ix * r, sz = (float)iz * r;
+                float2* bx = work + (pl * 3 + 0) * L::NPAD;
+                float2* by = bx + L::NPAD;
+                float2* bz = by + L::NPAD;
+                bx[x] = mul_mi(sx, ux0);
+                by[x] = y0;
+                bz[x] = mul_mi(sz, uz0);
+                if (xm != x) {                        // ix(xm) = -ix for x != 0
+                    bx[xm] = mul_mi(-sx, y1);
+                    by[xm] = y1;
+                    bz[xm] = mul_mi(sz, uz1);
                 }
             }
-            __syncthreads();                               // hy complete
+            __syncthreads();                               // line inputs complete
             if (smp == nsmp - 1 && tid == 0) {             // ring stage consumed: refill it
                 const int next = item + RC::STAGES * gridDim.x;
                 if (next < n_items) {
                     fence_proxy_async_smem();
-                    row_issue<N>(a, stage, &bars[s], next);
+                    row_issue<N, FROM_H0>(a, stage, &bars[s], next);
                 }
             }
 
-            // Gather the line inputs: 2 * X_H,f(x) = X_f(x) + conj X_f(-x).
             const int  yp     = pi * RC::PAIRS + pl_line;
             const bool active = yp <= N / 2;
-            const int  iz = yp - N / 2, izq = ((N - yp) & (N - 1)) - N / 2;
-            float2 v[L::E];
+            float2*    buf    = work + li * L::NPAD;
+            float2     v[L::E];
 #pragma unroll
-            for (int r = 0; r < L::E; ++r) {
-                const int x = t + r * (N / L::R1);
-                float2 hk = active ? hy[(pl_line * 2 + 0) * N + x] : make_float2(0.f, 0.f);
-                float2 hq = active ? hy[(pl_line * 2 + 1) * N + x] : make_float2(0.f, 0.f);
-                if (f != 1) {
-                    // -i (k/|k|) h (tilde_h0_t_cs.glsl:113-126); the DC mode gets 0
-                    const int   ix  = x - N / 2;
-                    const int   m   = ix * ix + iz * iz;
-                    const float rs  = m ? __frsqrt_rn((float)m) : 0.0f;
-                    const float fk  = -(float)(f == 0 ? ix : iz) * rs;
-                    const float fkq = -(float)(f == 0 ? (((N - x) & (N - 1)) - N / 2) : izq) * rs;
-                    hk = make_float2(-fk * hk.y, fk * hk.x);
-                    hq = make_float2(-fkq * hq.y, fkq * hq.x);
-                }
-                v[r] = make_float2(hk.x + hq.x, hk.y - hq.y);
-            }
-            __syncthreads();                               // hy is read; the line buffers reuse it
-            line_fft<L, +1>(v, work + li * L::NPAD, tw_s, t, li);
+            for (int r = 0; r < L::E; ++r) v[r] = buf[t + r * L::G];
+            line_sync<L, true>(li);                        // the line's inputs are in registers
+            line_fft<L, +1>(v, buf, tw_s, t, li);
             if (active) {
                 float2* out = a.inter + (((size_t)unit * 3 + f) * H + yp) * NP;
 #pragma unroll
@@ -233,8 +320,8 @@ __global__ void __launch_bounds__(RowCfg<N>::THREADS) k_row_pass(RowArgs a)
                 if (t == 0) out[N + 1] = v[0];
                 if (t == L::G - 1) out[0] = v[L::E - 1];
             }
-            // the next prepass overwrites `work`: every line has finished
-            // reading its buffer
+            // the next inputs overwrite the line buffers: every line has
+            // finished reading its own
             __syncthreads();
         }
     }
@@ -459,18 +546,25 @@ cudaError_t launch_h0(const H0Args& a, const float* noise, float4* h0, cudaStrea
     return cudaGetLastError();
 }
 
-template <int N, bool MULTI>
+cudaError_t launch_spec_combine(int N, int tiles, const float4* h0, int literal_conj, float2* spec, cudaStream_t s)
+{
+    const int n = N * N + 2 * N;
+    k_spec_combine<<<dim3((n + 255) / 256, tiles), 256, 0, s>>>(N, h0, literal_conj, spec);
+    return cudaGetLastError();
+}
+
+template <int N, bool MULTI, bool FROM_H0>
 static cudaError_t row_pass_nm(const RowArgs& a, cudaStream_t s)
 {
-    using RC = RowCfg<N>;
+    using RC = RowCfg<N, FROM_H0>;
     static int grid = 0;   // persistent grid: resident CTAs per SM x SMs
     if (!grid) {
-        cudaError_t e =
-            cudaFuncSetAttribute(k_row_pass<N, MULTI>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)RC::SMEM);
+        cudaError_t e = cudaFuncSetAttribute(k_row_pass<N, MULTI, FROM_H0>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)RC::SMEM);
         if (e != cudaSuccess) return e;
         int per_sm = 0, dev = 0, sms = 0;
-        if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_row_pass<N, MULTI>, RC::THREADS, RC::SMEM)) !=
-            cudaSuccess)
+        if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_row_pass<N, MULTI, FROM_H0>, RC::THREADS,
+                                                                RC::SMEM)) != cudaSuccess)
             return e;
         if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
         if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
@@ -478,14 +572,19 @@ static cudaError_t row_pass_nm(const RowArgs& a, cudaStream_t s)
         grid = per_sm * sms;
     }
     const int items = a.tiles * RC::ITEMS;
-    k_row_pass<N, MULTI><<<grid < items ? grid : items, RC::THREADS, RC::SMEM, s>>>(a);
+    k_row_pass<N, MULTI, FROM_H0><<<grid < items ? grid : items, RC::THREADS, RC::SMEM, s>>>(a);
     return cudaGetLastError();
 }
 
 template <int N>
 static cudaError_t row_pass_n(const RowArgs& a, cudaStream_t s)
 {
-    return (a.tiles == 1 && a.S == 1 && !a.fcs) ? row_pass_nm<N, false>(a, s) : row_pass_nm<N, true>(a, s);
+    if (!a.spec) {   // h0 input: single unit only
+        if (a.tiles != 1 || a.S != 1 || a.fcs) return cudaErrorInvalidValue;
+        return row_pass_nm<N, false, true>(a, s);
+    }
+    return (a.tiles == 1 && a.S == 1 && !a.fcs) ? row_pass_nm<N, false, false>(a, s)
+                                                : row_pass_nm<N, true, false>(a, s);
 }
 
 template <int N>
@@ -554,7 +653,7 @@ void col_pass_box(int N, unsigned box[2])
 size_t row_pass_smem(int N)
 {
     switch (N) {
-#define CASE(n) case n: return RowCfg<n>::SMEM;
+#define CASE(n) case n: return RowCfg<n, true>::SMEM;
         OCEAN_FOR_EACH_N(CASE)
 #undef CASE
     default: return 0;

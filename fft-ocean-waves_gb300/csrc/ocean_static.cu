@@ -123,6 +123,7 @@ extern "C" int ocean_update_noalloc(const ocean_params* params, const float* h0_
     const double K  = std::sqrt(g / (2.0 * M_PI * (double)params->L));
     const double kt = K * t;
     ocean::RowArgs ra;
+    ra.spec            = nullptr;            // G and D formed from h0 on the fly
     ra.h0              = reinterpret_cast<const float4*>(h0_dev);
     ra.inter           = d.inter;
     ra.tw              = d.tw;
