@@ -37,23 +37,48 @@ __device__ __forceinline__ float2 cmul(float2 a, float2 b)
 }
 __device__ __forceinline__ float2 conjf2(float2 a) { return make_float2(a.x, -a.y); }
 
-// cos(2*pi*k/32) and sin(2*pi*k/32) for k < 16, rounded to float.
-__host__ __device__ constexpr float cos32(int k)
+// cos(2*pi*k/32) and sin(2*pi*k/32), rounded to float.  Plain switches (no
+// recursion) so that, with k a constant after unrolling, they fold to
+// immediates instead of becoming called functions.
+__host__ __device__ __forceinline__ constexpr float cos32(int k)
 {
-    switch (k) {
+    switch (k & 31) {
     case 0: return 1.0f;
-    case 1: return 0.980785280403230449f;
-    case 2: return 0.923879532511286756f;
-    case 3: return 0.831469612302545237f;
-    case 4: return 0.707106781186547524f;
-    case 5: return 0.555570233019602225f;
-    case 6: return 0.382683432365089772f;
-    case 7: return 0.195090322016128268f;
+    case 1: return 0.980785251f;
+    case 2: return 0.923879504f;
+    case 3: return 0.831469595f;
+    case 4: return 0.707106769f;
+    case 5: return 0.555570245f;
+    case 6: return 0.382683426f;
+    case 7: return 0.195090324f;
     case 8: return 0.0f;
-    default: return -cos32(16 - k);
+    case 9: return -0.195090324f;
+    case 10: return -0.382683426f;
+    case 11: return -0.555570245f;
+    case 12: return -0.707106769f;
+    case 13: return -0.831469595f;
+    case 14: return -0.923879504f;
+    case 15: return -0.980785251f;
+    case 16: return -1.0f;
+    case 17: return -0.980785251f;
+    case 18: return -0.923879504f;
+    case 19: return -0.831469595f;
+    case 20: return -0.707106769f;
+    case 21: return -0.555570245f;
+    case 22: return -0.382683426f;
+    case 23: return -0.195090324f;
+    case 24: return 0.0f;
+    case 25: return 0.195090324f;
+    case 26: return 0.382683426f;
+    case 27: return 0.555570245f;
+    case 28: return 0.707106769f;
+    case 29: return 0.831469595f;
+    case 30: return 0.923879504f;
+    case 31: return 0.980785251f;
+    default: return 0.0f;
     }
 }
-__host__ __device__ constexpr float sin32(int k) { return k <= 8 ? cos32(8 - k) : cos32(k - 8); }
+__host__ __device__ __forceinline__ constexpr float sin32(int k) { return cos32((k + 24) & 31); }
 
 // x * W_32^idx with W = exp(SIGN * 2*pi*i/32); idx is a compile-time constant
 // after unrolling, so the branches fold away.
