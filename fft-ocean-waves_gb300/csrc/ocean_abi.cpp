@@ -59,19 +59,6 @@ int validate(const ocean_params* p)
 }
 
 // cuTensorMapEncodeTiled through the runtime's driver entry point (no -lcuda).
-PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder()
-{
-    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
-    if (!fn) {
-        void*                           p = nullptr;
-        cudaDriverEntryPointQueryResult q;
-        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
-                cudaSuccess &&
-            q == cudaDriverEntryPointSuccess)
-            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
-    }
-    return fn;
-}
 
 double gravity_of(const ocean_params& p) { return p.gravity > 0.0f ? (double)p.gravity : 9.81; }
 
@@ -122,24 +109,6 @@ int upload_twiddles(float2** d, int N)
     return OCEAN_OK;
 }
 
-int encode_inter_map(CUtensorMap* map, float2* inter, int N, int units)
-{
-    PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
-    if (!enc) return fail(OCEAN_ERR_UNSUPPORTED, "cuTensorMapEncodeTiled is not available from the driver");
-    const cuuint64_t H = (cuuint64_t)inter_rows(N), NP = (cuuint64_t)inter_pitch(N);
-    unsigned box[2];
-    col_pass_box(N, box);
-    // the intermediates as floats [units*3*H rows][2*NP]
-    cuuint64_t dims[2]    = {2 * NP, (cuuint64_t)units * 3 * H};
-    cuuint64_t strides[1] = {2 * NP * sizeof(float)};
-    cuuint32_t boxd[2]    = {box[0], box[1]};
-    cuuint32_t estr[2]    = {1, 1};
-    CUresult   r = enc(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, inter, dims, strides, boxd, estr,
-                       CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                       CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-    if (r != CUDA_SUCCESS) return fail(OCEAN_ERR_CUDA, "cuTensorMapEncodeTiled failed: " + std::to_string((int)r));
-    return OCEAN_OK;
-}
 
 }  // namespace host
 }  // namespace ocean
@@ -160,16 +129,16 @@ struct ocean_s {
     int          N = 0;
     float4*      h0     = nullptr;  // [N][N]
     float2*      spec   = nullptr;  // combined spectrum read by the row pass [spec_len(N)]
-    float2*      inter  = nullptr;  // [3][N/2+1][N+2] (periodic pad column each side)
+    float2*      inter  = nullptr;  // [3][N/2+1][N]: row-pass output
+    float*       tmap   = nullptr;  // [3][N][N]: column-transform output, column-major
     unsigned*    status = nullptr;  // device status word (bounded-wait time-outs)
-    CUtensorMap  inter_map;         // column-pass view of inter
     float2*      tw     = nullptr;  // [N]
     float*       noise  = nullptr;  // [4][N][N], kept for ocean_set_params
     float*       out    = nullptr;  // handle-owned outputs: dx, dy, dz, normal_j
     float2*      adj    = nullptr;  // adjoint scratch: [frames][3][N/2+1][N]
     int          adj_frames = 0;
     double*      sums   = nullptr;  // adjoint parameter sums (4 doubles)
-    bool         pdl_next = false;  // the next column pass directly follows this handle's row pass
+    bool         pdl_next = false;  // set inside ocean_update: each stage directly follows the previous one
     double       K      = 0.0;      // sqrt(g/(2*pi*L))
     double       w_dc   = 0.0;      // sqrt(g*1e-5): the floored DC frequency
 
@@ -178,6 +147,7 @@ struct ocean_s {
         cudaFree(h0);
         cudaFree(spec);
         cudaFree(inter);
+        cudaFree(tmap);
         cudaFree(status);
         cudaFree(tw);
         cudaFree(noise);
@@ -323,10 +293,10 @@ int ocean_create(const ocean_params* params, const float* noise_host, ocean_t** 
     o->N = params->N;
     o->set_consts();
     const size_t N = (size_t)o->N;
-    const size_t H = (size_t)ocean::inter_rows(o->N), NP = (size_t)ocean::inter_pitch(o->N);
     if ((e = cudaMalloc(&o->h0, N * N * sizeof(float4))) != cudaSuccess ||
         (e = cudaMalloc(&o->spec, ocean::spec_len(o->N) * sizeof(float2))) != cudaSuccess ||
-        (e = cudaMalloc(&o->inter, 3 * H * NP * sizeof(float2))) != cudaSuccess ||
+        (e = cudaMalloc(&o->inter, ocean::inter_len(o->N) * sizeof(float2))) != cudaSuccess ||
+        (e = cudaMalloc(&o->tmap, ocean::tmap_len(o->N) * sizeof(float))) != cudaSuccess ||
         (e = cudaMalloc(&o->status, sizeof(unsigned))) != cudaSuccess ||
         (e = cudaMalloc(&o->noise, 4 * N * N * sizeof(float))) != cudaSuccess) {
         delete o;
@@ -335,10 +305,6 @@ int ocean_create(const ocean_params* params, const float* noise_host, ocean_t** 
     if ((e = cudaMemset(o->status, 0, sizeof(unsigned))) != cudaSuccess) {
         delete o;
         return cuda_fail(e, "status clear");
-    }
-    if ((rc = encode_inter_map(&o->inter_map, o->inter, o->N, 1)) != OCEAN_OK) {
-        delete o;
-        return rc;
     }
     if ((rc = upload_twiddles(&o->tw, o->N)) != OCEAN_OK) {
         delete o;
@@ -449,28 +415,51 @@ int ocean_update_rows(ocean_t* o, double t, void* stream)
     return OCEAN_OK;
 }
 
-int ocean_update_columns(ocean_t* o, const ocean_outputs* out, void* stream)
+static ocean::ColArgs col_args(const ocean_s* o, const ocean_outputs& out)
+{
+    ocean::ColArgs ca;
+    ca.inter  = o->inter;
+    ca.tmap   = o->tmap;
+    ca.status = o->status;
+    ca.tw     = o->tw;
+    ca.units  = nullptr;
+    ca.u0     = o->col_unit(out);
+    return ca;
+}
+
+// out == NULL: the handle-owned buffers; checks pointers and alignment.
+static int resolve_outputs(ocean_t* o, const ocean_outputs* out, ocean_outputs* res)
+{
+    if (!out) {
+        int rc = ocean_get_outputs(o, res);
+        if (rc) return rc;
+    } else {
+        *res = *out;
+    }
+    if (!res->dx || !res->dy || !res->dz || !res->normal_j) return fail(OCEAN_ERR_INVALID, "NULL output pointer");
+    const uintptr_t al = reinterpret_cast<uintptr_t>(res->dx) | reinterpret_cast<uintptr_t>(res->dy) |
+                         reinterpret_cast<uintptr_t>(res->dz) | reinterpret_cast<uintptr_t>(res->normal_j);
+    if (al % 16) return fail(OCEAN_ERR_INVALID, "output pointers must be 16-byte aligned");
+    return OCEAN_OK;
+}
+
+int ocean_update_columns(ocean_t* o, void* stream)
 {
     if (!o) return fail(OCEAN_ERR_INVALID, "ocean is NULL");
-    ocean_outputs own;
-    if (!out) {
-        int rc = ocean_get_outputs(o, &own);
-        if (rc) return rc;
-        out = &own;
-    }
-    if (!out->dx || !out->dy || !out->dz || !out->normal_j) return fail(OCEAN_ERR_INVALID, "NULL output pointer");
-    const uintptr_t al = reinterpret_cast<uintptr_t>(out->dx) | reinterpret_cast<uintptr_t>(out->dy) |
-                         reinterpret_cast<uintptr_t>(out->dz) | reinterpret_cast<uintptr_t>(out->normal_j);
-    if (al % 16) return fail(OCEAN_ERR_INVALID, "output pointers must be 16-byte aligned");
-    ocean::ColArgs ca;
-    ca.map        = o->inter_map;
-    ca.status     = o->status;
-    ca.tw         = o->tw;
-    ca.units      = nullptr;
-    ca.u0         = o->col_unit(*out);
-    cudaError_t e = ocean::launch_col_pass(o->N, 1, ca, static_cast<cudaStream_t>(stream), o->pdl_next);
-    o->pdl_next   = false;
-    if (e != cudaSuccess) return cuda_fail(e, "column pass launch");
+    const ocean_outputs none{};
+    cudaError_t e = ocean::launch_col_fft(o->N, 1, col_args(o, none), static_cast<cudaStream_t>(stream), o->pdl_next);
+    if (e != cudaSuccess) return cuda_fail(e, "column transform launch");
+    return OCEAN_OK;
+}
+
+int ocean_update_outputs(ocean_t* o, const ocean_outputs* out, void* stream)
+{
+    if (!o) return fail(OCEAN_ERR_INVALID, "ocean is NULL");
+    ocean_outputs res;
+    int rc = resolve_outputs(o, out, &res);
+    if (rc) return rc;
+    cudaError_t e = ocean::launch_col_out(o->N, 1, col_args(o, res), static_cast<cudaStream_t>(stream), o->pdl_next);
+    if (e != cudaSuccess) return cuda_fail(e, "output launch");
     return OCEAN_OK;
 }
 
@@ -478,17 +467,17 @@ int ocean_update(ocean_t* o, double t, const ocean_outputs* out, void* stream)
 {
     if (!o) return fail(OCEAN_ERR_INVALID, "ocean is NULL");
     if (!std::isfinite(t)) return fail(OCEAN_ERR_INVALID, "time is not finite");
-    ocean_outputs own;
-    if (!out) {
-        int rc = ocean_get_outputs(o, &own);
-        if (rc) return rc;
-        out = &own;
-    }
-    if (!out->dx || !out->dy || !out->dz || !out->normal_j) return fail(OCEAN_ERR_INVALID, "NULL output pointer");
-    int rc = ocean_update_rows(o, t, stream);
+    ocean_outputs res;
+    int rc = resolve_outputs(o, out, &res);
     if (rc) return rc;
-    o->pdl_next = true;   // columns follow rows on the same stream: overlap their set-up
-    return ocean_update_columns(o, out, stream);
+    if ((rc = ocean_update_rows(o, t, stream)) != OCEAN_OK) return rc;
+    // each stage follows the previous one on the same stream: launched as
+    // programmatic dependents, their set-up overlaps the previous stage's tail
+    o->pdl_next = true;
+    rc = ocean_update_columns(o, stream);
+    if (rc == OCEAN_OK) rc = ocean_update_outputs(o, &res, stream);
+    o->pdl_next = false;
+    return rc;
 }
 
 int ocean_device_status(ocean_t* o, void* stream)

@@ -3,12 +3,13 @@
 //
 // Tiles are grouped by N.  Per group: the combined spectrum (G, D) of every
 // tile back to back (h0 itself is only a creation-time temporary), one
-// intermediate per (tile, time sample) back to back, one tensor map over all
-// of them, and one twiddle table.  An update is a CUDA graph of
+// intermediate and one set of column-major maps per (tile, time sample) back
+// to back, and one twiddle table.  An update is a CUDA graph of
 //   H2D copy of the per-unit constants (pinned staging -> device)
 //   per group: k_row_pass (persistent; each spectrum row pair is staged once and
-//              serves all samples of its tile) -> k_col_pass (grid: column
-//              tiles x units, programmatic dependent of the row pass)
+//              serves all samples of its tile) -> k_col_fft -> k_col_out
+//              (grids: column pairs / output tiles x units, each a
+//              programmatic dependent of the kernel before it)
 // captured at creation and replayed by ocean_batch_update.
 #include <cuda_runtime.h>
 
@@ -29,8 +30,8 @@ struct ocean_batch_s {
         std::vector<int> tiles;          // batch tile indices, in slot order
         float2*          spec  = nullptr;
         float2*          inter = nullptr;
+        float*           tmap  = nullptr;
         float2*          tw    = nullptr;
-        CUtensorMap      map;
         size_t           first_unit = 0; // this group's units start here in the unit arrays
     };
     int                       n_tiles = 0, S = 0;
@@ -58,6 +59,7 @@ struct ocean_batch_s {
         for (Group& g : groups) {
             cudaFree(g.spec);
             cudaFree(g.inter);
+            cudaFree(g.tmap);
             cudaFree(g.tw);
         }
         cudaFree(status);
@@ -99,12 +101,15 @@ int capture(ocean_batch_s* b)
         ra.S      = b->S;
         if ((e = ocean::launch_row_pass(g.N, ra, b->cap)) != cudaSuccess) break;
         ocean::ColArgs ca;
-        ca.map    = g.map;
+        ca.inter  = g.inter;
+        ca.tmap   = g.tmap;
         ca.status = b->status;
         ca.tw     = g.tw;
         ca.units  = b->d_units() + g.first_unit;
         ca.u0     = ocean::ColUnit{};
-        e = ocean::launch_col_pass(g.N, (int)g.tiles.size() * b->S, ca, b->cap, true);
+        const int units = (int)g.tiles.size() * b->S;
+        if ((e = ocean::launch_col_fft(g.N, units, ca, b->cap, true)) != cudaSuccess) break;
+        e = ocean::launch_col_out(g.N, units, ca, b->cap, true);
     }
     cudaGraph_t graph = nullptr;
     cudaError_t e2    = cudaStreamEndCapture(b->cap, &graph);
@@ -178,16 +183,15 @@ int ocean_batch_create(const ocean_params* params, const uint64_t* seeds, int32_
     }
     for (ocean_batch_s::Group& g : b->groups) {
         const size_t N = (size_t)g.N, NN = N * N, T = g.tiles.size();
-        const size_t H = (size_t)ocean::inter_rows(g.N), NP = (size_t)ocean::inter_pitch(g.N);
         if ((e = cudaMalloc(&g.spec, T * ocean::spec_len(g.N) * sizeof(float2))) != cudaSuccess ||
-            (e = cudaMalloc(&g.inter, T * samples * 3 * H * NP * sizeof(float2))) != cudaSuccess) {
+            (e = cudaMalloc(&g.inter, T * samples * ocean::inter_len(g.N) * sizeof(float2))) != cudaSuccess ||
+            (e = cudaMalloc(&g.tmap, T * samples * ocean::tmap_len(g.N) * sizeof(float))) != cudaSuccess) {
             cudaFree(d_noise);
             cudaFree(d_h0);
             delete b;
             return fail(OCEAN_ERR_NOMEM, std::string("batch allocation failed: ") + cudaGetErrorString(e));
         }
-        if ((rc = upload_twiddles(&g.tw, g.N)) != OCEAN_OK ||
-            (rc = encode_inter_map(&g.map, g.inter, g.N, (int)(T * samples))) != OCEAN_OK) {
+        if ((rc = upload_twiddles(&g.tw, g.N)) != OCEAN_OK) {
             cudaFree(d_noise);
             cudaFree(d_h0);
             delete b;

@@ -2,7 +2,6 @@
 // (single tiles in ocean_abi.cpp, batches in ocean_batch.cpp).
 #pragma once
 #include <cuda.h>
-#include <cudaTypedefs.h>
 #include <cuda_runtime.h>
 
 #include <string>
@@ -19,14 +18,10 @@ bool   is_pow2(int n);
 int    validate(const ocean_params* p);                     // OCEAN_OK or OCEAN_ERR_INVALID
 double gravity_of(const ocean_params& p);
 H0Args h0_args(const ocean_params& p);
-PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder();      // NULL if the driver lacks it
 uint64_t splitmix64_at(uint64_t seed, uint64_t i);
 
 int check_device();                                         // sm_103 or OCEAN_ERR_UNSUPPORTED
 int upload_twiddles(float2** d, int N);                     // cudaMalloc + fill exp(+2 pi i k/N)
-
-// Column-pass tensor map over `units` intermediates of size N stored back to back.
-int encode_inter_map(CUtensorMap* map, float2* inter, int N, int units);
 
 }  // namespace host
 }  // namespace ocean

@@ -37,12 +37,19 @@ struct H0Args {
 };
 
 // Row-pass output ("intermediate"): three fields (Dx, Dy, Dz) of rows
-// y' = 0..N/2 of the row-transformed Hermitian spectra.  Each row holds N+2
-// complex values: padded column p = x + 1 for x = -1..N, with x = -1 and x = N
-// the periodic copies of x = N-1 and x = 0, so that any column tile together
-// with its two neighbour columns is one contiguous 16-byte-aligned box.
-__host__ __device__ constexpr int inter_pitch(int N) { return N + 2; }
+// y' = 0..N/2 of the row-transformed Hermitian spectra, blocked by column pair
+// so that the column transforms of a pair read one contiguous run:
+// [3 fields][N/2 column pairs][N/2+1 rows][2 columns] complex.
 __host__ __device__ constexpr int inter_rows(int N) { return N / 2 + 1; }
+__host__ __device__ constexpr size_t inter_len(int N) { return 3 * (size_t)inter_rows(N) * N; }
+__host__ __device__ constexpr size_t inter_index(int N, int f, int x, int y)
+{
+    return (((size_t)f * (N / 2) + (x >> 1)) * inter_rows(N) + y) * 2 + (x & 1);
+}
+// Column-FFT output ("transposed maps"): the final Dx, Dy, Dz of one unit,
+// [3][N (x)][N (y)] floats, column-major so that each column transform writes
+// one contiguous run; the output kernel transposes them.
+__host__ __device__ constexpr size_t tmap_len(int N) { return 3 * (size_t)N * N; }
 
 // Combined spectrum read by the row pass, per tile: G[N][N] (G(k) = h0k(k) +
 // sigma(h0m(-k))), then D of column 0 [N], then D of row 0 [N]
@@ -54,7 +61,7 @@ __host__ __device__ constexpr size_t spec_len(int N) { return (size_t)N * N + 2 
 // samples: unit u = tile*S + s.  The spectrum of tile t is spec + t*spec_len(N)
 // or, with spec NULL (single unit only), it is formed on the fly from h0
 // ([N][N] float4 (h0k, h0m)).  The intermediate of unit u starts at
-// inter + u*3*(N/2+1)*(N+2).  Per-unit constants come from `fcs` (device,
+// inter + u*inter_len(N).  Per-unit constants come from `fcs` (device,
 // [tiles*S]) or, for a single unit, from `fc0`.
 struct RowArgs {
     const float2*      spec;
@@ -67,8 +74,13 @@ struct RowArgs {
     int                tiles, S;
 };
 
+// Column side of a frame: k_col_fft (column transforms, intermediate ->
+// transposed maps) then k_col_out (transpose, Sobel normal, Jacobian ->
+// caller's outputs).  Unit u reads inter + u*inter_len(N) and uses
+// tmap + u*tmap_len(N).
 struct ColArgs {
-    CUtensorMap    map;     // 2-D tensor map over inter: floats [units*3*(N/2+1)][2*(N+2)]
+    const float2*  inter;
+    float*         tmap;
     unsigned*      status;
     const float2*  tw;
     const ColUnit* units;   // device [units], or NULL: u0 for the single unit
@@ -111,12 +123,9 @@ cudaError_t launch_h0(const H0Args& a, const float* noise, float4* h0, cudaStrea
 cudaError_t launch_row_pass(int N, const RowArgs& a, cudaStream_t s);
 // spec[t] from h0[t] for `tiles` consecutive tiles of size N.
 cudaError_t launch_spec_combine(int N, int tiles, const float4* h0, int literal_conj, float2* spec, cudaStream_t s);
-// pdl: launch as a programmatic dependent of the preceding kernel in `s`.
-cudaError_t launch_col_pass(int N, int units, const ColArgs& a, cudaStream_t s, bool pdl);
-// Box of the column-pass tensor map at size N: {inner floats, rows}.
-void col_pass_box(int N, unsigned box[2]);
-// Shared memory the two passes need at size N (bytes), for validation.
-size_t row_pass_smem(int N);
-size_t col_pass_smem(int N);
+// k_col_fft / k_col_out for `units` units; pdl: launch as a programmatic
+// dependent of the preceding kernel in `s`.
+cudaError_t launch_col_fft(int N, int units, const ColArgs& a, cudaStream_t s, bool pdl);
+cudaError_t launch_col_out(int N, int units, const ColArgs& a, cudaStream_t s, bool pdl);
 
 }  // namespace ocean

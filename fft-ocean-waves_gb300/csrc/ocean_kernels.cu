@@ -1,7 +1,7 @@
 // ocean_kernels.cu -- the per-frame Tessendorf ocean update on sm_103a.
 //
-// One frame is two kernels and two HBM round trips (the reference dispatches
-// 6*log2(N)+5 full-grid passes, main.cpp:240-244):
+// One frame is three kernels, chained by programmatic dependent launch (the
+// reference dispatches 6*log2(N)+5 full-grid passes, main.cpp:240-244):
 //
 //   k_row_pass  spectrum evolution + choppy multiply (tilde_h0_t_cs.glsl:70-131)
 //               fused into the horizontal inverse FFT (butterfly_cs.glsl:54-91).
@@ -10,20 +10,23 @@
 //               X_H(k) = (X(k) + conj X(-k))/2, which leaves Re unchanged and
 //               makes the row-transformed rows y' and N-y' conjugates: only
 //               rows 0..N/2 are transformed and stored.  Persistent CTAs walk
-//               the row pairs (y', N-y'); the two h0 rows of the next pairs are
-//               fetched with 1-D bulk TMA copies into a two-stage shared-memory
-//               ring while the current pair is transformed, and the phase w*t
-//               is computed once per mode pair for all three fields.
+//               the row pairs (y', N-y'); the two spectrum rows of the next
+//               pairs are fetched with 1-D bulk TMA copies into a two-stage
+//               shared-memory ring while the current pair is transformed, and
+//               the phase w*t is computed once per four modes for all three
+//               fields.
 //
-//   k_col_pass  vertical inverse FFT (butterfly_cs.glsl:95-132) on column
-//               tiles fetched by 2-D tensor TMA (tile + one neighbour column on
-//               each side, thanks to the periodic padding of the
-//               intermediate), with two real results packed per complex
-//               transform (Dy + i*Dx per column, Dz of two columns), fused with
-//               the (-1)^(x+y)/N^2 inversion (inversion_cs.glsl:29-41), lambda
-//               scaling, the Sobel normal (normal_map_cs.glsl:37-53) and the
-//               Jacobian.  Launched as a programmatic dependent of the row pass
-//               so its set-up overlaps the row pass's tail.
+//   k_col_fft   vertical inverse FFT (butterfly_cs.glsl:95-132) of a column
+//               pair per line triple, two real results packed per complex
+//               transform (Dy + i*Dx per column, Dz of both columns), loaded
+//               straight into registers from the L2-resident intermediate,
+//               fused with the (-1)^(x+y)/N^2 inversion (inversion_cs.glsl:29-41)
+//               and the lambda scaling; writes the maps column-major.
+//
+//   k_col_out   32x32 output tiles: transposes the maps through shared memory,
+//               adds the Sobel normal on Dy (normal_map_cs.glsl:37-53) and the
+//               Jacobian, and writes dx, dy, dz and normal_j row-major with
+//               full-line stores.
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -130,7 +133,12 @@ struct RowCfg {
     static constexpr int LINES   = 3 * PAIRS;
     static constexpr int THREADS = LINES * L::G;
     static constexpr int ITEMS   = (N / 2 + 1 + PAIRS - 1) / PAIRS;  // work items per tile
-    static constexpr int STAGES  = 2;
+    // One ring stage: with MINB CTAs resident per SM a tile's row pairs are
+    // spread over (almost) every CTA slot at once, and the other resident
+    // CTAs hide a CTA's wait for its rows.
+    static constexpr int STAGES  = 1;
+    // resident CTAs per SM the register budget is set for (<= 80 registers)
+    static constexpr int MINB    = 65536 / (THREADS * 80) < 1 ? 1 : (65536 / (THREADS * 80) > 8 ? 8 : 65536 / (THREADS * 80));
     static constexpr int EW      = FROM_H0 ? 2 : 1;   // float2 per staged mode (h0: float4, G: float2)
     // shared memory (float2 units): tw[N] | ring [STAGES][PAIRS][2 rows][N modes] |
     // line buffers [LINES][NPAD] (line inputs in natural order, then the FFT's exchanges)
@@ -143,13 +151,14 @@ struct RowCfg {
 // Fetch the spectrum rows of work item `item` (tile item/ITEMS, row pairs
 // (item%ITEMS)*PAIRS ...) into a ring stage with 1-D bulk copies.
 template <int N, bool FROM_H0>
-__device__ __forceinline__ void row_issue(const RowArgs& a, float2* ring_stage, uint64_t* bar, int item)
+__device__ __forceinline__ void row_issue(const RowArgs& a, float2* ring_stage, uint64_t* bar, int item,
+                                          uint32_t extra_bytes = 0)
 {
     using RC = RowCfg<N, FROM_H0>;
     const int    tile = item / RC::ITEMS, pi = item % RC::ITEMS;
     const float2* src = FROM_H0 ? reinterpret_cast<const float2*>(a.h0 + (size_t)tile * N * N)
                                 : a.spec + (size_t)tile * spec_len(N);
-    uint32_t bytes = 0;
+    uint32_t bytes = extra_bytes;
 #pragma unroll
     for (int pl = 0; pl < RC::PAIRS; ++pl)
         if (pi * RC::PAIRS + pl <= N / 2) bytes += 2 * RC::ROW_BYTES;
@@ -209,11 +218,10 @@ __device__ __forceinline__ void row_modes(const RowArgs& a, const float2* rA, co
 // loop, which the compiler would otherwise hoist into registers.  FROM_H0: the
 // ring holds h0 rows and G, D are formed on the fly (ocean_update_noalloc).
 template <int N, bool MULTI, bool FROM_H0>
-__global__ void __launch_bounds__(RowCfg<N, FROM_H0>::THREADS) k_row_pass(RowArgs a)
+__global__ void __launch_bounds__(RowCfg<N, FROM_H0>::THREADS, RowCfg<N, FROM_H0>::MINB) k_row_pass(RowArgs a)
 {
     using RC = RowCfg<N, FROM_H0>;
     using L  = typename RC::L;
-    constexpr int NP = inter_pitch(N), H = inter_rows(N);
     extern __shared__ unsigned char smem_raw[];
     float2* smem = align_smem(smem_raw);
     float2* tw_s = smem;
@@ -223,18 +231,21 @@ __global__ void __launch_bounds__(RowCfg<N, FROM_H0>::THREADS) k_row_pass(RowArg
     __shared__ int wait_ok;
 
     const int tid = threadIdx.x;
+    const int n_items = a.tiles * RC::ITEMS;
+    // Thread 0 starts every copy at once: the twiddle table rides on the first
+    // stage's barrier (the first item waits for it before its transform).
     if (tid == 0) {
         for (int s = 0; s < RC::STAGES; ++s) mbar_init(&bars[s], 1);
         fence_mbar_init();
-    }
-    for (int i = tid; i < N; i += RC::THREADS) tw_s[i] = a.tw[i];
-    __syncthreads();
-    const int n_items = a.tiles * RC::ITEMS;
-    if (tid == 0)
         for (int s = 0; s < RC::STAGES; ++s) {
             const int item = blockIdx.x + s * gridDim.x;
-            if (item < n_items) row_issue<N, FROM_H0>(a, ring + (size_t)s * RC::PAIRS * 2 * N * RC::EW, &bars[s], item);
+            if (item >= n_items) break;
+            const uint32_t twb = s == 0 ? (uint32_t)(N * sizeof(float2)) : 0u;
+            row_issue<N, FROM_H0>(a, ring + (size_t)s * RC::PAIRS * 2 * N * RC::EW, &bars[s], item, twb);
+            if (twb) bulk_g2s(tw_s, a.tw, twb, &bars[0]);
         }
+    }
+    __syncthreads();
     // The column pass may start its set-up now; it waits for this grid to finish
     // before it reads the intermediate.
     pdl_launch_dependents();
@@ -245,7 +256,7 @@ __global__ void __launch_bounds__(RowCfg<N, FROM_H0>::THREADS) k_row_pass(RowArg
     uint32_t phase_bits = 0;
 
     for (int k = 0, item = blockIdx.x; item < n_items; ++k, item += gridDim.x) {
-        const int s = k & 1;
+        const int s = k % RC::STAGES;
         float2* stage = ring + (size_t)s * RC::PAIRS * 2 * N * RC::EW;
         if (!block_wait(&bars[s], (phase_bits >> s) & 1u, &wait_ok, a.status)) return;
         phase_bits ^= 1u << s;
@@ -311,14 +322,13 @@ __global__ void __launch_bounds__(RowCfg<N, FROM_H0>::THREADS) k_row_pass(RowArg
             line_sync<L, true>(li);                        // the line's inputs are in registers
             line_fft<L, +1>(v, buf, tw_s, t, li);
             if (active) {
-                float2* out = a.inter + (((size_t)unit * 3 + f) * H + yp) * NP;
+                // column-pair blocked: x and x+1 of a row are adjacent.  pos(t, e)
+                // is t plus an even constant, so the parity is t's.
+                static_assert(L::G % 2 == 0 && LineOut<L>::NS % 2 == 0, "even output offsets");
+                float2* out = a.inter + (size_t)unit * inter_len(N) + inter_index(N, f, t, yp);
 #pragma unroll
-                for (int e = 0; e < L::E; ++e) out[LineOut<L>::pos(t, e) + 1] = v[e];
-                // periodic pad columns: x = 0 is thread 0's first output and
-                // x = N-1 the last thread's last one
-                static_assert(LineOut<L>::pos(0, 0) == 0 && LineOut<L>::pos(L::G - 1, L::E - 1) == N - 1, "pad");
-                if (t == 0) out[N + 1] = v[0];
-                if (t == L::G - 1) out[0] = v[L::E - 1];
+                for (int e = 0; e < L::E; ++e)
+                    out[(size_t)(LineOut<L>::pos(0, e) >> 1) * (2 * inter_rows(N))] = v[e];
             }
             // the next inputs overwrite the line buffers: every line has
             // finished reading its own
@@ -328,211 +338,202 @@ __global__ void __launch_bounds__(RowCfg<N, FROM_H0>::THREADS) k_row_pass(RowArg
 }
 
 // ---------------------------------------------------------------------------
-// Column pass.
+// Column transforms.
 // ---------------------------------------------------------------------------
-constexpr int ceil8(int x) { return (x + 7) / 8 * 8; }
-constexpr int imax(int a, int b) { return a > b ? a : b; }
-
-// Column-pass line decomposition: as LineFor except at N = 2048, where the
-// column CTA's 6 lines x 64 threads (32-point first pass) keep 168 registers
-// per thread without spilling (16-point lines would need 768 threads).
+// Column line decomposition: as LineFor except at N = 2048, where 64 threads
+// per line (32-point first pass, 168 registers) keep two CTAs per SM.
 template <int N> struct ColLineFor { using type = typename LineFor<N>::type; };
 template <> struct ColLineFor<2048> { using type = LineCfg<2048, 32, 8, 8>; };
 
 template <int N>
 struct ColCfg {
     using L = typename ColLineFor<N>::type;
-    static constexpr int C       = N >= 2048 ? 4 : 8;   // output columns per CTA
-    static constexpr int CC      = C + 2;               // + one neighbour column each side
-    static constexpr int WL      = CC;                  // round 1: Dy + i*Dx lines, one per column
-    static constexpr int ZL      = CC / 2;              // round 2: Dz(c) + i*Dz(c+1) lines
-    static constexpr int THREADS = WL * L::G;
+    static constexpr int PAIRS   = L::G >= 32 ? 1 : 32 / L::G;   // column pairs per CTA
+    static constexpr int LINES   = 3 * PAIRS;
+    static constexpr int THREADS = LINES * L::G;
+    static constexpr int CTAS    = N / 2 / PAIRS;               // per unit
     static constexpr int H       = inter_rows(N);
-    // Staged rows per field: at least H, and at least half a line buffer so
-    // that a round's exchange buffers fit in the tile fields it has consumed.
-    static constexpr int HP0     = imax(H, (L::NPAD + 1) / 2);
-    static constexpr int NCHUNK  = (HP0 + 255) / 256;   // TMA boxes per field (<= 256 rows)
-    static constexpr int BR      = ceil8((HP0 + NCHUNK - 1) / NCHUNK);   // 128-byte aligned boxes
-    static constexpr int HP      = NCHUNK * BR;
-    static constexpr int OS      = N + 4;               // staging column stride (floats)
-    static constexpr size_t FIELD = (size_t)HP * CC;    // float2 per tile field
-    static constexpr size_t SMEM = sizeof(float2) * (N + 3 * FIELD) + 128;   // + base alignment slack
-    static constexpr int GRID    = N / C;
-    static constexpr uint32_t TILE_BYTES = (uint32_t)(sizeof(float2) * 3 * FIELD);
-    static_assert((size_t)WL * L::NPAD <= 2 * FIELD && (size_t)ZL * L::NPAD <= FIELD, "exchange buffers");
-    static_assert((size_t)CC * OS <= 2 * FIELD, "staging");
+    // the staged intermediate [3][PAIRS][H][2] shares the line buffers
+    static constexpr size_t TILE = (size_t)3 * PAIRS * H * 2;
+    static constexpr size_t WORK = (size_t)LINES * L::NPAD > TILE ? (size_t)LINES * L::NPAD : TILE;
+    static constexpr size_t SMEM = sizeof(float2) * (N + WORK) + 128;
+    static constexpr uint32_t FIELD_BYTES = (uint32_t)(sizeof(float2) * PAIRS * H * 2);
+    static_assert((N / 2) % PAIRS == 0, "column pairs per CTA");
+    static_assert(FIELD_BYTES % 16 == 0, "bulk copy size");
 };
 
+// Line triple of column pair (x0, x0+1): line 0 = Dy + i*Dx of column x0,
+// line 1 the same of column x0+1, line 2 = Dz(x0) + i*Dz(x0+1).  Rows y > N/2
+// are the conjugates of rows N-y (the row-transformed spectra are Hermitian in
+// y), so the inputs come from rows 0..N/2 of the intermediate, whose column
+// pairs are contiguous: one 1-D bulk copy per field stages them.
 template <int N>
-__global__ void __launch_bounds__(ColCfg<N>::THREADS) k_col_pass(const __grid_constant__ ColArgs a)
+__global__ void __launch_bounds__(ColCfg<N>::THREADS) k_col_fft(const __grid_constant__ ColArgs a)
 {
     using CF = ColCfg<N>;
     using L  = typename CF::L;
-    constexpr int C = CF::C, CC = CF::CC, H = CF::H, OS = CF::OS, ZL = CF::ZL;
+    constexpr int H = CF::H;
     extern __shared__ unsigned char smem_raw[];
     float2* smem = align_smem(smem_raw);
     float2* tw_s = smem;
-    float2* tile = smem + N;                                 // [3][HP][CC]: Dx, Dy, Dz (TMA boxes)
-    // round buffers and staging alias the tile fields once they are consumed
-    float2* xbuf1 = tile;                                    // round 1 exchange: fields Dx, Dy
-    float2* xbuf2 = tile + 2 * CF::FIELD;                    // round 2 exchange: field Dz
-    float*  sx = reinterpret_cast<float*>(tile);             // staged Dx [CC][OS]
-    float*  sy = reinterpret_cast<float*>(tile + CF::FIELD); // staged Dy
-    float*  sz = reinterpret_cast<float*>(tile + 2 * CF::FIELD);
+    float2* work = smem + N;                                 // staged tile, then line buffers
     __shared__ __align__(8) uint64_t bar;
     __shared__ int wait_ok;
-    const int x0   = blockIdx.x * C;
-    const int unit = blockIdx.y;
-    const int tid  = threadIdx.x;
-    // read the unit's fields where they are used (a struct copy would stay
-    // live in registers across the FFTs)
-    const ColUnit* cu = a.units ? a.units + unit : &a.u0;
-
+    const int      tid  = threadIdx.x;
+    const int      unit = blockIdx.y;
+    const ColUnit* cu   = a.units ? a.units + unit : &a.u0;
     if (tid == 0) {
         mbar_init(&bar, 1);
         fence_mbar_init();
-        asm volatile("prefetch.tensormap [%0];" ::"l"(&a.map) : "memory");
     }
     for (int i = tid; i < N; i += CF::THREADS) tw_s[i] = a.tw[i];
     pdl_wait_prior();                                        // the row pass has finished
     __syncthreads();
+    const int pair0 = blockIdx.x * CF::PAIRS;
     if (tid == 0) {
-        // Columns x0-1 .. x0+C are padded columns x0 .. x0+C+1 of the intermediate.
-        mbar_arrive_expect_tx(&bar, CF::TILE_BYTES);
+        mbar_arrive_expect_tx(&bar, 3 * CF::FIELD_BYTES);
+        const float2* in = a.inter + (size_t)unit * inter_len(N);
 #pragma unroll
         for (int f = 0; f < 3; ++f)
-#pragma unroll
-            for (int q = 0; q < CF::NCHUNK; ++q)
-                tma_load_2d(tile + f * CF::FIELD + (size_t)q * CF::BR * CC, &a.map, 2 * x0,
-                            (unit * 3 + f) * H + q * CF::BR, &bar);
+            bulk_g2s(work + (size_t)f * CF::PAIRS * H * 2, in + inter_index(N, f, 2 * pair0, 0), CF::FIELD_BYTES, &bar);
     }
     if (!block_wait(&bar, 0, &wait_ok, a.status)) return;
 
+    const int li = tid / L::G, t = tid % L::G;
+    const int kind = li % 3, pl = li / 3;
+    const int x0   = 2 * (pair0 + pl);
+    // Input r of thread t is row y = t + r*G (G = N/R1, t < G): rows below
+    // N/2 for r < R1/2, the conjugate of row N - y for r > R1/2, and for
+    // r = R1/2 row N/2 - t, conjugated unless t = 0 (y = N/2).  So every
+    // shared-memory offset is a per-thread base plus a constant.
+    constexpr int G = L::G;
+    const float2* fy = work + ((size_t)(1 * CF::PAIRS + pl) * H) * 2 + (kind & 1);   // Dy (x0 or x0+1)
+    const float2* fx = work + ((size_t)(0 * CF::PAIRS + pl) * H) * 2 + (kind & 1);   // Dx
+    const float2* fz = work + ((size_t)(2 * CF::PAIRS + pl) * H) * 2;                // Dz pair
     float2 v[L::E];
-    // ---- round 1: column lines Dy + i*Dx, one line per G consecutive threads
-    // (a warp never spans two lines' exchange buffers).
-    {
-        const int cc = tid / L::G, t = tid % L::G;
 #pragma unroll
-        for (int r = 0; r < L::E; ++r) {
-            const int  y  = t + r * (N / L::R1);
-            const bool lo = y <= N / 2;
-            const int  ys = lo ? y : N - y;                  // rows N-y are conjugates of rows y
-            float2 p = tile[CF::FIELD + ys * CC + cc];       // Dy
-            float2 q = tile[ys * CC + cc];                   // Dx
-            if (!lo) { p.y = -p.y; q.y = -q.y; }
-            v[r] = make_float2(p.x - q.y, p.y + q.x);        // p + i*q
+    for (int r = 0; r < L::E; ++r) {
+        const int  ys  = r < L::R1 / 2 ? t + r * G : (r == L::R1 / 2 ? N / 2 - t : N - t - r * G);
+        const bool cj  = r > L::R1 / 2 || (r == L::R1 / 2 && t != 0);
+        float2 p, q;
+        if (kind < 2) {
+            p = fy[2 * ys];
+            q = fx[2 * ys];
+        } else {
+            const float4 z = *reinterpret_cast<const float4*>(fz + 2 * ys);
+            p = make_float2(z.x, z.y);                                     // Dz(x0)
+            q = make_float2(z.z, z.w);                                     // Dz(x0+1)
         }
-        __syncthreads();                                     // fields Dx, Dy consumed
-        line_fft<L, +1>(v, xbuf1 + cc * L::NPAD, tw_s, t, cc);
-        __syncthreads();                                     // every line done with xbuf1
-        const int   xa = x0 - 1 + cc;                        // parity is all that matters
-        const float sa = cu->scale, sb = cu->scale * cu->lambda;
+        if (cj) { p.y = -p.y; q.y = -q.y; }
+        v[r] = make_float2(p.x - q.y, p.y + q.x);                          // p + i*q
+    }
+    __syncthreads();                                         // the tile is consumed: line buffers reuse it
+    pdl_launch_dependents();                                 // k_col_out may start its set-up
+    line_fft<L, +1>(v, work + li * L::NPAD, tw_s, t, li);
+
+    float* const tm = a.tmap + (size_t)unit * tmap_len(N);
+    const float  sa = cu->scale, sb = cu->scale * cu->lambda;
+    // output y = pos(t, e) is t plus an even constant: the (-1)^(x+y) sign is
+    // the thread's
+    static_assert(L::G % 2 == 0 && LineOut<L>::NS % 2 == 0, "even output offsets");
+    if (kind < 2) {
+        const int   x  = x0 + kind;
+        const float sg = ((x + t) & 1) ? -1.0f : 1.0f;
+        const float ka = sg * sa, kb = sg * sb;
+        float* ox = tm + (size_t)x * N + t;                       // Dx column x
+        float* oy = tm + ((size_t)N + x) * N + t;                 // Dy column x
 #pragma unroll
         for (int e = 0; e < L::E; ++e) {
-            const int   y  = LineOut<L>::pos(t, e);
-            const float sg = ((xa + y) & 1) ? -1.0f : 1.0f;
-            sy[cc * OS + y] = sg * sa * v[e].x;
-            sx[cc * OS + y] = sg * sb * v[e].y;
+            oy[LineOut<L>::pos(0, e)] = ka * v[e].x;
+            ox[LineOut<L>::pos(0, e)] = kb * v[e].y;
+        }
+    } else {
+        const float sg = ((x0 + t) & 1) ? -1.0f : 1.0f;
+        const float kb = sg * sb;
+        float* oz = tm + ((size_t)2 * N + x0) * N + t;            // Dz columns x0, x0+1
+#pragma unroll
+        for (int e = 0; e < L::E; ++e) {
+            oz[LineOut<L>::pos(0, e)]     = kb * v[e].x;
+            oz[N + LineOut<L>::pos(0, e)] = -kb * v[e].y;
         }
     }
-    // ---- round 2: Dz(c) + i*Dz(c+1) lines on the first ZL*G threads.
-    {
-        const bool zact = tid < ZL * L::G;
-        const int  p2 = tid / L::G, t = tid % L::G;
-        if (zact) {
-#pragma unroll
-            for (int r = 0; r < L::E; ++r) {
-                const int  y  = t + r * (N / L::R1);
-                const bool lo = y <= N / 2;
-                const int  ys = lo ? y : N - y;
-                const float4 z2 = *reinterpret_cast<const float4*>(tile + 2 * CF::FIELD + ys * CC + 2 * p2);
-                float2 p = make_float2(z2.x, z2.y), q = make_float2(z2.z, z2.w);
-                if (!lo) { p.y = -p.y; q.y = -q.y; }
-                v[r] = make_float2(p.x - q.y, p.y + q.x);
-            }
-        }
-        __syncthreads();                                     // field Dz consumed
-        if (zact || L::G < 32) line_fft<L, +1>(v, xbuf2 + (zact ? p2 : 0) * L::NPAD, tw_s, t, zact ? p2 : 0, zact);
-        __syncthreads();                                     // every line done with xbuf2
-        if (zact) {
-            const int   xa = x0 - 1 + 2 * p2;
-            const float sb = cu->scale * cu->lambda;
-#pragma unroll
-            for (int e = 0; e < L::E; ++e) {
-                const int   y  = LineOut<L>::pos(t, e);
-                const float sg = ((xa + y) & 1) ? -1.0f : 1.0f;
-                sz[(2 * p2) * OS + y]     = sg * sb * v[e].x;
-                sz[(2 * p2 + 1) * OS + y] = -sg * sb * v[e].y;
-            }
-        }
-    }
-    __syncthreads();
+}
 
-    // Epilogue: a 4-row x 2-column block per thread (float4 shared reads down
-    // the staged columns, float2 global stores across them); Sobel normal on Dy
-    // and the Jacobian of x - (Dx, Dz).
-    float* const  odx = cu->dx;
-    float* const  ody = cu->dy;
-    float* const  odz = cu->dz;
-    float4* const onj = cu->nj;
-    const float   inv2d = cu->inv2d;
-    for (int i = tid; i < (C / 2) * (N / 4); i += CF::THREADS) {
-        const int cp = i % (C / 2), y0 = 4 * (i / (C / 2));
-        const int cb = 2 * cp + 1;                                // staged column of output column 2cp
-        const int ym = (y0 - 1) & (N - 1), yn = (y0 + 4) & (N - 1);
-        // Y[d][k]: Dy at staged column cb-1+d, rows y0-1+k (d < 4, k < 6)
-        float Y[4][6], X[2][6], Z[2][6], XS[2][4], ZS[2][4];
+// ---------------------------------------------------------------------------
+// Output tiles: 32 x 32 texels per CTA, with a one-texel periodic halo.
+// ---------------------------------------------------------------------------
+constexpr int kOutT  = 32;             // tile edge
+constexpr int kOutW  = kOutT + 2;      // with halo
+constexpr int kOutP  = kOutT + 3;      // shared pitch: odd, so column-wise reads are conflict-free
+constexpr int kOutTh = 256;
+
+template <int N>
+__global__ void __launch_bounds__(kOutTh) k_col_out(const __grid_constant__ ColArgs a)
+{
+    __shared__ float S[3][kOutW][kOutP];                     // [field][x][y]: Dx, Dy, Dz
+    const int      unit = blockIdx.z;
+    const int      x0 = blockIdx.x * kOutT, y0 = blockIdx.y * kOutT;
+    const ColUnit* cu = a.units ? a.units + unit : &a.u0;
+    float* const   odx = cu->dx;
+    float* const   ody = cu->dy;
+    float* const   odz = cu->dz;
+    float4* const  onj = cu->nj;
+    const float    inv2d = cu->inv2d;
+    const float*   tm = a.tmap + (size_t)unit * tmap_len(N);
+    pdl_wait_prior();                                        // the column transforms have finished
+    // One warp per staged column (field f, column xx): lane l loads row
+    // y0-1+l, and the two last rows of the warp's columns are spread over the
+    // lanes (lane l: column l/2, row y0+31+(l&1)).  Every load of a thread is
+    // issued before its first shared-memory store.
+    constexpr int NCOL = 3 * kOutW, WARPS = kOutTh / 32, PER = (NCOL + WARPS - 1) / WARPS;
+    static_assert(2 * PER <= 32, "edge rows: one per lane");
+    const int lane = threadIdx.x % 32, warp = threadIdx.x / 32;
+    float     body[PER], edge = 0.0f;
 #pragma unroll
-        for (int d = 0; d < 4; ++d) {
-            const float* col = sy + (cb - 1 + d) * OS;
-            const float4 m4 = *reinterpret_cast<const float4*>(col + y0);
-            Y[d][0] = col[ym]; Y[d][1] = m4.x; Y[d][2] = m4.y; Y[d][3] = m4.z; Y[d][4] = m4.w; Y[d][5] = col[yn];
+    for (int j = 0; j < PER; ++j) {
+        const int c = warp + WARPS * j;                          // warp-uniform
+        if (c < NCOL) {
+            const int f = c / kOutW, xx = c - f * kOutW;
+            body[j] = tm[((size_t)f * N + ((x0 - 1 + xx) & (N - 1))) * N + ((y0 - 1 + lane) & (N - 1))];
         }
+    }
+    const int ce = warp + WARPS * (lane >> 1);
+    const int fe = ce / kOutW, xe = ce - fe * kOutW;
+    if (lane < 2 * PER && ce < NCOL)
+        edge = tm[((size_t)fe * N + ((x0 - 1 + xe) & (N - 1))) * N + ((y0 + 31 + (lane & 1)) & (N - 1))];
 #pragma unroll
-        for (int d = 0; d < 2; ++d) {
-            const float* cx = sx + (cb + d) * OS;
-            const float4 mx = *reinterpret_cast<const float4*>(cx + y0);
-            X[d][0] = cx[ym]; X[d][1] = mx.x; X[d][2] = mx.y; X[d][3] = mx.z; X[d][4] = mx.w; X[d][5] = cx[yn];
-            const float* cz = sz + (cb + d) * OS;
-            const float4 mz = *reinterpret_cast<const float4*>(cz + y0);
-            Z[d][0] = cz[ym]; Z[d][1] = mz.x; Z[d][2] = mz.y; Z[d][3] = mz.z; Z[d][4] = mz.w; Z[d][5] = cz[yn];
-            // the outer x-neighbours: staged columns cb-1 (d = 0) and cb+2 (d = 1)
-            const float4 ox = *reinterpret_cast<const float4*>(sx + (cb - 1 + 3 * d) * OS + y0);
-            const float4 oz = *reinterpret_cast<const float4*>(sz + (cb - 1 + 3 * d) * OS + y0);
-            XS[d][0] = ox.x; XS[d][1] = ox.y; XS[d][2] = ox.z; XS[d][3] = ox.w;
-            ZS[d][0] = oz.x; ZS[d][1] = oz.y; ZS[d][2] = oz.z; ZS[d][3] = oz.w;
+    for (int j = 0; j < PER; ++j) {
+        const int c = warp + WARPS * j;
+        if (c < NCOL) {
+            const int f = c / kOutW, xx = c - f * kOutW;
+            S[f][xx][lane] = body[j];
         }
+    }
+    if (lane < 2 * PER && ce < NCOL) S[fe][xe][32 + (lane & 1)] = edge;
+    __syncthreads();
+    const int xx = threadIdx.x % kOutT + 1;
 #pragma unroll
-        for (int k = 0; k < 4; ++k) {
-            float4 njv[2];
-#pragma unroll
-            for (int d = 0; d < 2; ++d) {
-                // taps z0..z7 (normal_map_cs.glsl:37-44) around (column d, row k+1)
-                const float z0 = Y[d][k], z1 = Y[d + 1][k], z2 = Y[d + 2][k];
-                const float z3 = Y[d][k + 1], z4 = Y[d + 2][k + 1];
-                const float z5 = Y[d][k + 2], z6 = Y[d + 1][k + 2], z7 = Y[d + 2][k + 2];
-                const float nz = z0 + 2.0f * z1 + z2 - z5 - 2.0f * z6 - z7;
-                const float nx = z0 + 2.0f * z3 + z5 - z2 - 2.0f * z4 - z7;
-                const float rn = rsqrtf(nx * nx + 1.0f + nz * nz);
-                const float xl = d == 0 ? XS[0][k] : X[0][k + 1], xr = d == 0 ? X[1][k + 1] : XS[1][k];
-                const float zl = d == 0 ? ZS[0][k] : Z[0][k + 1], zr = d == 0 ? Z[1][k + 1] : ZS[1][k];
-                const float dxx = (xr - xl) * inv2d;
-                const float dxz = (X[d][k + 2] - X[d][k]) * inv2d;
-                const float dzx = (zr - zl) * inv2d;
-                const float dzz = (Z[d][k + 2] - Z[d][k]) * inv2d;
-                // J = (1 - dxx)(1 - dzz) - dxz*dzx, formed as 1 + deviation so that
-                // the only rounding at the scale of 1 is the final add
-                const float dJ = (dxx * dzz - dxz * dzx) - dxx - dzz;
-                njv[d] = make_float4(nx * rn, rn, nz * rn, 1.0f + dJ);
-            }
-            const size_t o = (size_t)(y0 + k) * N + x0 + 2 * cp;
-            *reinterpret_cast<float2*>(odx + o) = make_float2(X[0][k + 1], X[1][k + 1]);
-            *reinterpret_cast<float2*>(ody + o) = make_float2(Y[1][k + 1], Y[2][k + 1]);
-            *reinterpret_cast<float2*>(odz + o) = make_float2(Z[0][k + 1], Z[1][k + 1]);
-            onj[o]     = njv[0];
-            onj[o + 1] = njv[1];
-        }
+    for (int j = 0; j < kOutT * kOutT / kOutTh; ++j) {
+        const int yy = threadIdx.x / kOutT + j * (kOutTh / kOutT) + 1;
+        // taps z0..z7 (normal_map_cs.glsl:37-44): z0 = (x-1, y-1), z1 = (x, y-1), ...
+        const float z0 = S[1][xx - 1][yy - 1], z1 = S[1][xx][yy - 1], z2 = S[1][xx + 1][yy - 1];
+        const float z3 = S[1][xx - 1][yy], z4 = S[1][xx + 1][yy];
+        const float z5 = S[1][xx - 1][yy + 1], z6 = S[1][xx][yy + 1], z7 = S[1][xx + 1][yy + 1];
+        const float nz = z0 + 2.0f * z1 + z2 - z5 - 2.0f * z6 - z7;
+        const float nx = z0 + 2.0f * z3 + z5 - z2 - 2.0f * z4 - z7;
+        const float rn = rsqrtf(nx * nx + 1.0f + nz * nz);
+        const float dxx = (S[0][xx + 1][yy] - S[0][xx - 1][yy]) * inv2d;
+        const float dxz = (S[0][xx][yy + 1] - S[0][xx][yy - 1]) * inv2d;
+        const float dzx = (S[2][xx + 1][yy] - S[2][xx - 1][yy]) * inv2d;
+        const float dzz = (S[2][xx][yy + 1] - S[2][xx][yy - 1]) * inv2d;
+        // J = (1 - dxx)(1 - dzz) - dxz*dzx, formed as 1 + deviation so that the
+        // only rounding at the scale of 1 is the final add
+        const float  dJ = (dxx * dzz - dxz * dzx) - dxx - dzz;
+        const size_t o  = (size_t)(y0 + yy - 1) * N + x0 + xx - 1;
+        odx[o] = S[0][xx][yy];
+        ody[o] = S[1][xx][yy];
+        odz[o] = S[2][xx][yy];
+        onj[o] = make_float4(nx * rn, rn, nz * rn, 1.0f + dJ);
     }
 }
 
@@ -587,34 +588,46 @@ static cudaError_t row_pass_n(const RowArgs& a, cudaStream_t s)
                                                 : row_pass_nm<N, true, false>(a, s);
 }
 
+static cudaLaunchAttribute pdl_attr()
+{
+    cudaLaunchAttribute at;
+    at.id                                         = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at.val.programmaticStreamSerializationAllowed = 1;
+    return at;
+}
+
 template <int N>
-static cudaError_t col_pass_n(int units, const ColArgs& a, cudaStream_t s, bool pdl)
+static cudaError_t col_fft_n(int units, const ColArgs& a, cudaStream_t s, bool pdl)
 {
     using CF = ColCfg<N>;
     static bool attr = false;
     if (!attr) {
-        cudaError_t e = cudaFuncSetAttribute(k_col_pass<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)CF::SMEM);
+        cudaError_t e = cudaFuncSetAttribute(k_col_fft<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)CF::SMEM);
         if (e != cudaSuccess) return e;
         attr = true;
     }
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim          = dim3(CF::GRID, units);
-    cfg.blockDim         = dim3(CF::THREADS);
-    cfg.dynamicSmemBytes = CF::SMEM;
-    cfg.stream           = s;
-    cudaLaunchAttribute at[1];
-    at[0].id                                         = cudaLaunchAttributeProgrammaticStreamSerialization;
-    at[0].val.programmaticStreamSerializationAllowed = 1;
-    cfg.attrs    = at;
-    cfg.numAttrs = pdl ? 1 : 0;
-    return cudaLaunchKernelEx(&cfg, k_col_pass<N>, a);
+    cudaLaunchAttribute at[1] = {pdl_attr()};
+    cudaLaunchConfig_t  cfg   = {};
+    cfg.gridDim               = dim3(CF::CTAS, units);
+    cfg.blockDim              = dim3(CF::THREADS);
+    cfg.dynamicSmemBytes      = CF::SMEM;
+    cfg.stream                = s;
+    cfg.attrs                 = at;
+    cfg.numAttrs              = pdl ? 1 : 0;
+    return cudaLaunchKernelEx(&cfg, k_col_fft<N>, a);
 }
 
 template <int N>
-static void col_box_n(unsigned box[2])
+static cudaError_t col_out_n(int units, const ColArgs& a, cudaStream_t s, bool pdl)
 {
-    box[0] = 2 * ColCfg<N>::CC;
-    box[1] = ColCfg<N>::BR;
+    cudaLaunchAttribute at[1] = {pdl_attr()};
+    cudaLaunchConfig_t  cfg   = {};
+    cfg.gridDim               = dim3(N / kOutT, N / kOutT, units);
+    cfg.blockDim              = dim3(kOutTh);
+    cfg.stream                = s;
+    cfg.attrs                 = at;
+    cfg.numAttrs              = pdl ? 1 : 0;
+    return cudaLaunchKernelEx(&cfg, k_col_out<N>, a);
 }
 
 #define OCEAN_FOR_EACH_N(M) M(32) M(64) M(128) M(256) M(512) M(1024) M(2048)
@@ -629,44 +642,23 @@ cudaError_t launch_row_pass(int N, const RowArgs& a, cudaStream_t s)
     }
 }
 
-cudaError_t launch_col_pass(int N, int units, const ColArgs& a, cudaStream_t s, bool pdl)
+cudaError_t launch_col_fft(int N, int units, const ColArgs& a, cudaStream_t s, bool pdl)
 {
     switch (N) {
-#define CASE(n) case n: return col_pass_n<n>(units, a, s, pdl);
+#define CASE(n) case n: return col_fft_n<n>(units, a, s, pdl);
         OCEAN_FOR_EACH_N(CASE)
 #undef CASE
     default: return cudaErrorInvalidValue;
     }
 }
 
-void col_pass_box(int N, unsigned box[2])
-{
-    box[0] = box[1] = 0;
-    switch (N) {
-#define CASE(n) case n: col_box_n<n>(box); break;
-        OCEAN_FOR_EACH_N(CASE)
-#undef CASE
-    default: break;
-    }
-}
-
-size_t row_pass_smem(int N)
+cudaError_t launch_col_out(int N, int units, const ColArgs& a, cudaStream_t s, bool pdl)
 {
     switch (N) {
-#define CASE(n) case n: return RowCfg<n, true>::SMEM;
+#define CASE(n) case n: return col_out_n<n>(units, a, s, pdl);
         OCEAN_FOR_EACH_N(CASE)
 #undef CASE
-    default: return 0;
-    }
-}
-
-size_t col_pass_smem(int N)
-{
-    switch (N) {
-#define CASE(n) case n: return ColCfg<n>::SMEM;
-        OCEAN_FOR_EACH_N(CASE)
-#undef CASE
-    default: return 0;
+    default: return cudaErrorInvalidValue;
     }
 }
 

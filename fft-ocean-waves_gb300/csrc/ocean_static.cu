@@ -6,15 +6,16 @@
 // code, code that runs while the application's allocator is locked or its
 // memory pool is exhausted, and callers that must hold a fixed memory budget
 // decided at load time.  For them this entry point takes the spectrum h0 and
-// the output maps from the caller and keeps the one piece of scratch the frame
-// needs -- the row-pass intermediate -- in a fixed array compiled into this
-// library, instead of in a handle's cudaMalloc'd buffer.
+// the output maps from the caller and keeps the scratch the frame needs -- the
+// row-pass intermediate and the column-major maps of the column transforms --
+// in fixed arrays compiled into this library, instead of in a handle's
+// cudaMalloc'd buffers.
 //
-// The array is a file-scope `static __device__` array sized for N <= 1024
-// (12,632,112 bytes); every GPU that loads the library holds it until the
-// process exits.  In host code its name is only a stand-in: the device address
-// is obtained with cudaGetSymbolAddress once per device, with that device
-// current, on the first call made on that device.
+// The arrays are file-scope `static __device__` arrays sized for N <= 1024
+// (25,190,400 bytes of scratch); every GPU that loads the library holds them
+// until the process exits.  In host code their names are only stand-ins: the
+// device addresses are obtained with cudaGetSymbolAddress once per device, with
+// that device current, on the first call made on that device.
 #include <cuda.h>
 #include <cuda_runtime.h>
 
@@ -29,10 +30,14 @@
 namespace {
 
 constexpr int    kStaticMaxN     = 1024;
-constexpr size_t kStaticInterLen = 3 * (size_t)(kStaticMaxN / 2 + 1) * (kStaticMaxN + 2);  // float2
+constexpr size_t kStaticInterLen = 3 * (size_t)(kStaticMaxN / 2 + 1) * kStaticMaxN;  // float2
+constexpr size_t kStaticTmapLen  = 3 * (size_t)kStaticMaxN * kStaticMaxN;            // float
+static_assert(kStaticInterLen * 8 + kStaticTmapLen * 4 == 25190400, "documented scratch size");
 
-// The frame's scratch: row-pass intermediate, twiddle table, device status word.
+// The frame's scratch: row-pass intermediate, column-major maps, twiddle
+// table, device status word.
 static __device__ __align__(256) float2   g_static_inter[kStaticInterLen];
+static __device__ __align__(256) float    g_static_tmap[kStaticTmapLen];
 static __device__ __align__(256) float2   g_static_tw[kStaticMaxN];
 static __device__ __align__(256) unsigned g_static_status;
 
@@ -41,11 +46,10 @@ constexpr int kMaxDevices = 64;
 struct DeviceScratch {
     bool        ready   = false;
     float2*     inter   = nullptr;   // device addresses of the arrays above
+    float*      tmap    = nullptr;
     float2*     tw      = nullptr;
     unsigned*   status  = nullptr;
     int         tw_N    = 0;         // N whose twiddles the table holds
-    int         map_N   = 0;         // N the tensor map was encoded for
-    CUtensorMap map;
 };
 
 // exp(+2*pi*i*k/N) for k < N, from double-precision sincospi.
@@ -67,6 +71,7 @@ int setup(int dev, DeviceScratch& d, cudaStream_t s)
 {
     cudaError_t e;
     if ((e = cudaGetSymbolAddress(reinterpret_cast<void**>(&d.inter), g_static_inter)) != cudaSuccess ||
+        (e = cudaGetSymbolAddress(reinterpret_cast<void**>(&d.tmap), g_static_tmap)) != cudaSuccess ||
         (e = cudaGetSymbolAddress(reinterpret_cast<void**>(&d.tw), g_static_tw)) != cudaSuccess ||
         (e = cudaGetSymbolAddress(reinterpret_cast<void**>(&d.status), g_static_status)) != cudaSuccess)
         return ocean::host::cuda_fail(e, "cudaGetSymbolAddress of the static scratch");
@@ -113,10 +118,6 @@ extern "C" int ocean_update_noalloc(const ocean_params* params, const float* h0_
         if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(e, "static twiddle launch");
         d.tw_N = N;
     }
-    if (d.map_N != N) {
-        if ((rc = encode_inter_map(&d.map, d.inter, N, 1)) != OCEAN_OK) return rc;
-        d.map_N = N;
-    }
 
     // one frame: the same two kernels as ocean_update, scratch from the arrays
     const double g  = gravity_of(*params);
@@ -138,7 +139,8 @@ extern "C" int ocean_update_noalloc(const ocean_params* params, const float* h0_
     ra.S               = 1;
     if ((e = ocean::launch_row_pass(N, ra, s)) != cudaSuccess) return cuda_fail(e, "row pass launch");
     ocean::ColArgs ca;
-    ca.map       = d.map;
+    ca.inter     = d.inter;
+    ca.tmap      = d.tmap;
     ca.status    = d.status;
     ca.tw        = d.tw;
     ca.units     = nullptr;
@@ -150,6 +152,7 @@ extern "C" int ocean_update_noalloc(const ocean_params* params, const float* h0_
     ca.u0.lambda = params->choppiness;
     ca.u0.inv2d  = (float)((double)N / (2.0 * (double)params->L));
     ca.u0.pad_   = 0.0f;
-    if ((e = ocean::launch_col_pass(N, 1, ca, s, true)) != cudaSuccess) return cuda_fail(e, "column pass launch");
+    if ((e = ocean::launch_col_fft(N, 1, ca, s, true)) != cudaSuccess) return cuda_fail(e, "column transform launch");
+    if ((e = ocean::launch_col_out(N, 1, ca, s, true)) != cudaSuccess) return cuda_fail(e, "output launch");
     return OCEAN_OK;
 }

@@ -96,16 +96,24 @@ OCEAN_API void ocean_destroy(ocean_t* ocean);
  * double-float precision).  Replaces tilde_h0_t(); butterfly_fft(dy),
  * butterfly_fft(dx), butterfly_fft(dz); generate_normal_map()
  * (main.cpp:240-244).  out == NULL writes the handle-owned buffers returned
- * by ocean_get_outputs().  Two kernel launches on `stream`. */
+ * by ocean_get_outputs().  Three kernel launches on `stream`. */
 OCEAN_API int ocean_update(ocean_t* ocean, double t, const ocean_outputs* out, void* stream);
 
-/* ocean_update in its two stages, for callers that interleave other work or
- * time the kernels separately: the row stage (evolution + horizontal FFT,
- * replacing tilde_h0_t() and the horizontal butterfly passes, main.cpp:240,
- * :626-640) and the column stage (vertical FFT + inversion + normal map,
- * main.cpp:647-707).  ocean_update == rows then columns on one stream. */
+/* ocean_update in its three stages, one kernel each, for callers that
+ * interleave other work or time the kernels separately:
+ *   rows     evolution + horizontal FFT (tilde_h0_t() and the horizontal
+ *            butterfly passes, main.cpp:240, :626-640) into the handle's
+ *            intermediate;
+ *   columns  vertical FFT + inversion (the vertical butterfly passes and
+ *            inversion_cs.glsl, main.cpp:647-682) into the handle's
+ *            column-major maps;
+ *   outputs  the maps written to dx, dy, dz, plus the normal map and
+ *            Jacobian (generate_normal_map(), main.cpp:244, :687-707); out ==
+ *            NULL writes the handle-owned buffers.
+ * ocean_update == rows, columns, outputs on one stream. */
 OCEAN_API int ocean_update_rows(ocean_t* ocean, double t, void* stream);
-OCEAN_API int ocean_update_columns(ocean_t* ocean, const ocean_outputs* out, void* stream);
+OCEAN_API int ocean_update_columns(ocean_t* ocean, void* stream);
+OCEAN_API int ocean_update_outputs(ocean_t* ocean, const ocean_outputs* out, void* stream);
 
 /* Synchronise `stream` and report (and clear) the handle's device status:
  * OCEAN_ERR_TIMEOUT if a kernel gave up a bounded wait for its TMA copies
@@ -179,8 +187,9 @@ OCEAN_API void ocean_batch_destroy(ocean_batch_t* batch);
  * exhausted, and callers held to a memory budget fixed at load time.  No
  * handle: the caller passes the parameters, the spectrum h0 (device,
  * N*N*4 floats, the layout of ocean_get_h0 / ocean_compute_h0) and the output
- * maps.  The frame's scratch (the row-pass intermediate, 12,632,112 bytes,
- * plus a twiddle table and a status word) lives in static device arrays
+ * maps.  The frame's scratch (the row-pass intermediate and the column
+ * transforms' maps, 25,190,400 bytes, plus a twiddle table and a status word)
+ * lives in static device arrays
  * compiled into the library, sized for N <= 1024; every GPU that loads the
  * library holds them until the process exits.  N > 1024 is rejected with
  * OCEAN_ERR_INVALID.  The first call on a device resolves the arrays' addresses
