@@ -2,14 +2,17 @@
 // include/ocean.h).  No counterpart in the reference, which renders one tile.
 //
 // Tiles are grouped by N.  Per group: the combined spectrum (G, D) of every
-// tile back to back (h0 itself is only a creation-time temporary), one
-// intermediate and one set of column-major maps per (tile, time sample) back
-// to back, and one twiddle table.  An update is a CUDA graph of
+// tile back to back (h0 itself is only a creation-time temporary), one twiddle
+// table, and scratch (intermediate + column-major maps) for one wave of units
+// (unit = (tile, time sample)).  A wave is as many units as fit a 64 MB scratch
+// budget, so its three stages run out of L2: whole tiles with all their
+// samples for small N, runs of samples of one tile for large N.  An update is
+// a CUDA graph of
 //   H2D copy of the per-unit constants (pinned staging -> device)
-//   per group: k_row_pass (persistent; each spectrum row pair is staged once and
-//              serves all samples of its tile) -> k_col_fft -> k_col_out
-//              (grids: column pairs / output tiles x units, each a
-//              programmatic dependent of the kernel before it)
+//   per wave: k_row_pass (persistent; each spectrum row pair is staged once
+//             and serves all samples of its tile in the wave) -> k_col_fft ->
+//             k_col_out (grids: column pairs / output tiles x units, each a
+//             programmatic dependent of the kernel before it)
 // captured at creation and replayed by ocean_batch_update.
 #include <cuda_runtime.h>
 
@@ -33,6 +36,9 @@ struct ocean_batch_s {
         float*           tmap  = nullptr;
         float2*          tw    = nullptr;
         size_t           first_unit = 0; // this group's units start here in the unit arrays
+        int              wave_tiles = 1; // tiles per wave (all S samples), or
+        int              wave_smp   = 0; // if > 0: samples per wave of a single tile
+        int              wave_units = 1; // units the scratch holds
     };
     int                       n_tiles = 0, S = 0;
     std::vector<ocean_params> params;
@@ -81,6 +87,58 @@ struct ocean_batch_s {
 
 namespace {
 
+// Scratch (intermediate + column-major maps) one wave of units may use: a
+// wave's three stages then run out of L2 (129 MB) instead of HBM.
+constexpr size_t kWaveBytes = 64ull << 20;
+
+size_t unit_scratch_bytes(int N) { return ocean::inter_len(N) * sizeof(float2) + ocean::tmap_len(N) * sizeof(float); }
+
+// Waves of a group: whole tiles (all samples) when a tile's samples fit the
+// budget, else runs of samples of one tile; units are tile-major, so a wave's
+// units are contiguous and share their tiles' spectra.
+void plan_waves(ocean_batch_s::Group& g, int S)
+{
+    const size_t U = std::max<size_t>(1, kWaveBytes / unit_scratch_bytes(g.N));
+    const size_t T = g.tiles.size();
+    if (U >= (size_t)S) {
+        g.wave_tiles = (int)std::min(T, U / S);
+        g.wave_smp   = 0;
+        g.wave_units = g.wave_tiles * S;
+    } else {   // equal runs: ceil(S / U) waves per tile
+        const int runs = (int)((S + U - 1) / U);
+        g.wave_tiles   = 1;
+        g.wave_smp     = (S + runs - 1) / runs;
+        g.wave_units   = g.wave_smp;
+    }
+}
+
+// One wave: `tiles` tiles from slot t0, samples s0 .. s0+smp-1 of each.
+cudaError_t launch_wave(ocean_batch_s* b, const ocean_batch_s::Group& g, int t0, int tiles, int s0, int smp)
+{
+    const size_t u0 = g.first_unit + (size_t)t0 * b->S + s0;   // first unit (batch order)
+    ocean::RowArgs ra;
+    ra.spec   = g.spec + (size_t)t0 * ocean::spec_len(g.N);
+    ra.h0     = nullptr;
+    ra.inter  = g.inter;
+    ra.tw     = g.tw;
+    ra.status = b->status;
+    ra.fcs    = b->d_fc() + u0;
+    ra.fc0    = ocean::FrameConsts{};
+    ra.tiles  = tiles;
+    ra.S      = smp;
+    cudaError_t e = ocean::launch_row_pass(g.N, ra, b->cap);
+    if (e != cudaSuccess) return e;
+    ocean::ColArgs ca;
+    ca.inter  = g.inter;
+    ca.tmap   = g.tmap;
+    ca.status = b->status;
+    ca.tw     = g.tw;
+    ca.units  = b->d_units() + u0;
+    ca.u0     = ocean::ColUnit{};
+    if ((e = ocean::launch_col_fft(g.N, tiles * smp, ca, b->cap, true)) != cudaSuccess) return e;
+    return ocean::launch_col_out(g.N, tiles * smp, ca, b->cap, true);
+}
+
 int capture(ocean_batch_s* b)
 {
     cudaError_t e;
@@ -88,28 +146,16 @@ int capture(ocean_batch_s* b)
         return cuda_fail(e, "batch graph capture");
     e = cudaMemcpyAsync(b->d_desc, b->h_desc, b->desc_bytes, cudaMemcpyHostToDevice, b->cap);
     for (size_t gi = 0; gi < b->groups.size() && e == cudaSuccess; ++gi) {
-        ocean_batch_s::Group& g = b->groups[gi];
-        ocean::RowArgs ra;
-        ra.spec   = g.spec;
-        ra.h0     = nullptr;
-        ra.inter  = g.inter;
-        ra.tw     = g.tw;
-        ra.status = b->status;
-        ra.fcs    = b->d_fc() + g.first_unit;
-        ra.fc0    = ocean::FrameConsts{};
-        ra.tiles  = (int)g.tiles.size();
-        ra.S      = b->S;
-        if ((e = ocean::launch_row_pass(g.N, ra, b->cap)) != cudaSuccess) break;
-        ocean::ColArgs ca;
-        ca.inter  = g.inter;
-        ca.tmap   = g.tmap;
-        ca.status = b->status;
-        ca.tw     = g.tw;
-        ca.units  = b->d_units() + g.first_unit;
-        ca.u0     = ocean::ColUnit{};
-        const int units = (int)g.tiles.size() * b->S;
-        if ((e = ocean::launch_col_fft(g.N, units, ca, b->cap, true)) != cudaSuccess) break;
-        e = ocean::launch_col_out(g.N, units, ca, b->cap, true);
+        const ocean_batch_s::Group& g = b->groups[gi];
+        const int T = (int)g.tiles.size();
+        if (g.wave_smp == 0) {
+            for (int t0 = 0; t0 < T && e == cudaSuccess; t0 += g.wave_tiles)
+                e = launch_wave(b, g, t0, std::min(g.wave_tiles, T - t0), 0, b->S);
+        } else {
+            for (int t = 0; t < T && e == cudaSuccess; ++t)
+                for (int s0 = 0; s0 < b->S && e == cudaSuccess; s0 += g.wave_smp)
+                    e = launch_wave(b, g, t, 1, s0, std::min(g.wave_smp, b->S - s0));
+        }
     }
     cudaGraph_t graph = nullptr;
     cudaError_t e2    = cudaStreamEndCapture(b->cap, &graph);
@@ -183,9 +229,11 @@ int ocean_batch_create(const ocean_params* params, const uint64_t* seeds, int32_
     }
     for (ocean_batch_s::Group& g : b->groups) {
         const size_t N = (size_t)g.N, NN = N * N, T = g.tiles.size();
+        plan_waves(g, samples);
+        const size_t W = (size_t)g.wave_units;
         if ((e = cudaMalloc(&g.spec, T * ocean::spec_len(g.N) * sizeof(float2))) != cudaSuccess ||
-            (e = cudaMalloc(&g.inter, T * samples * ocean::inter_len(g.N) * sizeof(float2))) != cudaSuccess ||
-            (e = cudaMalloc(&g.tmap, T * samples * ocean::tmap_len(g.N) * sizeof(float))) != cudaSuccess) {
+            (e = cudaMalloc(&g.inter, W * ocean::inter_len(g.N) * sizeof(float2))) != cudaSuccess ||
+            (e = cudaMalloc(&g.tmap, W * ocean::tmap_len(g.N) * sizeof(float))) != cudaSuccess) {
             cudaFree(d_noise);
             cudaFree(d_h0);
             delete b;
