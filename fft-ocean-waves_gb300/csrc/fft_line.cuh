@@ -163,6 +163,19 @@ template <> struct LineFor<512>  { using type = LineCfg<512, 16, 16, 2>; };
 template <> struct LineFor<1024> { using type = LineCfg<1024, 16, 16, 4>; };
 template <> struct LineFor<2048> { using type = LineCfg<2048, 16, 16, 8>; };
 
+// Inter-pass twiddles of a decomposition, laid out so that the threads of a
+// warp read consecutive entries (no bank conflicts, no index arithmetic):
+//   pass 2: T[r*R1 + k]          = W_N^(k*r*N/(R1*R2)),  k < R1,    r < R2;
+//   pass 3: T[P2 + r*R1*R2 + k]  = W_N^(k*r),            k < R1*R2, r < R3;
+// W_N = exp(+2*pi*i/N), rounded from double (conjugated in the transform for
+// SIGN < 0).  Built once per size by launch_twiddles().
+template <class C>
+struct TwPlan {
+    static constexpr int P2  = C::R1 * C::R2;
+    static constexpr int P3  = C::R3 > 1 ? C::R1 * C::R2 * C::R3 : 0;
+    static constexpr int LEN = P2 + P3;
+};
+
 // Barrier among the threads of one line.  With NAMED, lines of >= 32 threads
 // use named barrier 1 + li, so lines progress independently; this requires
 // every warp to belong to a single line (threads of one warp must not wait on
@@ -206,40 +219,18 @@ __device__ __forceinline__ void stockham_pass(float2* v, float2* buf, const floa
     }
     line_sync<C, NAMED>(li);
     if (!active) return;
+    // twiddle plan of this pass: entry r*NSN + k
+    const float2* T = NSP == 1 ? tw : tw + TwPlan<C>::P2;
+    static_assert(NSP == 1 ? NSN == C::R1 : NSN == C::R1 * C::R2, "plan layout");
 #pragma unroll
     for (int b = 0; b < C::R1 / RN; ++b) {
-        const int j    = t + b * C::G;
-        const int k    = j % NSN;
-        const int step = N / (NSN * RN);
-        if constexpr (RN <= 8) {
+        const int j = t + b * C::G;
+        const int k = j % NSN;
 #pragma unroll
-            for (int r = 1; r < RN; ++r) {
-                float2 w = tw[(k * r * step) & (N - 1)];
-                if (SIGN < 0) w.y = -w.y;
-                v[b * RN + r] = cmul(v[b * RN + r], w);
-            }
-        } else {
-            // W^{kr} = A[r mod 8] * B[r div 8]: 7 + RN/8 - 1 table reads instead of
-            // RN - 1, which keeps the live twiddle registers few (one extra
-            // rounding per twiddle)
-            float2 A[8], B[RN / 8];
-            A[0] = make_float2(1.0f, 0.0f);
-            B[0] = A[0];
-#pragma unroll
-            for (int i = 1; i < 8; ++i) {
-                A[i] = tw[(k * i * step) & (N - 1)];
-                if (SIGN < 0) A[i].y = -A[i].y;
-            }
-#pragma unroll
-            for (int i = 1; i < RN / 8; ++i) {
-                B[i] = tw[(k * 8 * i * step) & (N - 1)];
-                if (SIGN < 0) B[i].y = -B[i].y;
-            }
-#pragma unroll
-            for (int r = 1; r < RN; ++r) {
-                const float2 w = (r & 7) == 0 ? B[r >> 3] : ((r >> 3) == 0 ? A[r] : cmul(A[r & 7], B[r >> 3]));
-                v[b * RN + r] = cmul(v[b * RN + r], w);
-            }
+        for (int r = 1; r < RN; ++r) {
+            float2 w = T[r * NSN + k];
+            if (SIGN < 0) w.y = -w.y;
+            v[b * RN + r] = cmul(v[b * RN + r], w);
         }
         dft<RN, SIGN>(v + b * RN);
     }
@@ -248,8 +239,7 @@ __device__ __forceinline__ void stockham_pass(float2* v, float2* buf, const floa
 // Full line transform of line `li` (barrier id 1 + li, so li < 15; NAMED as
 // in line_sync).  On entry
 // v[r] = x[t + r*N/R1]; on exit v[b*RL + r] = X[(t + b*G) + r*(N/RL)] with RL
-// the last radix.  tw: N-entry table tw[i] = exp(+2*pi*i*i/N) (conjugated here
-// for SIGN < 0).  On return every thread of the line has finished reading
+// the last radix.  tw: the decomposition's twiddle plan (TwPlan<C>).  On return every thread of the line has finished reading
 // `buf`.  Threads with active == false do no work; for lines of >= 32 threads
 // they may skip the call entirely, for smaller lines they must call it (the
 // barrier is then the block's).

@@ -94,18 +94,12 @@ int check_device()
 
 int upload_twiddles(float2** d, int N)
 {
-    std::vector<float2> tw((size_t)N);
-    for (int k = 0; k < N; ++k) {
-        const double a = 2.0 * M_PI * (double)k / (double)N;
-        tw[k]          = make_float2((float)std::cos(a), (float)std::sin(a));
-    }
     cudaError_t e;
-    if ((e = cudaMalloc(d, N * sizeof(float2))) != cudaSuccess) {
+    if ((e = cudaMalloc(d, ocean::twiddle_len(N) * sizeof(float2))) != cudaSuccess) {
         *d = nullptr;
         return fail(OCEAN_ERR_NOMEM, std::string("device allocation failed: ") + cudaGetErrorString(e));
     }
-    if ((e = cudaMemcpy(*d, tw.data(), N * sizeof(float2), cudaMemcpyHostToDevice)) != cudaSuccess)
-        return cuda_fail(e, "twiddle upload");
+    if ((e = ocean::launch_twiddles(N, *d, 0)) != cudaSuccess) return cuda_fail(e, "twiddle plan launch");
     return OCEAN_OK;
 }
 

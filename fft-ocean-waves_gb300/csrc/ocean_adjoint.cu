@@ -50,7 +50,8 @@ struct AdjColCfg {
     static constexpr int THREADS = LINES * L::G;
     static constexpr int H       = N / 2 + 1;
     static constexpr int LS      = L::NPAD + 1;         // odd line stride: lines hit distinct banks
-    static constexpr size_t SMEM = sizeof(float2) * (N + (size_t)LINES * LS);
+    static constexpr int TW      = TwPlan<L>::LEN;
+    static constexpr size_t SMEM = sizeof(float2) * (TW + (size_t)LINES * LS);
 };
 
 template <int N>
@@ -61,8 +62,8 @@ __global__ void __launch_bounds__(AdjColCfg<N>::THREADS) k_adj_col_pass(AdjColAr
     constexpr int C = CF::C, H = CF::H, LS = CF::LS, WL = CF::WL, ZL = CF::ZL;
     extern __shared__ float2 smem[];
     float2* tw_s = smem;
-    float2* buf  = smem + N;
-    for (int i = threadIdx.x; i < N; i += CF::THREADS) tw_s[i] = a.tw[i];
+    float2* buf  = smem + CF::TW;
+    for (int i = threadIdx.x; i < CF::TW; i += CF::THREADS) tw_s[i] = a.tw[i];
 
     const int    x0 = blockIdx.x * C;
     const size_t NN = (size_t)N * N;
@@ -131,9 +132,10 @@ struct AdjRowCfg {
     static constexpr int THREADS = LINES * L::G;
     static constexpr int H       = N / 2 + 1;
     static constexpr int LS      = L::NPAD + 1;
-    // tw | line buffers | h0 rows [PAIRS][2][N] | accumulators [PAIRS][2][N];
+    static constexpr int TW      = TwPlan<L>::LEN;
+    // twiddle plan | line buffers | h0 rows [PAIRS][2][N] | accumulators [PAIRS][2][N];
     // the float4 arrays start on a 128-byte boundary (LS is odd, LINES may be)
-    static constexpr size_t F4OFF = ((size_t)(N + LINES * LS) + 15) / 16 * 16;   // in float2
+    static constexpr size_t F4OFF = ((size_t)(TW + LINES * LS) + 15) / 16 * 16;   // in float2
     static constexpr size_t SMEM  = sizeof(float2) * F4OFF + sizeof(float4) * 4 * (size_t)PAIRS * N + 128;
     static constexpr int GRID     = (H + PAIRS - 1) / PAIRS;
 };
@@ -161,13 +163,13 @@ __global__ void __launch_bounds__(AdjRowCfg<N>::THREADS) k_adj_row_pass(AdjRowAr
     extern __shared__ unsigned char smem_raw[];
     float2* smem = reinterpret_cast<float2*>((reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
     float2* tw_s = smem;
-    float2* buf  = smem + N;
+    float2* buf  = smem + CF::TW;
     float4* h0s  = reinterpret_cast<float4*>(smem + CF::F4OFF);          // [PAIRS][2][N], 128-byte aligned
     float4* acc  = h0s + 2 * PAIRS * N;                                // [PAIRS][2][N]
     __shared__ double red[32];
 
     const int tid = threadIdx.x;
-    for (int i = tid; i < N; i += CF::THREADS) tw_s[i] = a.tw[i];
+    for (int i = tid; i < CF::TW; i += CF::THREADS) tw_s[i] = a.tw[i];
     for (int i = tid; i < 2 * PAIRS * N; i += CF::THREADS) {
         const int pl = i / (2 * N), side = (i / N) & 1, x = i % N;
         const int yp = blockIdx.x * PAIRS + pl;

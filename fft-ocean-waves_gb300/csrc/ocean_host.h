@@ -21,7 +21,7 @@ H0Args h0_args(const ocean_params& p);
 uint64_t splitmix64_at(uint64_t seed, uint64_t i);
 
 int check_device();                                         // sm_103 or OCEAN_ERR_UNSUPPORTED
-int upload_twiddles(float2** d, int N);                     // cudaMalloc + fill exp(+2 pi i k/N)
+int upload_twiddles(float2** d, int N);                     // cudaMalloc + the twiddle plans (on stream 0)
 
 }  // namespace host
 }  // namespace ocean

@@ -67,7 +67,7 @@ struct RowArgs {
     const float2*      spec;
     const float4*      h0;
     float2*            inter;
-    const float2*      tw;      // [N] exp(+2*pi*i*k/N)
+    const float2*      tw;      // twiddle plans (launch_twiddles)
     unsigned*          status;  // device status word (bounded-wait time-outs)
     const FrameConsts* fcs;
     FrameConsts        fc0;
@@ -120,6 +120,10 @@ cudaError_t launch_adj_col(int N, int T, const AdjColArgs& a, cudaStream_t s);
 cudaError_t launch_adj_row(int N, const AdjRowArgs& a, cudaStream_t s);
 
 cudaError_t launch_h0(const H0Args& a, const float* noise, float4* h0, cudaStream_t s);
+// The twiddle plans of size N (row decomposition, then column decomposition;
+// TwPlan in fft_line.cuh): twiddle_len(N) complex values.
+size_t      twiddle_len(int N);
+cudaError_t launch_twiddles(int N, float2* tw, cudaStream_t s);
 cudaError_t launch_row_pass(int N, const RowArgs& a, cudaStream_t s);
 // spec[t] from h0[t] for `tiles` consecutive tiles of size N.
 cudaError_t launch_spec_combine(int N, int tiles, const float4* h0, int literal_conj, float2* spec, cudaStream_t s);

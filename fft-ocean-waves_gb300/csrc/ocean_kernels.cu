@@ -144,7 +144,8 @@ struct RowCfg {
     // line buffers [LINES][NPAD] (line inputs in natural order, then the FFT's exchanges)
     static constexpr size_t RING  = (size_t)STAGES * PAIRS * 2 * N * EW;
     static constexpr size_t WORK  = (size_t)LINES * L::NPAD;
-    static constexpr size_t SMEM  = sizeof(float2) * (N + RING + WORK) + 128;   // + base alignment slack
+    static constexpr int    TW    = TwPlan<L>::LEN;
+    static constexpr size_t SMEM  = sizeof(float2) * (TW + RING + WORK) + 128;   // + base alignment slack
     static constexpr uint32_t ROW_BYTES = (uint32_t)(N * EW * sizeof(float2));
 };
 
@@ -213,6 +214,43 @@ __device__ __forceinline__ void row_modes(const RowArgs& a, const float2* rA, co
     }
 }
 
+// Line inputs of row yp at the position pair (x, N-x) for the three fields:
+// the modes (x, yp), (N-x, yp), (N-x, N-yp), (x, N-yp) share |k| (ix^2 and iz^2
+// are even) and so the phase.  rows: the pair's two staged rows (yp, then
+// N-yp); lines: the three line buffers (Dx, Dy, Dz, NPAD apart).
+template <int N, bool FROM_H0, int NPAD>
+__device__ __forceinline__ void row_position(const RowArgs& a, const float2* rows, float2* lines, int tile, int x,
+                                             int yp, const FrameConsts& fc)
+{
+    constexpr int EW = FROM_H0 ? 2 : 1;
+    const int yq = (N - yp) & (N - 1), xm = (N - x) & (N - 1);
+    const int ix = x - N / 2, iz = yp - N / 2;
+    float c, sn, r;
+    mode_phase_r(ix * ix + iz * iz, fc, c, sn, r);
+    float2 g[4], d[4];
+    row_modes<N, FROM_H0>(a, rows, rows + N * EW, tile, x, xm, yp, yq, fc.literal_conj, g, d);
+    const float2 y0 = herm_sum(g[0], g[1], c, sn);
+    const float2 y1 = herm_sum(g[2], g[3], c, sn);
+    float2 ux0 = y0, uz0 = y0, uz1 = y1;
+    if (x == 0) ux0 = herm_diff(d[0], d[1], c, sn);
+    if (yp == 0) {
+        uz0 = herm_diff(d[0], d[1], c, sn);
+        uz1 = herm_diff(d[2], d[3], c, sn);
+    }
+    const float sx = (float)ix * r, sz = (float)iz * r;
+    float2* bx = lines;
+    float2* by = bx + NPAD;
+    float2* bz = by + NPAD;
+    bx[x] = mul_mi(sx, ux0);
+    by[x] = y0;
+    bz[x] = mul_mi(sz, uz0);
+    if (xm != x) {                        // ix(xm) = -ix for x != 0
+        bx[xm] = mul_mi(-sx, y1);
+        by[xm] = y1;
+        bz[xm] = mul_mi(sz, uz1);
+    }
+}
+
 // MULTI: more than one (tile, sample) unit per launch (batches).  The single
 // unit instantiation keeps the per-element constants out of a runtime sample
 // loop, which the compiler would otherwise hoist into registers.  FROM_H0: the
@@ -225,8 +263,8 @@ __global__ void __launch_bounds__(RowCfg<N, FROM_H0>::THREADS, RowCfg<N, FROM_H0
     extern __shared__ unsigned char smem_raw[];
     float2* smem = align_smem(smem_raw);
     float2* tw_s = smem;
-    float2* ring = smem + N;                                         // [STAGES][PAIRS][2][N*EW]
-    float2* work = smem + N + RC::RING;                              // line buffers
+    float2* ring = smem + RC::TW;                                    // [STAGES][PAIRS][2][N*EW]
+    float2* work = ring + RC::RING;                                  // line buffers
     __shared__ __align__(8) uint64_t bars[RC::STAGES];
     __shared__ int wait_ok;
 
@@ -240,7 +278,7 @@ __global__ void __launch_bounds__(RowCfg<N, FROM_H0>::THREADS, RowCfg<N, FROM_H0
         for (int s = 0; s < RC::STAGES; ++s) {
             const int item = blockIdx.x + s * gridDim.x;
             if (item >= n_items) break;
-            const uint32_t twb = s == 0 ? (uint32_t)(N * sizeof(float2)) : 0u;
+            const uint32_t twb = s == 0 ? (uint32_t)(RC::TW * sizeof(float2)) : 0u;
             row_issue<N, FROM_H0>(a, ring + (size_t)s * RC::PAIRS * 2 * N * RC::EW, &bars[s], item, twb);
             if (twb) bulk_g2s(tw_s, a.tw, twb, &bars[0]);
         }
@@ -272,37 +310,11 @@ __global__ void __launch_bounds__(RowCfg<N, FROM_H0>::THREADS, RowCfg<N, FROM_H0
             // share |k| (ix^2 and iz^2 are even) and so the phase.
             constexpr int HX = N / 2 + 1;
             for (int i = tid; i < RC::PAIRS * HX; i += RC::THREADS) {
-                const int pl = i / HX, x = i - pl * HX;
+                const int pl = RC::PAIRS == 1 ? 0 : i / HX, x = i - pl * HX;
                 const int yp = pi * RC::PAIRS + pl;
-                if (yp > N / 2) continue;
-                const int yq = (N - yp) & (N - 1), xm = (N - x) & (N - 1);
-                const int ix = x - N / 2, iz = yp - N / 2;
-                float c, sn, r;
-                mode_phase_r(ix * ix + iz * iz, fc, c, sn, r);
-                float2 g[4], d[4];
-                const float2* rA = stage + (pl * 2 + 0) * N * RC::EW;
-                const float2* rB = stage + (pl * 2 + 1) * N * RC::EW;
-                row_modes<N, FROM_H0>(a, rA, rB, tile, x, xm, yp, yq, fc.literal_conj, g, d);
-                const float2 y0 = herm_sum(g[0], g[1], c, sn);
-                const float2 y1 = herm_sum(g[2], g[3], c, sn);
-                float2 ux0 = y0, uz0 = y0, uz1 = y1;
-                if (x == 0) ux0 = herm_diff(d[0], d[1], c, sn);
-                if (yp == 0) {
-                    uz0 = herm_diff(d[0], d[1], c, sn);
-                    uz1 = herm_diff(d[2], d[3], c, sn);
-                }
-                const float sx = (float)ix * r, sz = (float)iz * r;
-                float2* bx = work + (pl * 3 + 0) * L::NPAD;
-                float2* by = bx + L::NPAD;
-                float2* bz = by + L::NPAD;
-                bx[x] = mul_mi(sx, ux0);
-                by[x] = y0;
-                bz[x] = mul_mi(sz, uz0);
-                if (xm != x) {                        // ix(xm) = -ix for x != 0
-                    bx[xm] = mul_mi(-sx, y1);
-                    by[xm] = y1;
-                    bz[xm] = mul_mi(sz, uz1);
-                }
+                if (RC::PAIRS > 1 && yp > N / 2) continue;
+                row_position<N, FROM_H0, L::NPAD>(a, stage + (pl * 2) * N * RC::EW, work + (pl * 3) * L::NPAD, tile,
+                                                  x, yp, fc);
             }
             __syncthreads();                               // line inputs complete
             if (smp == nsmp - 1 && tid == 0) {             // ring stage consumed: refill it
@@ -338,6 +350,137 @@ __global__ void __launch_bounds__(RowCfg<N, FROM_H0>::THREADS, RowCfg<N, FROM_H0
 }
 
 // ---------------------------------------------------------------------------
+// Warp-specialised row pass (lines of whole warps, N >= 512).  The three
+// line FFTs of a job (row pair x time sample) run on 3*G "transform" threads
+// while 128 "prepass" threads compute the next job's line inputs into the
+// other of two line-buffer sets; each set is the inputs, then the FFT's
+// exchange space.  Hand-off by named barriers: FULL[b] (prepass arrives,
+// transform waits) and EMPTY[b] (transform arrives, prepass waits before
+// refilling set b).  Both sides walk the same job sequence and execute the
+// same number of barrier operations whatever happens, so a timed-out copy
+// wait (flagged in the status word) never leaves a warp waiting.
+// ---------------------------------------------------------------------------
+template <int N, bool FROM_H0>
+struct RowWsCfg {
+    using L = typename LineFor<N>::type;
+    static_assert(L::G >= 32 && L::G % 32 == 0, "lines of whole warps");
+    static constexpr int FFT_THREADS = 3 * L::G;
+    static constexpr int PRE_THREADS = 128;
+    static constexpr int THREADS     = FFT_THREADS + PRE_THREADS;
+    static constexpr int ITEMS       = N / 2 + 1;   // row pairs per tile
+    static constexpr int STAGES      = 2;
+    static constexpr int EW          = FROM_H0 ? 2 : 1;
+    static constexpr size_t RING     = (size_t)STAGES * 2 * N * EW;
+    static constexpr size_t BUF      = (size_t)3 * L::NPAD;   // one job's three line buffers
+    static constexpr int    TW       = TwPlan<L>::LEN;
+    static constexpr size_t SMEM     = sizeof(float2) * (TW + RING + 2 * BUF) + 128;
+    static constexpr int MINB        = 65536 / (THREADS * 96) < 1 ? 1 : 65536 / (THREADS * 96);
+    static constexpr int BAR_FULL = 4, BAR_EMPTY = 6, BAR_PRE = 8;   // named barriers (lines use 1..3)
+};
+
+__device__ __forceinline__ void named_sync(int id, int count)
+{
+    asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(count) : "memory");
+}
+__device__ __forceinline__ void named_arrive(int id, int count)
+{
+    asm volatile("bar.arrive %0, %1;" ::"r"(id), "r"(count) : "memory");
+}
+
+template <int N, bool MULTI, bool FROM_H0>
+__global__ void __launch_bounds__(RowWsCfg<N, FROM_H0>::THREADS, RowWsCfg<N, FROM_H0>::MINB) k_row_ws(RowArgs a)
+{
+    using WC = RowWsCfg<N, FROM_H0>;
+    using L  = typename WC::L;
+    extern __shared__ unsigned char smem_raw[];
+    float2* smem = align_smem(smem_raw);
+    float2* tw_s = smem;
+    float2* ring = smem + WC::TW;                            // [STAGES][2 rows][N*EW]
+    float2* bufs = ring + WC::RING;                          // [2][3 lines][NPAD]
+    __shared__ __align__(8) uint64_t bars[WC::STAGES];
+    __shared__ int wait_ok;
+
+    const int tid     = threadIdx.x;
+    const int n_items = a.tiles * WC::ITEMS;
+    const int nsmp    = MULTI ? a.S : 1;
+    const int n_jobs  = (n_items - (int)blockIdx.x + (int)gridDim.x - 1) / (int)gridDim.x * nsmp;
+    if (tid == 0) {
+        for (int s = 0; s < WC::STAGES; ++s) mbar_init(&bars[s], 1);
+        fence_mbar_init();
+        for (int s = 0; s < WC::STAGES; ++s) {
+            const int item = blockIdx.x + s * gridDim.x;
+            if (item >= n_items) break;
+            const uint32_t twb = s == 0 ? (uint32_t)(WC::TW * sizeof(float2)) : 0u;
+            row_issue<N, FROM_H0>(a, ring + (size_t)s * 2 * N * WC::EW, &bars[s], item, twb);
+            if (twb) bulk_g2s(tw_s, a.tw, twb, &bars[0]);
+        }
+        wait_ok = 1;
+    }
+    __syncthreads();
+    pdl_launch_dependents();
+
+    if (tid < WC::FFT_THREADS) {
+        const int li = tid / L::G, t = tid % L::G;           // line = field 0: Dx, 1: Dy, 2: Dz
+        for (int j = 0; j < n_jobs; ++j) {
+            const int b = j & 1, ki = j / nsmp, smp = j - ki * nsmp;
+            const int item = blockIdx.x + ki * gridDim.x, tile = item / WC::ITEMS, yp = item % WC::ITEMS;
+            const int unit = MULTI ? tile * a.S + smp : 0;
+            named_sync(WC::BAR_FULL + b, WC::THREADS);       // the job's line inputs are complete
+            float2* buf = bufs + b * WC::BUF + li * L::NPAD;
+            float2  v[L::E];
+#pragma unroll
+            for (int r = 0; r < L::E; ++r) v[r] = buf[t + r * L::G];
+            line_sync<L, true>(li);
+            line_fft<L, +1>(v, buf, tw_s, t, li);
+            named_arrive(WC::BAR_EMPTY + b, WC::THREADS);    // every thread of the line is done with buf
+            static_assert(L::G % 2 == 0 && LineOut<L>::NS % 2 == 0, "even output offsets");
+            float2* out = a.inter + (size_t)unit * inter_len(N) + inter_index(N, li, t, yp);
+#pragma unroll
+            for (int e = 0; e < L::E; ++e) out[(size_t)(LineOut<L>::pos(0, e) >> 1) * (2 * inter_rows(N))] = v[e];
+        }
+    } else {
+        const int pt = tid - WC::FFT_THREADS;
+        uint32_t  phase_bits = 0;
+        bool      gave_up    = false;                         // a copy wait timed out: stop waiting
+        for (int j = 0; j < n_jobs; ++j) {
+            const int b = j & 1, ki = j / nsmp, smp = j - ki * nsmp;
+            const int item = blockIdx.x + ki * gridDim.x, tile = item / WC::ITEMS, yp = item % WC::ITEMS;
+            const int st = ki % WC::STAGES;
+            float2* stage = ring + (size_t)st * 2 * N * WC::EW;
+            if (smp == 0) {                                  // the item's rows (and, first, the twiddles)
+                if (pt == 0 && !gave_up) {
+                    if (!mbar_wait_bounded(&bars[st], (phase_bits >> st) & 1u)) {
+                        atomicOr(a.status, kDeviceTimeout);
+                        (void)mbar_wait_bounded(&bars[st], (phase_bits >> st) & 1u);
+                        wait_ok = 0;
+                    }
+                }
+                phase_bits ^= 1u << st;
+                named_sync(WC::BAR_PRE, WC::PRE_THREADS);
+                gave_up = wait_ok == 0;
+            }
+            if (j >= 2) named_sync(WC::BAR_EMPTY + b, WC::THREADS);   // set b's previous job is transformed
+            const FrameConsts fc = MULTI ? a.fcs[tile * a.S + smp] : a.fc0;
+            for (int x = pt; x <= N / 2; x += WC::PRE_THREADS)
+                row_position<N, FROM_H0, L::NPAD>(a, stage, bufs + b * WC::BUF, tile, x, yp, fc);
+            named_arrive(WC::BAR_FULL + b, WC::THREADS);
+            if (smp == nsmp - 1) {                           // every prepass thread is done with the stage
+                named_sync(WC::BAR_PRE, WC::PRE_THREADS);
+                if (pt == 0) {
+                    const int next = item + WC::STAGES * gridDim.x;
+                    if (next < n_items) {
+                        fence_proxy_async_smem();
+                        row_issue<N, FROM_H0>(a, stage, &bars[st], next);
+                    }
+                }
+            }
+        }
+        // the transform side's last arrivals on EMPTY
+        for (int j = n_jobs - 2 > 0 ? n_jobs - 2 : 0; j < n_jobs; ++j) named_sync(WC::BAR_EMPTY + (j & 1), WC::THREADS);
+    }
+}
+
+// ---------------------------------------------------------------------------
 // Column transforms.
 // ---------------------------------------------------------------------------
 // Column line decomposition: as LineFor except at N = 2048, where 64 threads
@@ -356,7 +499,9 @@ struct ColCfg {
     // the staged intermediate [3][PAIRS][H][2] shares the line buffers
     static constexpr size_t TILE = (size_t)3 * PAIRS * H * 2;
     static constexpr size_t WORK = (size_t)LINES * L::NPAD > TILE ? (size_t)LINES * L::NPAD : TILE;
-    static constexpr size_t SMEM = sizeof(float2) * (N + WORK) + 128;
+    static constexpr int    TW   = TwPlan<L>::LEN;
+    static constexpr int    TW0  = TwPlan<typename LineFor<N>::type>::LEN;   // the row plan precedes it
+    static constexpr size_t SMEM = sizeof(float2) * (TW + WORK) + 128;
     static constexpr uint32_t FIELD_BYTES = (uint32_t)(sizeof(float2) * PAIRS * H * 2);
     static_assert((N / 2) % PAIRS == 0, "column pairs per CTA");
     static_assert(FIELD_BYTES % 16 == 0, "bulk copy size");
@@ -376,17 +521,20 @@ __global__ void __launch_bounds__(ColCfg<N>::THREADS) k_col_fft(const __grid_con
     extern __shared__ unsigned char smem_raw[];
     float2* smem = align_smem(smem_raw);
     float2* tw_s = smem;
-    float2* work = smem + N;                                 // staged tile, then line buffers
-    __shared__ __align__(8) uint64_t bar;
+    float2* work = smem + CF::TW;                            // staged tile, then line buffers
+    __shared__ __align__(8) uint64_t bar, bar_tw;
     __shared__ int wait_ok;
     const int      tid  = threadIdx.x;
     const int      unit = blockIdx.y;
     const ColUnit* cu   = a.units ? a.units + unit : &a.u0;
     if (tid == 0) {
         mbar_init(&bar, 1);
+        mbar_init(&bar_tw, 1);
         fence_mbar_init();
+        // the twiddle plan does not depend on the row pass: fetch it now
+        mbar_arrive_expect_tx(&bar_tw, CF::TW * sizeof(float2));
+        bulk_g2s(tw_s, a.tw + CF::TW0, CF::TW * sizeof(float2), &bar_tw);
     }
-    for (int i = tid; i < N; i += CF::THREADS) tw_s[i] = a.tw[i];
     pdl_wait_prior();                                        // the row pass has finished
     __syncthreads();
     const int pair0 = blockIdx.x * CF::PAIRS;
@@ -427,7 +575,7 @@ __global__ void __launch_bounds__(ColCfg<N>::THREADS) k_col_fft(const __grid_con
         if (cj) { p.y = -p.y; q.y = -q.y; }
         v[r] = make_float2(p.x - q.y, p.y + q.x);                          // p + i*q
     }
-    __syncthreads();                                         // the tile is consumed: line buffers reuse it
+    if (!block_wait(&bar_tw, 0, &wait_ok, a.status)) return;   // also: the tile is consumed
     pdl_launch_dependents();                                 // k_col_out may start its set-up
     line_fft<L, +1>(v, work + li * L::NPAD, tw_s, t, li);
 
@@ -466,75 +614,151 @@ constexpr int kOutT  = 32;             // tile edge
 constexpr int kOutW  = kOutT + 2;      // with halo
 constexpr int kOutP  = kOutT + 3;      // shared pitch: odd, so column-wise reads are conflict-free
 constexpr int kOutTh = 256;
+constexpr int kOutRows = kOutT * kOutT / kOutTh;   // rows per thread (one column, consecutive rows)
 
 template <int N>
-__global__ void __launch_bounds__(kOutTh) k_col_out(const __grid_constant__ ColArgs a)
+__global__ void __launch_bounds__(kOutTh, 5) k_col_out(const __grid_constant__ ColArgs a)
 {
-    __shared__ float S[3][kOutW][kOutP];                     // [field][x][y]: Dx, Dy, Dz
+    __shared__ float S[3][kOutW][kOutP];                     // [field][x][y]: Dx, Dy, Dz; index = coordinate - origin + 1
     const int      unit = blockIdx.z;
     const int      x0 = blockIdx.x * kOutT, y0 = blockIdx.y * kOutT;
     const ColUnit* cu = a.units ? a.units + unit : &a.u0;
-    float* const   odx = cu->dx;
-    float* const   ody = cu->dy;
-    float* const   odz = cu->dz;
-    float4* const  onj = cu->nj;
-    const float    inv2d = cu->inv2d;
     const float*   tm = a.tmap + (size_t)unit * tmap_len(N);
+    const int      tid = threadIdx.x;
     pdl_wait_prior();                                        // the column transforms have finished
-    // One warp per staged column (field f, column xx): lane l loads row
-    // y0-1+l, and the two last rows of the warp's columns are spread over the
-    // lanes (lane l: column l/2, row y0+31+(l&1)).  Every load of a thread is
-    // issued before its first shared-memory store.
-    constexpr int NCOL = 3 * kOutW, WARPS = kOutTh / 32, PER = (NCOL + WARPS - 1) / WARPS;
-    static_assert(2 * PER <= 32, "edge rows: one per lane");
-    const int lane = threadIdx.x % 32, warp = threadIdx.x / 32;
-    float     body[PER], edge = 0.0f;
+
+    // Stage the maps: each of the 3 x 34 columns (field f, x = x0-1 .. x0+32)
+    // is rows y0 .. y0+31 (eight aligned 16-byte pieces) plus the halo rows
+    // y0-1 and y0+32.  All loads of a thread are issued before its stores.
+    constexpr int NCOL = 3 * kOutW, NPC = NCOL * 8, NV = (NPC + kOutTh - 1) / kOutTh;
+    float4 body[NV];
 #pragma unroll
-    for (int j = 0; j < PER; ++j) {
-        const int c = warp + WARPS * j;                          // warp-uniform
-        if (c < NCOL) {
-            const int f = c / kOutW, xx = c - f * kOutW;
-            body[j] = tm[((size_t)f * N + ((x0 - 1 + xx) & (N - 1))) * N + ((y0 - 1 + lane) & (N - 1))];
+    for (int j = 0; j < NV; ++j) {
+        const int i = tid + j * kOutTh;                      // piece i: column i/8, rows y0 + 4*(i%8) ..
+        if (i < NPC) {
+            const int c = i >> 3, f = c / kOutW, xx = c - f * kOutW;
+            body[j] = *reinterpret_cast<const float4*>(tm + ((size_t)f * N + ((x0 - 1 + xx) & (N - 1))) * N + y0 +
+                                                       4 * (i & 7));
         }
     }
-    const int ce = warp + WARPS * (lane >> 1);
-    const int fe = ce / kOutW, xe = ce - fe * kOutW;
-    if (lane < 2 * PER && ce < NCOL)
-        edge = tm[((size_t)fe * N + ((x0 - 1 + xe) & (N - 1))) * N + ((y0 + 31 + (lane & 1)) & (N - 1))];
+    float edge[(2 * NCOL + kOutTh - 1) / kOutTh];
 #pragma unroll
-    for (int j = 0; j < PER; ++j) {
-        const int c = warp + WARPS * j;
-        if (c < NCOL) {
-            const int f = c / kOutW, xx = c - f * kOutW;
-            S[f][xx][lane] = body[j];
+    for (int j = 0; j < (2 * NCOL + kOutTh - 1) / kOutTh; ++j) {
+        const int i = tid + j * kOutTh;                      // halo value i: column i/2, row y0-1 or y0+32
+        if (i < 2 * NCOL) {
+            const int c = i >> 1, f = c / kOutW, xx = c - f * kOutW;
+            const int y = (i & 1) ? (y0 + kOutT) & (N - 1) : (y0 - 1) & (N - 1);
+            edge[j] = tm[((size_t)f * N + ((x0 - 1 + xx) & (N - 1))) * N + y];
         }
     }
-    if (lane < 2 * PER && ce < NCOL) S[fe][xe][32 + (lane & 1)] = edge;
+#pragma unroll
+    for (int j = 0; j < NV; ++j) {
+        const int i = tid + j * kOutTh;
+        if (i < NPC) {
+            const int c = i >> 3, f = c / kOutW, xx = c - f * kOutW, yy = 1 + 4 * (i & 7);
+            S[f][xx][yy]     = body[j].x;
+            S[f][xx][yy + 1] = body[j].y;
+            S[f][xx][yy + 2] = body[j].z;
+            S[f][xx][yy + 3] = body[j].w;
+        }
+    }
+#pragma unroll
+    for (int j = 0; j < (2 * NCOL + kOutTh - 1) / kOutTh; ++j) {
+        const int i = tid + j * kOutTh;
+        if (i < 2 * NCOL) {
+            const int c = i >> 1, f = c / kOutW, xx = c - f * kOutW;
+            S[f][xx][(i & 1) ? kOutT + 1 : 0] = edge[j];
+        }
+    }
     __syncthreads();
-    const int xx = threadIdx.x % kOutT + 1;
+
+    // Four consecutive rows of one column per thread; a warp covers 32
+    // consecutive columns, so every store is a full line.  Rows yy-1 .. yy+4
+    // of the three columns around xx are read once and shared by the four
+    // texels.
+    const int xx = tid % kOutT + 1;                          // staged column of output x0 + xx - 1
+    const int yb = (tid / kOutT) * kOutRows;                 // first output row - y0
+    float C0[kOutRows + 2], C1[kOutRows + 2], C2[kOutRows + 2];   // Dy at xx-1, xx, xx+1
+    float Xm[kOutRows], Xp[kOutRows], Zm[kOutRows], Zp[kOutRows];  // Dx, Dz at xx-1 and xx+1
+    float Xc[kOutRows + 2], Zc[kOutRows + 2];                       // Dx, Dz at xx
 #pragma unroll
-    for (int j = 0; j < kOutT * kOutT / kOutTh; ++j) {
-        const int yy = threadIdx.x / kOutT + j * (kOutTh / kOutT) + 1;
-        // taps z0..z7 (normal_map_cs.glsl:37-44): z0 = (x-1, y-1), z1 = (x, y-1), ...
-        const float z0 = S[1][xx - 1][yy - 1], z1 = S[1][xx][yy - 1], z2 = S[1][xx + 1][yy - 1];
-        const float z3 = S[1][xx - 1][yy], z4 = S[1][xx + 1][yy];
-        const float z5 = S[1][xx - 1][yy + 1], z6 = S[1][xx][yy + 1], z7 = S[1][xx + 1][yy + 1];
+    for (int k = 0; k < kOutRows + 2; ++k) {
+        C0[k] = S[1][xx - 1][yb + k];
+        C1[k] = S[1][xx][yb + k];
+        C2[k] = S[1][xx + 1][yb + k];
+        Xc[k] = S[0][xx][yb + k];
+        Zc[k] = S[2][xx][yb + k];
+    }
+#pragma unroll
+    for (int k = 0; k < kOutRows; ++k) {
+        Xm[k] = S[0][xx - 1][yb + k + 1];
+        Xp[k] = S[0][xx + 1][yb + k + 1];
+        Zm[k] = S[2][xx - 1][yb + k + 1];
+        Zp[k] = S[2][xx + 1][yb + k + 1];
+    }
+    float* const  odx = cu->dx;
+    float* const  ody = cu->dy;
+    float* const  odz = cu->dz;
+    float4* const onj = cu->nj;
+    const float   inv2d = cu->inv2d;
+    const size_t  o0 = (size_t)(y0 + yb) * N + x0 + xx - 1;
+#pragma unroll
+    for (int k = 0; k < kOutRows; ++k) {
+        // taps z0..z7 (normal_map_cs.glsl:37-44): z0 = (x-1, y-1), z1 = (x, y-1),
+        // z2 = (x+1, y-1), z3 = (x-1, y), z4 = (x+1, y), z5..z7 the row below
+        const float z0 = C0[k], z1 = C1[k], z2 = C2[k], z3 = C0[k + 1], z4 = C2[k + 1];
+        const float z5 = C0[k + 2], z6 = C1[k + 2], z7 = C2[k + 2];
         const float nz = z0 + 2.0f * z1 + z2 - z5 - 2.0f * z6 - z7;
         const float nx = z0 + 2.0f * z3 + z5 - z2 - 2.0f * z4 - z7;
         const float rn = rsqrtf(nx * nx + 1.0f + nz * nz);
-        const float dxx = (S[0][xx + 1][yy] - S[0][xx - 1][yy]) * inv2d;
-        const float dxz = (S[0][xx][yy + 1] - S[0][xx][yy - 1]) * inv2d;
-        const float dzx = (S[2][xx + 1][yy] - S[2][xx - 1][yy]) * inv2d;
-        const float dzz = (S[2][xx][yy + 1] - S[2][xx][yy - 1]) * inv2d;
+        const float dxx = (Xp[k] - Xm[k]) * inv2d;
+        const float dxz = (Xc[k + 2] - Xc[k]) * inv2d;
+        const float dzx = (Zp[k] - Zm[k]) * inv2d;
+        const float dzz = (Zc[k + 2] - Zc[k]) * inv2d;
         // J = (1 - dxx)(1 - dzz) - dxz*dzx, formed as 1 + deviation so that the
         // only rounding at the scale of 1 is the final add
         const float  dJ = (dxx * dzz - dxz * dzx) - dxx - dzz;
-        const size_t o  = (size_t)(y0 + yy - 1) * N + x0 + xx - 1;
-        odx[o] = S[0][xx][yy];
-        ody[o] = S[1][xx][yy];
-        odz[o] = S[2][xx][yy];
+        const size_t o  = o0 + (size_t)k * N;
+        odx[o] = Xc[k + 1];
+        ody[o] = C1[k + 1];
+        odz[o] = Zc[k + 1];
         onj[o] = make_float4(nx * rn, rn, nz * rn, 1.0f + dJ);
     }
+}
+
+// ---------------------------------------------------------------------------
+// Twiddle plans: the row decomposition's, then the column decomposition's.
+// ---------------------------------------------------------------------------
+template <class C>
+__device__ float2 plan_entry(int i)
+{
+    constexpr int P2 = TwPlan<C>::P2;
+    long e;                                                   // exponent of W_N
+    if (i < P2) {
+        e = (long)(i % C::R1) * (i / C::R1) * (C::N / (C::R1 * C::R2));
+    } else {
+        i -= P2;
+        e = (long)(i % P2) * (i / P2);
+    }
+    double sn, cs;
+    sincospi(2.0 * (double)(e % C::N) / (double)C::N, &sn, &cs);
+    return make_float2((float)cs, (float)sn);
+}
+
+template <int N>
+__global__ void k_twiddles(float2* __restrict__ tw)
+{
+    using LR = typename LineFor<N>::type;
+    using LC = typename ColLineFor<N>::type;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < TwPlan<LR>::LEN) tw[i] = plan_entry<LR>(i);
+    else if (i < TwPlan<LR>::LEN + TwPlan<LC>::LEN) tw[i] = plan_entry<LC>(i - TwPlan<LR>::LEN);
+}
+
+template <int N>
+static size_t twiddle_len_n()
+{
+    return (size_t)TwPlan<typename LineFor<N>::type>::LEN + TwPlan<typename ColLineFor<N>::type>::LEN;
 }
 
 // ---------------------------------------------------------------------------
@@ -577,15 +801,44 @@ static cudaError_t row_pass_nm(const RowArgs& a, cudaStream_t s)
     return cudaGetLastError();
 }
 
+template <int N, bool MULTI, bool FROM_H0>
+static cudaError_t row_ws_nm(const RowArgs& a, cudaStream_t s)
+{
+    using WC = RowWsCfg<N, FROM_H0>;
+    static int grid = 0;   // resident CTAs per SM x SMs
+    if (!grid) {
+        cudaError_t e = cudaFuncSetAttribute(k_row_ws<N, MULTI, FROM_H0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)WC::SMEM);
+        if (e != cudaSuccess) return e;
+        int per_sm = 0, dev = 0, sms = 0;
+        if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_row_ws<N, MULTI, FROM_H0>, WC::THREADS,
+                                                                WC::SMEM)) != cudaSuccess)
+            return e;
+        if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
+        if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
+        if (per_sm < 1) return cudaErrorInvalidConfiguration;
+        grid = per_sm * sms;
+    }
+    const int items = a.tiles * WC::ITEMS;
+    k_row_ws<N, MULTI, FROM_H0><<<grid < items ? grid : items, WC::THREADS, WC::SMEM, s>>>(a);
+    return cudaGetLastError();
+}
+
 template <int N>
 static cudaError_t row_pass_n(const RowArgs& a, cudaStream_t s)
 {
-    if (!a.spec) {   // h0 input: single unit only
-        if (a.tiles != 1 || a.S != 1 || a.fcs) return cudaErrorInvalidValue;
-        return row_pass_nm<N, false, true>(a, s);
+    const bool single = a.tiles == 1 && a.S == 1 && !a.fcs;
+    if (!a.spec && !single) return cudaErrorInvalidValue;    // h0 input: single unit only
+    if constexpr (LineFor<N>::type::G >= 32) {                // lines of whole warps: warp-specialised
+        if (!a.spec) {
+            if constexpr (N <= 1024) return row_ws_nm<N, false, true>(a, s);
+            else return cudaErrorInvalidValue;                // its staged h0 rows would not fit
+        }
+        return single ? row_ws_nm<N, false, false>(a, s) : row_ws_nm<N, true, false>(a, s);
+    } else {
+        if (!a.spec) return row_pass_nm<N, false, true>(a, s);
+        return single ? row_pass_nm<N, false, false>(a, s) : row_pass_nm<N, true, false>(a, s);
     }
-    return (a.tiles == 1 && a.S == 1 && !a.fcs) ? row_pass_nm<N, false, false>(a, s)
-                                                : row_pass_nm<N, true, false>(a, s);
 }
 
 static cudaLaunchAttribute pdl_attr()
@@ -631,6 +884,29 @@ static cudaError_t col_out_n(int units, const ColArgs& a, cudaStream_t s, bool p
 }
 
 #define OCEAN_FOR_EACH_N(M) M(32) M(64) M(128) M(256) M(512) M(1024) M(2048)
+
+size_t twiddle_len(int N)
+{
+    switch (N) {
+#define CASE(n) case n: return twiddle_len_n<n>();
+        OCEAN_FOR_EACH_N(CASE)
+#undef CASE
+    default: return 0;
+    }
+}
+
+cudaError_t launch_twiddles(int N, float2* tw, cudaStream_t s)
+{
+    const size_t n = twiddle_len(N);
+    if (!n) return cudaErrorInvalidValue;
+    switch (N) {
+#define CASE(n_) case n_: k_twiddles<n_><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(tw); break;
+        OCEAN_FOR_EACH_N(CASE)
+#undef CASE
+    default: return cudaErrorInvalidValue;
+    }
+    return cudaGetLastError();
+}
 
 cudaError_t launch_row_pass(int N, const RowArgs& a, cudaStream_t s)
 {

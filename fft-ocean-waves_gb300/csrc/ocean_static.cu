@@ -38,7 +38,8 @@ static_assert(kStaticInterLen * 8 + kStaticTmapLen * 4 == 25190400, "documented 
 // table, device status word.
 static __device__ __align__(256) float2   g_static_inter[kStaticInterLen];
 static __device__ __align__(256) float    g_static_tmap[kStaticTmapLen];
-static __device__ __align__(256) float2   g_static_tw[kStaticMaxN];
+constexpr size_t kStaticTwLen    = 2560;   // twiddle plans of N = 1024, the largest needed
+static __device__ __align__(256) float2   g_static_tw[kStaticTwLen];
 static __device__ __align__(256) unsigned g_static_status;
 
 constexpr int kMaxDevices = 64;
@@ -52,15 +53,6 @@ struct DeviceScratch {
     int         tw_N    = 0;         // N whose twiddles the table holds
 };
 
-// exp(+2*pi*i*k/N) for k < N, from double-precision sincospi.
-__global__ void k_static_twiddles(float2* tw, int N)
-{
-    const int k = blockIdx.x * blockDim.x + threadIdx.x;
-    if (k >= N) return;
-    double sn, cs;
-    sincospi(2.0 * (double)k / (double)N, &sn, &cs);
-    tw[k] = make_float2((float)cs, (float)sn);
-}
 
 std::mutex    g_mu;
 DeviceScratch g_dev[kMaxDevices];
@@ -114,8 +106,8 @@ extern "C" int ocean_update_noalloc(const ocean_params* params, const float* h0_
     DeviceScratch&              d = g_dev[dev];
     if (!d.ready && (rc = setup(dev, d, s)) != OCEAN_OK) return rc;
     if (d.tw_N != N) {                 // the table holds another size's twiddles
-        k_static_twiddles<<<(N + 255) / 256, 256, 0, s>>>(d.tw, N);
-        if ((e = cudaGetLastError()) != cudaSuccess) return cuda_fail(e, "static twiddle launch");
+        if (ocean::twiddle_len(N) > kStaticTwLen) return fail(OCEAN_ERR_UNSUPPORTED, "twiddle plan exceeds its static array");
+        if ((e = ocean::launch_twiddles(N, d.tw, s)) != cudaSuccess) return cuda_fail(e, "static twiddle launch");
         d.tw_N = N;
     }
 
