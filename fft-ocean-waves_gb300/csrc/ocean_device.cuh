@@ -18,6 +18,33 @@ namespace ocean {
 // number of cycles is dropped before sincospi, so the reduced phase keeps
 // ~1e-7 absolute accuracy while K*t*m^(1/4) stays below ~2^20 cycles.
 // ---------------------------------------------------------------------------
+// sin and cos of 2*pi*f for |f| <= 1/2: the quadrant q = rint(4f) is split
+// off exactly (g = f - q/4, |g| <= 1/8), theta = 2*pi*g (|theta| <= pi/4), and
+// sin/cos theta are their Taylor series to theta^9 / theta^10 (truncation
+// below 2e-9 on the octant), Horner-evaluated with FMA; the quadrant rotates
+// the result.  Max abs error ~8e-8 against double (FP32 rounding level).
+__device__ __forceinline__ void sincos_2pi(float f, float& s, float& c)
+{
+    const float q  = rintf(4.0f * f);
+    const float g  = __fmaf_rn(-0.25f, q, f);                 // exact
+    const float th = 6.28318530717958648f * g;
+    const float t2 = th * th;
+    float ps = __fmaf_rn(t2, 1.0f / 362880.0f, -1.0f / 5040.0f);
+    ps       = __fmaf_rn(t2, ps, 1.0f / 120.0f);
+    ps       = __fmaf_rn(t2, ps, -1.0f / 6.0f);
+    const float sn = __fmaf_rn(th, t2 * ps, th);
+    float pc = __fmaf_rn(t2, -1.0f / 3628800.0f, 1.0f / 40320.0f);
+    pc       = __fmaf_rn(t2, pc, -1.0f / 720.0f);
+    pc       = __fmaf_rn(t2, pc, 1.0f / 24.0f);
+    pc       = __fmaf_rn(t2, pc, -0.5f);
+    const float cs = __fmaf_rn(t2, pc, 1.0f);
+    const int   qi = (int)q & 3;
+    s = (qi & 1) ? cs : sn;
+    c = (qi & 1) ? sn : cs;
+    if (qi == 1 || qi == 2) c = -c;
+    if (qi >= 2) s = -s;
+}
+
 // cos/sin of the phase of mode m at the frame's time, and r = 1/sqrt(m)
 // (0 for m = 0) to the accuracy of rsqrtf.
 __device__ __forceinline__ void mode_phase_r(int m, const FrameConsts& fc, float& c, float& s, float& r)
@@ -42,7 +69,7 @@ __device__ __forceinline__ void mode_phase_r(int m, const FrameConsts& fc, float
         f               = __fadd_rn(f, -rintf(f));
         r               = r1;
     }
-    sincospif(2.0f * f, &s, &c);
+    sincos_2pi(f, s, c);
 }
 
 __device__ __forceinline__ void mode_phase(int m, const FrameConsts& fc, float& c, float& s)

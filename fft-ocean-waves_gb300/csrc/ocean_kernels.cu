@@ -365,7 +365,7 @@ struct RowWsCfg {
     using L = typename LineFor<N>::type;
     static_assert(L::G >= 32 && L::G % 32 == 0, "lines of whole warps");
     static constexpr int FFT_THREADS = 3 * L::G;
-    static constexpr int PRE_THREADS = 128;
+    static constexpr int PRE_THREADS = N >= 2048 ? 256 : 128;
     static constexpr int THREADS     = FFT_THREADS + PRE_THREADS;
     static constexpr int ITEMS       = N / 2 + 1;   // row pairs per tile
     static constexpr int STAGES      = 2;
@@ -375,7 +375,7 @@ struct RowWsCfg {
     static constexpr int    TW       = TwPlan<L>::LEN;
     static constexpr size_t SMEM     = sizeof(float2) * (TW + RING + 2 * BUF) + 128;
     static constexpr int MINB        = 65536 / (THREADS * 96) < 1 ? 1 : 65536 / (THREADS * 96);
-    static constexpr int BAR_FULL = 4, BAR_EMPTY = 6, BAR_PRE = 8;   // named barriers (lines use 1..3)
+    static constexpr int BAR_FULL = 4, BAR_EMPTY = 6, BAR_PRE = 8, BAR_TW = 9;   // named barriers (lines use 1..3)
 };
 
 __device__ __forceinline__ void named_sync(int id, int count)
@@ -397,7 +397,7 @@ __global__ void __launch_bounds__(RowWsCfg<N, FROM_H0>::THREADS, RowWsCfg<N, FRO
     float2* tw_s = smem;
     float2* ring = smem + WC::TW;                            // [STAGES][2 rows][N*EW]
     float2* bufs = ring + WC::RING;                          // [2][3 lines][NPAD]
-    __shared__ __align__(8) uint64_t bars[WC::STAGES];
+    __shared__ __align__(8) uint64_t bars[WC::STAGES], bar_tw;
     __shared__ int wait_ok;
 
     const int tid     = threadIdx.x;
@@ -405,14 +405,19 @@ __global__ void __launch_bounds__(RowWsCfg<N, FROM_H0>::THREADS, RowWsCfg<N, FRO
     const int nsmp    = MULTI ? a.S : 1;
     const int n_jobs  = (n_items - (int)blockIdx.x + (int)gridDim.x - 1) / (int)gridDim.x * nsmp;
     if (tid == 0) {
+        // issue order = need order: the first rows (prepass), the twiddles
+        // (transforms), the next rows
         for (int s = 0; s < WC::STAGES; ++s) mbar_init(&bars[s], 1);
+        mbar_init(&bar_tw, 1);
         fence_mbar_init();
         for (int s = 0; s < WC::STAGES; ++s) {
             const int item = blockIdx.x + s * gridDim.x;
             if (item >= n_items) break;
-            const uint32_t twb = s == 0 ? (uint32_t)(WC::TW * sizeof(float2)) : 0u;
-            row_issue<N, FROM_H0>(a, ring + (size_t)s * 2 * N * WC::EW, &bars[s], item, twb);
-            if (twb) bulk_g2s(tw_s, a.tw, twb, &bars[0]);
+            row_issue<N, FROM_H0>(a, ring + (size_t)s * 2 * N * WC::EW, &bars[s], item);
+            if (s == 0) {
+                mbar_arrive_expect_tx(&bar_tw, WC::TW * sizeof(float2));
+                bulk_g2s(tw_s, a.tw, WC::TW * sizeof(float2), &bar_tw);
+            }
         }
         wait_ok = 1;
     }
@@ -421,6 +426,11 @@ __global__ void __launch_bounds__(RowWsCfg<N, FROM_H0>::THREADS, RowWsCfg<N, FRO
 
     if (tid < WC::FFT_THREADS) {
         const int li = tid / L::G, t = tid % L::G;           // line = field 0: Dx, 1: Dy, 2: Dz
+        if (tid == 0 && !mbar_wait_bounded(&bar_tw, 0)) {
+            atomicOr(a.status, kDeviceTimeout);
+            (void)mbar_wait_bounded(&bar_tw, 0);
+        }
+        named_sync(WC::BAR_TW, WC::FFT_THREADS);             // the twiddle plan is in
         for (int j = 0; j < n_jobs; ++j) {
             const int b = j & 1, ki = j / nsmp, smp = j - ki * nsmp;
             const int item = blockIdx.x + ki * gridDim.x, tile = item / WC::ITEMS, yp = item % WC::ITEMS;
@@ -461,6 +471,7 @@ __global__ void __launch_bounds__(RowWsCfg<N, FROM_H0>::THREADS, RowWsCfg<N, FRO
             }
             if (j >= 2) named_sync(WC::BAR_EMPTY + b, WC::THREADS);   // set b's previous job is transformed
             const FrameConsts fc = MULTI ? a.fcs[tile * a.S + smp] : a.fc0;
+#pragma unroll 4
             for (int x = pt; x <= N / 2; x += WC::PRE_THREADS)
                 row_position<N, FROM_H0, L::NPAD>(a, stage, bufs + b * WC::BUF, tile, x, yp, fc);
             named_arrive(WC::BAR_FULL + b, WC::THREADS);
