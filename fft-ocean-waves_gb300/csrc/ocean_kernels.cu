@@ -494,9 +494,11 @@ __global__ void __launch_bounds__(RowWsCfg<N, FROM_H0>::THREADS, RowWsCfg<N, FRO
 // ---------------------------------------------------------------------------
 // Column transforms.
 // ---------------------------------------------------------------------------
-// Column line decomposition: as LineFor except at N = 2048, where 64 threads
-// per line (32-point first pass, 168 registers) keep two CTAs per SM.
+// Column line decomposition: 32-point first passes at N = 1024 (one warp per
+// line, 32 x 32: one exchange instead of two) and N = 2048 (64 threads per
+// line, 32 x 8 x 8, 168 registers: two CTAs per SM); else as LineFor.
 template <int N> struct ColLineFor { using type = typename LineFor<N>::type; };
+template <> struct ColLineFor<1024> { using type = LineCfg<1024, 32, 32>; };
 template <> struct ColLineFor<2048> { using type = LineCfg<2048, 32, 8, 8>; };
 
 template <int N>
