@@ -41,7 +41,12 @@ BYTES_PER_TEXEL = 92            # algorithmic bytes per texel per frame
 # The frame's 92 B/texel split over the three kernels: rows read h0 (16) and
 # write the intermediate (24); columns read it (24); outputs write dx, dy, dz
 # and normal_j (28).
-KERNEL_BYTES = {"k_row_pass": 40, "k_col_fft": 24, "k_col_out": 28}
+KERNEL_BYTES = {"k_row_pass": 40, "k_row_ws": 40, "k_col_fft": 24, "k_col_out": 28}
+
+
+def row_kernel(N):
+    """The row stage's kernel: warp-specialised where a line is whole warps."""
+    return "k_row_ws" if N >= 512 else "k_row_pass"
 
 
 def c2_params(N):
@@ -254,7 +259,7 @@ def run_gpu(args, world, rank, local):
                 kv[i][3].record(stream)
             torch.cuda.synchronize()
             kernel_ms = {name: sum(kv[i][j].elapsed_time(kv[i][j + 1]) for i in range(K)) / K
-                         for j, name in enumerate(("k_row_pass", "k_col_fft", "k_col_out"))}
+                         for j, name in enumerate((row_kernel(N), "k_col_fft", "k_col_out"))}
 
             # e2e: C-ABI call + all outputs copied to pinned host memory, every frame.
             hdx, hdy, hdz = (torch.empty((N, N), dtype=torch.float32, pin_memory=True) for _ in range(3))
