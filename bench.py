@@ -289,6 +289,7 @@ def run_gpu(args, world, rank, local):
         oc.update(t_chk, dx, dy, dz, nj, stream=stream)
         torch.cuda.synchronize()
         frame = {"dx": dx.cpu().numpy(), "dy": dy.cpu().numpy(), "dz": dz.cpu().numpy(), "nj": nj.cpu().numpy()}
+        grid_stats = None if args.no_extra else bench_grid(torch, og, dev, stream, flush, (dx, dy, dz, nj))
     oc.close()
 
     if rank != 0:
@@ -323,6 +324,7 @@ def run_gpu(args, world, rank, local):
         "wall_s_timed_region": round(wall, 4),
     }
     if not args.no_extra:
+        out["grid"] = grid_stats
         out["adjoint"] = bench_adjoint(torch, og, dev, stream)
         out["batched"] = bench_batched(torch, og, dev, stream, flush)
     if not args.no_cpu:
@@ -451,6 +453,35 @@ def bench_batched(torch, og, dev, stream, flush, S=8, reps=3):
             "loop_tile_frames_per_s": round(n * S / (lms * 1e-3), 1), "speedup_vs_loop": round(lms / bms, 3),
             "loop_graph_ms": round(gms, 3), "speedup_vs_graphed_loop": round(gms / bms, 3),
             "batched_effective_GBps": round(92 * texels / (bms * 1e-3) / 1e9, 1)}
+
+
+def bench_grid(torch, og, dev, stream, flush, oc_maps, reps=20):
+    """The render grid's displacement (the reference's 1024-square grid, UV
+    repeat 64) over one frame's N=1024 maps, and its tessellation levels."""
+    dx, dy, dz, nj = oc_maps
+    g = og.grid_params()
+    n = g.squares
+    verts = torch.empty(((n + 1) * (n + 1), 8), device=dev)
+    levels = torch.empty((2 * n * n, 4), device=dev)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+    vt, lt = [], []
+    with torch.cuda.stream(stream):
+        for r in range(reps + 3):
+            flush()
+            ev[0].record(stream)
+            og.displace_grid(dx, dy, dz, nj, g, verts, stream=stream)
+            ev[1].record(stream)
+            og.grid_tess_levels(g, levels, stream=stream)
+            ev[2].record(stream)
+            torch.cuda.synchronize()
+            if r >= 3:
+                vt.append(ev[0].elapsed_time(ev[1]))
+                lt.append(ev[1].elapsed_time(ev[2]))
+    v_ms, l_ms = sum(vt) / len(vt), sum(lt) / len(lt)
+    nv = (n + 1) * (n + 1)
+    return {"workload": f"grid of {n} squares (UV repeat 64) over N={dy.shape[0]} maps, L2 flushed",
+            "vertices": nv, "displace_ms": round(v_ms, 4), "vertices_per_s": round(nv / (v_ms * 1e-3), 1),
+            "tess_levels_ms": round(l_ms, 4), "triangles_per_s": round(2 * n * n / (l_ms * 1e-3), 1)}
 
 
 def run_reference(args, world, rank):

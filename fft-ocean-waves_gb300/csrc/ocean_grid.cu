@@ -1,0 +1,167 @@
+// ocean_grid.cu -- the displaced grid: the consumer side of the maps.
+//
+// The reference renders a grid of GRID_SIZE = 1024 squares per side with a
+// texture repeat of GRID_UV_SCALE = 64 (main.cpp:20-21, generate_grid
+// main.cpp:748-824): (n+1)^2 vertices at (x, 0, z), x, z in [-n/2, n/2], two
+// triangles per square.  Its tessellation control stage picks per-triangle
+// levels from the eye distance (grid_tcs.glsl:27-59) and its evaluation stage
+// displaces each vertex by the maps (grid_tes.glsl:55-66).  These kernels
+// produce the same quantities into headless device buffers:
+//
+//   k_displace_grid   per grid vertex: y += Dy(uv) * displacement_scale,
+//                     x -= Dx(uv), z -= Dz(uv) (Dx, Dz already carry lambda),
+//                     normal = normal_map(uv).xyz, texcoord; the maps are
+//                     sampled bilinearly with REPEAT wrap.
+//   k_tess_levels     per triangle: outer levels from the mean eye distance of
+//                     each edge's end points (20 / 10 / 5 / 1 up to 10 / 20 /
+//                     30 / beyond), inner = outer[2].
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <cmath>
+
+#include "ocean.h"
+#include "ocean_host.h"
+
+namespace {
+
+struct GridArgs {
+    const float*  dx;
+    const float*  dy;
+    const float*  dz;
+    const float4* nj;
+    int           N;         // map size
+    int           n;         // squares per side
+    long long     step_int;  // integer part of texels per vertex step (uv_scale * N / n)
+    float         step_frac; // its fraction
+    float         uv_scale;
+    float         disp;
+};
+
+// Texel coordinate of vertex index i along one axis, reduced into [0, N) before
+// the half-texel shift so that large repeats keep sub-texel precision.
+__device__ __forceinline__ float texel_coord(const GridArgs& a, int i)
+{
+    const long long ip = ((long long)i * a.step_int) % a.N;
+    return (float)ip + (float)i * a.step_frac - 0.5f;
+}
+
+__device__ __forceinline__ void bilinear_taps(int N, float s, int& i0, int& i1, float& w)
+{
+    const float f = floorf(s);
+    w             = s - f;
+    int i         = (int)f % N;
+    if (i < 0) i += N;
+    i0 = i;
+    i1 = i + 1 == N ? 0 : i + 1;
+}
+
+__global__ void k_displace_grid(GridArgs a, float* __restrict__ out)
+{
+    const int nv = a.n + 1;
+    const int v  = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= nv * nv) return;
+    const int zi = v / nv, xi = v - zi * nv;
+    int   x0, x1, y0, y1;
+    float wx, wy;
+    bilinear_taps(a.N, texel_coord(a, xi), x0, x1, wx);
+    bilinear_taps(a.N, texel_coord(a, zi), y0, y1, wy);
+    const size_t o00 = (size_t)y0 * a.N + x0, o01 = (size_t)y0 * a.N + x1;
+    const size_t o10 = (size_t)y1 * a.N + x0, o11 = (size_t)y1 * a.N + x1;
+    auto lerp2 = [&](const float* m) {
+        const float top = __ldg(m + o00) * (1.0f - wx) + __ldg(m + o01) * wx;
+        const float bot = __ldg(m + o10) * (1.0f - wx) + __ldg(m + o11) * wx;
+        return top * (1.0f - wy) + bot * wy;
+    };
+    const float4 n00 = __ldg(a.nj + o00), n01 = __ldg(a.nj + o01), n10 = __ldg(a.nj + o10), n11 = __ldg(a.nj + o11);
+    const float  w00 = (1.0f - wx) * (1.0f - wy), w01 = wx * (1.0f - wy), w10 = (1.0f - wx) * wy, w11 = wx * wy;
+    const int    h = a.n / 2;
+    float4* o = reinterpret_cast<float4*>(out + 8 * (size_t)v);
+    o[0] = make_float4((float)(xi - h) - lerp2(a.dx), lerp2(a.dy) * a.disp, (float)(zi - h) - lerp2(a.dz),
+                       n00.x * w00 + n01.x * w01 + n10.x * w10 + n11.x * w11);
+    o[1] = make_float4(n00.y * w00 + n01.y * w01 + n10.y * w10 + n11.y * w11,
+                       n00.z * w00 + n01.z * w01 + n10.z * w10 + n11.z * w11, (float)xi / (float)a.n * a.uv_scale,
+                       (float)zi / (float)a.n * a.uv_scale);
+}
+
+__device__ __forceinline__ float tess_level(float d0, float d1)
+{
+    const float avg = (d0 + d1) / 2.0f;
+    return avg <= 10.0f ? 20.0f : avg <= 20.0f ? 10.0f : avg <= 30.0f ? 5.0f : 1.0f;
+}
+
+__global__ void k_tess_levels(int n, float cx, float cy, float cz, float4* __restrict__ out)
+{
+    const int sq = blockIdx.x * blockDim.x + threadIdx.x;
+    if (sq >= n * n) return;
+    const int   zi = sq / n, xi = sq - zi * n, h = n / 2;
+    const float x0 = (float)(xi - h), x1 = x0 + 1.0f, z0 = (float)(zi - h), z1 = z0 + 1.0f;
+    auto dist = [&](float x, float z) {
+        const float ex = cx - x, ez = cz - z;
+        return sqrtf(ex * ex + cy * cy + ez * ez);
+    };
+    // triangle A: (x, z), (x, z+1), (x+1, z); triangle B: (x+1, z), (x, z+1), (x+1, z+1)
+    const float a0 = dist(x0, z0), a1 = dist(x0, z1), a2 = dist(x1, z0), b2 = dist(x1, z1);
+    const float oa2 = tess_level(a0, a1), ob2 = tess_level(a2, a1);
+    out[2 * (size_t)sq]     = make_float4(tess_level(a1, a2), tess_level(a2, a0), oa2, oa2);
+    out[2 * (size_t)sq + 1] = make_float4(tess_level(a1, b2), tess_level(b2, a2), ob2, ob2);
+}
+
+int check_grid(const ocean_grid_params* g)
+{
+    using namespace ocean::host;
+    if (!g) return fail(OCEAN_ERR_INVALID, "grid params are NULL");
+    if (g->squares < 2 || g->squares > 16384 || (g->squares & 1))
+        return fail(OCEAN_ERR_INVALID, "squares must be even and in [2, 16384]");
+    if (!std::isfinite(g->texcoord_scale) || !std::isfinite(g->displacement_scale))
+        return fail(OCEAN_ERR_INVALID, "grid scales must be finite");
+    return OCEAN_OK;
+}
+
+}  // namespace
+
+extern "C" int ocean_displace_grid(const ocean_outputs* maps, int32_t N, const ocean_grid_params* g, float* vertices,
+                                   void* stream)
+{
+    using namespace ocean::host;
+    int rc = check_grid(g);
+    if (rc) return rc;
+    if (!maps || !maps->dx || !maps->dy || !maps->dz || !maps->normal_j || !vertices)
+        return fail(OCEAN_ERR_INVALID, "NULL pointer");
+    if (!is_pow2(N) || N < 2 || N > 65536) return fail(OCEAN_ERR_INVALID, "N must be a power of two");
+    if ((reinterpret_cast<uintptr_t>(vertices) | reinterpret_cast<uintptr_t>(maps->normal_j)) % 16)
+        return fail(OCEAN_ERR_INVALID, "vertices and normal_j must be 16-byte aligned");
+    GridArgs a;
+    a.dx = maps->dx;
+    a.dy = maps->dy;
+    a.dz = maps->dz;
+    a.nj = reinterpret_cast<const float4*>(maps->normal_j);
+    a.N  = N;
+    a.n  = g->squares;
+    const double step = (double)g->texcoord_scale * N / g->squares;   // texels per vertex
+    const double fl   = std::floor(step);
+    a.step_int  = (long long)fl;
+    a.step_frac = (float)(step - fl);
+    a.uv_scale  = g->texcoord_scale;
+    a.disp      = g->displacement_scale;
+    const long long nv = (long long)(g->squares + 1) * (g->squares + 1);
+    k_displace_grid<<<(unsigned)((nv + 255) / 256), 256, 0, static_cast<cudaStream_t>(stream)>>>(a, vertices);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(e, "displaced grid launch");
+    return OCEAN_OK;
+}
+
+extern "C" int ocean_grid_tess_levels(const ocean_grid_params* g, float* levels, void* stream)
+{
+    using namespace ocean::host;
+    int rc = check_grid(g);
+    if (rc) return rc;
+    if (!levels) return fail(OCEAN_ERR_INVALID, "levels is NULL");
+    if (reinterpret_cast<uintptr_t>(levels) % 16) return fail(OCEAN_ERR_INVALID, "levels must be 16-byte aligned");
+    const long long sq = (long long)g->squares * g->squares;
+    k_tess_levels<<<(unsigned)((sq + 255) / 256), 256, 0, static_cast<cudaStream_t>(stream)>>>(
+        g->squares, g->camera[0], g->camera[1], g->camera[2], reinterpret_cast<float4*>(levels));
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(e, "tessellation level launch");
+    return OCEAN_OK;
+}

@@ -35,7 +35,8 @@ EXPORTS = [
     "ocean_set_params", "ocean_get_params", "ocean_get_h0", "ocean_set_h0", "ocean_compute_h0",
     "ocean_fill_noise", "ocean_bit_reversed_indices", "ocean_butterfly_table", "ocean_last_error",
     "ocean_version", "ocean_backward", "ocean_device_status", "ocean_batch_create", "ocean_batch_update",
-    "ocean_batch_device_status", "ocean_batch_destroy", "ocean_update_noalloc",
+    "ocean_batch_device_status", "ocean_batch_destroy", "ocean_update_noalloc", "ocean_displace_grid",
+    "ocean_grid_tess_levels",
 ]
 OCEAN_GRAD_ACCUMULATE = 1
 
@@ -125,6 +126,8 @@ def load() -> C.CDLL:
     L.ocean_batch_destroy.argtypes = [vp]
     L.ocean_batch_destroy.restype = None
     L.ocean_update_noalloc.argtypes = [P(ocean_params), vp, C.c_double, P(ocean_outputs), vp]
+    L.ocean_displace_grid.argtypes = [P(ocean_outputs), C.c_int32, P(ocean_grid_params), vp, vp]
+    L.ocean_grid_tess_levels.argtypes = [P(ocean_grid_params), vp, vp]
     L.ocean_last_error.restype = C.c_char_p
     for name in EXPORTS:
         if name not in ("ocean_destroy", "ocean_last_error", "ocean_batch_destroy"):
@@ -186,6 +189,29 @@ def update_noalloc(params: Params, h0_dev, t: float, dx, dy, dz, normal_j, strea
     cp = params.c()
     o = ocean_outputs(_addr(dx), _addr(dy), _addr(dz), _addr(normal_j))
     check(load().ocean_update_noalloc(C.byref(cp), _addr(h0_dev), float(t), C.byref(o), _stream(stream)))
+
+
+class ocean_grid_params(C.Structure):
+    _fields_ = [("squares", C.c_int32), ("texcoord_scale", C.c_float), ("displacement_scale", C.c_float),
+                ("camera", C.c_float * 3)]
+
+
+def grid_params(squares=1024, texcoord_scale=64.0, displacement_scale=0.5, camera=(0.0, 10.0, 0.0)):
+    """The reference's render grid (GRID_SIZE 1024, GRID_UV_SCALE 64, displacement 0.5) by default."""
+    return ocean_grid_params(int(squares), float(texcoord_scale), float(displacement_scale),
+                             (C.c_float * 3)(*[float(c) for c in camera]))
+
+
+def displace_grid(dx, dy, dz, normal_j, grid: "ocean_grid_params", vertices, stream=None) -> None:
+    """Displaced grid vertices ((squares+1)^2, 8) from one frame's maps (device)."""
+    N = int(dy.shape[0])
+    o = ocean_outputs(_addr(dx), _addr(dy), _addr(dz), _addr(normal_j))
+    check(load().ocean_displace_grid(C.byref(o), N, C.byref(grid), _addr(vertices), _stream(stream)))
+
+
+def grid_tess_levels(grid: "ocean_grid_params", levels, stream=None) -> None:
+    """Per-triangle tessellation levels (2*squares^2, 4) into `levels` (device)."""
+    check(load().ocean_grid_tess_levels(C.byref(grid), _addr(levels), _stream(stream)))
 
 
 def compute_h0(params: Params, noise_dev, h0_dev, stream=None) -> None:

@@ -200,6 +200,37 @@ OCEAN_API void ocean_batch_destroy(ocean_batch_t* batch);
 OCEAN_API int ocean_update_noalloc(const ocean_params* params, const float* h0_dev, double t,
                                    const ocean_outputs* out, void* stream);
 
+/* ---- Displaced grid (the consumer of the maps) ------------------------ */
+
+/* The render grid of main.cpp:748-824 (generate_grid(GRID_SIZE, GRID_UV_SCALE),
+ * main.cpp:20-21): `squares` squares per side, (squares+1)^2 vertices at
+ * (x, 0, z) with integer x, z in [-squares/2, squares/2], two triangles per
+ * square (vertex indices i0, i0+squares+1, i0+1 and i0+1, i0+squares+1,
+ * i0+squares+2). */
+typedef struct ocean_grid_params {
+    int32_t squares;            /* even, 2..16384; the reference uses 1024 */
+    float   texcoord_scale;     /* texture repeats over the grid; the reference uses 64 */
+    float   displacement_scale; /* vertical scale of Dy; the reference's default 0.5 (main.cpp:1632) */
+    float   camera[3];          /* eye position for the tessellation levels */
+} ocean_grid_params;
+
+/* The tessellation evaluation stage at the grid's vertices
+ * (grid_tes.glsl:55-66): position (x - Dx, Dy * displacement_scale, z - Dz),
+ * normal = normal_map.xyz, texcoord, with the maps (one frame's outputs,
+ * N x N, device) sampled bilinearly with REPEAT wrap.  dx and dz are
+ * ocean_update's outputs, which already carry lambda (the shader's
+ * u_Choppiness).  vertices: device, (squares+1)^2 * 8 floats (position xyz,
+ * normal xyz, texcoord uv), 16-byte aligned. */
+OCEAN_API int ocean_displace_grid(const ocean_outputs* maps, int32_t N, const ocean_grid_params* grid,
+                                  float* vertices, void* stream);
+
+/* The tessellation control stage (grid_tcs.glsl:27-59) per triangle:
+ * outer[0..2] from the mean eye distance of edges (v1, v2), (v2, v0),
+ * (v0, v1): 20 up to 10, 10 up to 20, 5 up to 30, else 1; inner = outer[2].
+ * levels: device, 2 * squares^2 * 4 floats (triangle 2*(z*squares + x) + t),
+ * 16-byte aligned. */
+OCEAN_API int ocean_grid_tess_levels(const ocean_grid_params* grid, float* levels, void* stream);
+
 /* ---- Adjoint --------------------------------------------------------- */
 
 /* Flags for ocean_backward */

@@ -359,6 +359,86 @@ void orc_backward(const orc_params* p, const double* h0, const double* times, in
     grads[3] = dlam;
 }
 
+/* Displaced grid (the consumer of the maps).
+ *
+ * The grid of main.cpp:748-824 (generate_grid(GRID_SIZE = 1024, GRID_UV_SCALE
+ * = 64), :20-21): n squares per side, (n+1)^2 vertices at (x, 0, z) for
+ * integer x, z in [-n/2, n/2], texcoord ((x + n/2)/n, (z + n/2)/n) * scale,
+ * two triangles per square with indices (i0, i1, i2), (i2, i1, i1 + 1),
+ * i0 = (n+1) z' + x', i1 = i0 + n + 1, i2 = i0 + 1.
+ *
+ * orc_displace_grid: the tessellation evaluation stage at the grid's own
+ * vertices (grid_tes.glsl:55-66): y += Dy(uv) * disp_scale, x -= Dx(uv),
+ * z -= Dz(uv), normal = normal_map(uv).xyz, with the maps sampled bilinearly
+ * with REPEAT wrap (texel centres at (i + 0.5)/N).  dx and dz are the build's
+ * outputs, which already carry lambda (the shader's u_Choppiness factor).
+ * out: (n+1)^2 * 8 = position xyz, normal xyz, texcoord uv.
+ *
+ * orc_tess_levels: the tessellation control stage (grid_tcs.glsl:27-59) per
+ * triangle: outer[0] = level(d1, d2), outer[1] = level(d2, d0), outer[2] =
+ * level(d0, d1), inner = outer[2], level of the mean eye distance: 20 up to
+ * 10, 10 up to 20, 5 up to 30, else 1.  out: 2 n^2 * 4. */
+static double orc_bilinear(const double* m, int N, int stride, int comp, double u, double v)
+{
+    double sx = u * N - 0.5, sy = v * N - 0.5;
+    double fx = floor(sx), fy = floor(sy);
+    double ax = sx - fx, ay = sy - fy;
+    long   x0 = (long)fx, y0 = (long)fy;
+    long   xa = ((x0 % N) + N) % N, xb = (xa + 1) % N;
+    long   ya = ((y0 % N) + N) % N, yb = (ya + 1) % N;
+#define M(yy, xx) m[((size_t)(yy) * N + (xx)) * stride + comp]
+    double top = M(ya, xa) * (1.0 - ax) + M(ya, xb) * ax;
+    double bot = M(yb, xa) * (1.0 - ax) + M(yb, xb) * ax;
+#undef M
+    return top * (1.0 - ay) + bot * ay;
+}
+
+void orc_displace_grid(int N, const double* dx, const double* dy, const double* dz, const double* nj, int n,
+                       double uv_scale, double disp_scale, double* out)
+{
+    int h = n / 2;
+    for (int zi = 0; zi <= n; ++zi)
+        for (int xi = 0; xi <= n; ++xi) {
+            double  u = (double)xi / n * uv_scale, v = (double)zi / n * uv_scale;
+            double* o = out + 8 * ((size_t)zi * (n + 1) + xi);
+            o[0] = (double)(xi - h) - orc_bilinear(dx, N, 1, 0, u, v);
+            o[1] = orc_bilinear(dy, N, 1, 0, u, v) * disp_scale;
+            o[2] = (double)(zi - h) - orc_bilinear(dz, N, 1, 0, u, v);
+            for (int c = 0; c < 3; ++c) o[3 + c] = orc_bilinear(nj, N, 4, c, u, v);
+            o[6] = u;
+            o[7] = v;
+        }
+}
+
+static double orc_level(double d0, double d1)
+{
+    double avg = (d0 + d1) / 2.0;
+    return avg <= 10.0 ? 20.0 : avg <= 20.0 ? 10.0 : avg <= 30.0 ? 5.0 : 1.0;
+}
+
+void orc_tess_levels(int n, const double* cam, double* out)
+{
+    int h = n / 2;
+    for (int zi = 0; zi < n; ++zi)
+        for (int xi = 0; xi < n; ++xi) {
+            /* triangle A: (x, z), (x, z+1), (x+1, z); triangle B: (x+1, z), (x, z+1), (x+1, z+1) */
+            double px[2][3] = {{xi - h, xi - h, xi + 1 - h}, {xi + 1 - h, xi - h, xi + 1 - h}};
+            double pz[2][3] = {{zi - h, zi + 1 - h, zi - h}, {zi - h, zi + 1 - h, zi + 1 - h}};
+            for (int tr = 0; tr < 2; ++tr) {
+                double d[3];
+                for (int k = 0; k < 3; ++k) {
+                    double ex = cam[0] - px[tr][k], ey = cam[1], ez = cam[2] - pz[tr][k];
+                    d[k] = sqrt(ex * ex + ey * ey + ez * ez);
+                }
+                double* o = out + 4 * (2 * ((size_t)zi * n + xi) + tr);
+                o[0] = orc_level(d[1], d[2]);
+                o[1] = orc_level(d[2], d[0]);
+                o[2] = orc_level(d[0], d[1]);
+                o[3] = o[2];
+            }
+        }
+}
+
 /* FFT tables of the reference, restated in double.
  * Bit reversal over log2(N) bits: main.cpp:35-64 (reverse_bits) as used by
  * generate_bit_reversed_indices() main.cpp:733-744. */

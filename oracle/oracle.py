@@ -72,6 +72,8 @@ def lib():
         L.orc_backward.argtypes = [pp, dp, dp, C.c_int, dp, dp, dp, dp, dp]
         L.orc_bit_reversed.argtypes = [C.c_int, C.POINTER(C.c_int32)]
         L.orc_twiddle_table.argtypes = [C.c_int, dp]
+        L.orc_displace_grid.argtypes = [C.c_int, dp, dp, dp, dp, C.c_int, C.c_double, C.c_double, dp]
+        L.orc_tess_levels.argtypes = [C.c_int, dp, dp]
         L.orc_count_clamped.argtypes = [pp]
         L.orc_count_clamped.restype = C.c_int
         L.port_create.argtypes = [pp, fp]
@@ -189,6 +191,25 @@ def backward(p: Params, h0a: np.ndarray, times, g_dx=None, g_dy=None, g_dz=None)
                        *[(_p(g, C.c_double) if g is not None else None) for g in gs],
                        _p(dh0, C.c_double), _p(gr, C.c_double))
     return dh0, {"dA": gr[0], "dV": gr[1], "dtheta": gr[2], "dlambda": gr[3]}
+
+
+def displace_grid(frame: dict, n: int, uv_scale: float = 64.0, disp_scale: float = 0.5) -> np.ndarray:
+    """Displaced grid vertices (n+1)^2 x 8 (position, normal, texcoord) from
+    one frame's maps (dx, dy, dz (N, N), nj (N, N, 4)): orc_displace_grid."""
+    N = frame["dy"].shape[0]
+    m = [np.ascontiguousarray(frame[k], dtype=np.float64) for k in ("dx", "dy", "dz", "nj")]
+    out = np.empty(((n + 1) * (n + 1), 8))
+    lib().orc_displace_grid(N, *[_p(x, C.c_double) for x in m], n, float(uv_scale), float(disp_scale),
+                            _p(out, C.c_double))
+    return out
+
+
+def tess_levels(n: int, camera) -> np.ndarray:
+    """Per-triangle tessellation levels 2n^2 x 4 (outer 0..2, inner): orc_tess_levels."""
+    cam = np.asarray(camera, dtype=np.float64)
+    out = np.empty((2 * n * n, 4))
+    lib().orc_tess_levels(n, _p(cam, C.c_double), _p(out, C.c_double))
+    return out
 
 
 def bit_reversed(N: int) -> np.ndarray:
