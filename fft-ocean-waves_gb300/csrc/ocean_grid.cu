@@ -15,6 +15,10 @@
 //   k_tess_levels     per triangle: outer levels from the mean eye distance of
 //                     each edge's end points (20 / 10 / 5 / 1 up to 10 / 20 /
 //                     30 / beyond), inner = outer[2].
+//   k_shade           per displaced vertex: the ocean fragment shader
+//                     (ocean_fs.glsl:11-37): Fresnel-Schlick mix of the sea
+//                     colour and the sky cube map along the reflected view
+//                     ray, N.L, Reinhard tonemap, gamma 1/2.2.
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -107,6 +111,63 @@ __global__ void k_tess_levels(int n, float cx, float cy, float cz, float4* __res
     out[2 * (size_t)sq + 1] = make_float4(tess_level(a1, b2), tess_level(b2, a2), ob2, ob2);
 }
 
+// Cube-map lookup (faces +X, -X, +Y, -Y, +Z, -Z of S x S RGBA texels): face and
+// face coordinates from the major axis of r as in the OpenGL specification's
+// cube-map table (ties go to x, then y), bilinear within the face, clamp to
+// edge.
+__device__ __forceinline__ float3 cube_sample(const float4* __restrict__ sky, int S, float3 r)
+{
+    const float ax = fabsf(r.x), ay = fabsf(r.y), az = fabsf(r.z);
+    int   face;
+    float ma, sc, tc;
+    if (ax >= ay && ax >= az) {
+        face = r.x >= 0.0f ? 0 : 1; ma = ax; sc = r.x >= 0.0f ? -r.z : r.z; tc = -r.y;
+    } else if (ay >= az) {
+        face = r.y >= 0.0f ? 2 : 3; ma = ay; sc = r.x; tc = r.y >= 0.0f ? r.z : -r.z;
+    } else {
+        face = r.z >= 0.0f ? 4 : 5; ma = az; sc = r.z >= 0.0f ? r.x : -r.x; tc = -r.y;
+    }
+    const float s = 0.5f * (sc / ma + 1.0f) * S - 0.5f, t = 0.5f * (tc / ma + 1.0f) * S - 0.5f;
+    const float fs = floorf(s), ft = floorf(t), ws = s - fs, wt = t - ft;
+    const int   s0 = (int)fs, t0 = (int)ft;
+    const int   sa = min(max(s0, 0), S - 1), sb = min(max(s0 + 1, 0), S - 1);
+    const int   ta = min(max(t0, 0), S - 1), tb = min(max(t0 + 1, 0), S - 1);
+    const float4* f = sky + (size_t)face * S * S;
+    const float4 a = __ldg(f + (size_t)ta * S + sa), b = __ldg(f + (size_t)ta * S + sb);
+    const float4 c = __ldg(f + (size_t)tb * S + sa), d = __ldg(f + (size_t)tb * S + sb);
+    const float w00 = (1 - ws) * (1 - wt), w01 = ws * (1 - wt), w10 = (1 - ws) * wt, w11 = ws * wt;
+    return make_float3(a.x * w00 + b.x * w01 + c.x * w10 + d.x * w11, a.y * w00 + b.y * w01 + c.y * w10 + d.y * w11,
+                       a.z * w00 + b.z * w01 + c.z * w10 + d.z * w11);
+}
+
+struct ShadeArgs {
+    float3 cam, sun, sea;
+    int    S;
+};
+
+__global__ void k_shade(const float4* __restrict__ vert, long long n, ShadeArgs a, const float4* __restrict__ sky,
+                        float4* __restrict__ out)
+{
+    const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4 p0 = __ldg(vert + 2 * i), p1 = __ldg(vert + 2 * i + 1);   // position xyz, normal x | normal yz, uv
+    const float3 N  = make_float3(p0.w, p1.x, p1.y);
+    float3       V  = make_float3(a.cam.x - p0.x, a.cam.y - p0.y, a.cam.z - p0.z);
+    const float  iv = rsqrtf(V.x * V.x + V.y * V.y + V.z * V.z);
+    V               = make_float3(V.x * iv, V.y * iv, V.z * iv);
+    const float  nv = N.x * V.x + N.y * V.y + N.z * V.z;
+    const float3 R  = make_float3(2.0f * nv * N.x - V.x, 2.0f * nv * N.y - V.y, 2.0f * nv * N.z - V.z);
+    const float3 sk = cube_sample(sky, a.S, R);
+    const float  om = 1.0f - fmaxf(nv, 0.0f);
+    const float  F  = 0.04f + 0.96f * (om * om) * (om * om) * om;
+    const float  nl = fmaxf(-(N.x * a.sun.x + N.y * a.sun.y + N.z * a.sun.z), 0.0f);
+    auto tone = [&](float sea, float skyc) {
+        const float c = nl * (sea * (1.0f - F) + skyc * F);
+        return powf(c / (c + 1.0f), 1.0f / 2.2f);
+    };
+    out[i] = make_float4(tone(a.sea.x, sk.x), tone(a.sea.y, sk.y), tone(a.sea.z, sk.z), 1.0f);
+}
+
 int check_grid(const ocean_grid_params* g)
 {
     using namespace ocean::host;
@@ -163,5 +224,32 @@ extern "C" int ocean_grid_tess_levels(const ocean_grid_params* g, float* levels,
         g->squares, g->camera[0], g->camera[1], g->camera[2], reinterpret_cast<float4*>(levels));
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_fail(e, "tessellation level launch");
+    return OCEAN_OK;
+}
+
+extern "C" int ocean_shade_grid(const float* vertices, int64_t n_vertices, const ocean_shade_params* p,
+                                const float* sky_cubemap, float* colors, void* stream)
+{
+    using namespace ocean::host;
+    if (!vertices || !p || !sky_cubemap || !colors) return fail(OCEAN_ERR_INVALID, "NULL pointer");
+    if (n_vertices < 0) return fail(OCEAN_ERR_INVALID, "n_vertices must be >= 0");
+    if (p->sky_size < 1 || p->sky_size > 16384) return fail(OCEAN_ERR_INVALID, "sky_size must be in [1, 16384]");
+    if ((reinterpret_cast<uintptr_t>(vertices) | reinterpret_cast<uintptr_t>(sky_cubemap) |
+         reinterpret_cast<uintptr_t>(colors)) % 16)
+        return fail(OCEAN_ERR_INVALID, "vertices, sky_cubemap and colors must be 16-byte aligned");
+    for (int c = 0; c < 3; ++c)
+        if (!std::isfinite(p->camera[c]) || !std::isfinite(p->sun_direction[c]) || !std::isfinite(p->sea_color[c]))
+            return fail(OCEAN_ERR_INVALID, "shading parameters must be finite");
+    if (!n_vertices) return OCEAN_OK;
+    ShadeArgs a;
+    a.cam = make_float3(p->camera[0], p->camera[1], p->camera[2]);
+    a.sun = make_float3(p->sun_direction[0], p->sun_direction[1], p->sun_direction[2]);
+    a.sea = make_float3(p->sea_color[0], p->sea_color[1], p->sea_color[2]);
+    a.S   = p->sky_size;
+    k_shade<<<(unsigned)((n_vertices + 255) / 256), 256, 0, static_cast<cudaStream_t>(stream)>>>(
+        reinterpret_cast<const float4*>(vertices), n_vertices, a, reinterpret_cast<const float4*>(sky_cubemap),
+        reinterpret_cast<float4*>(colors));
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(e, "shading launch");
     return OCEAN_OK;
 }

@@ -36,7 +36,7 @@ EXPORTS = [
     "ocean_fill_noise", "ocean_bit_reversed_indices", "ocean_butterfly_table", "ocean_last_error",
     "ocean_version", "ocean_backward", "ocean_device_status", "ocean_batch_create", "ocean_batch_update",
     "ocean_batch_device_status", "ocean_batch_destroy", "ocean_update_noalloc", "ocean_displace_grid",
-    "ocean_grid_tess_levels",
+    "ocean_grid_tess_levels", "ocean_shade_grid",
 ]
 OCEAN_GRAD_ACCUMULATE = 1
 
@@ -128,6 +128,7 @@ def load() -> C.CDLL:
     L.ocean_update_noalloc.argtypes = [P(ocean_params), vp, C.c_double, P(ocean_outputs), vp]
     L.ocean_displace_grid.argtypes = [P(ocean_outputs), C.c_int32, P(ocean_grid_params), vp, vp]
     L.ocean_grid_tess_levels.argtypes = [P(ocean_grid_params), vp, vp]
+    L.ocean_shade_grid.argtypes = [vp, C.c_int64, P(ocean_shade_params), vp, vp, vp]
     L.ocean_last_error.restype = C.c_char_p
     for name in EXPORTS:
         if name not in ("ocean_destroy", "ocean_last_error", "ocean_batch_destroy"):
@@ -212,6 +213,20 @@ def displace_grid(dx, dy, dz, normal_j, grid: "ocean_grid_params", vertices, str
 def grid_tess_levels(grid: "ocean_grid_params", levels, stream=None) -> None:
     """Per-triangle tessellation levels (2*squares^2, 4) into `levels` (device)."""
     check(load().ocean_grid_tess_levels(C.byref(grid), _addr(levels), _stream(stream)))
+
+
+class ocean_shade_params(C.Structure):
+    _fields_ = [("camera", C.c_float * 3), ("sun_direction", C.c_float * 3), ("sea_color", C.c_float * 3),
+                ("sky_size", C.c_int32)]
+
+
+def shade_grid(vertices, camera, sun_direction, sea_color, sky, colors, stream=None) -> None:
+    """ocean_fs.glsl's colour at each displaced vertex: vertices (n, 8), sky
+    (6, S, S, 4) cube map, colors (n, 4); device tensors."""
+    f3 = lambda v: (C.c_float * 3)(*[float(x) for x in v])
+    p = ocean_shade_params(f3(camera), f3(sun_direction), f3(sea_color), int(sky.shape[1]))
+    check(load().ocean_shade_grid(_addr(vertices), int(vertices.shape[0]), C.byref(p), _addr(sky), _addr(colors),
+                                  _stream(stream)))
 
 
 def compute_h0(params: Params, noise_dev, h0_dev, stream=None) -> None:

@@ -231,6 +231,27 @@ OCEAN_API int ocean_displace_grid(const ocean_outputs* maps, int32_t N, const oc
  * 16-byte aligned. */
 OCEAN_API int ocean_grid_tess_levels(const ocean_grid_params* grid, float* levels, void* stream);
 
+/* The ocean fragment shader (ocean_fs.glsl:11-37) at the displaced grid's
+ * vertices: N = the vertex normal as given, V = normalize(camera - P),
+ * R = reflect(-V, N), F = 0.04 + 0.96 (1 - max(N.V, 0))^5,
+ * color = max(-N.sun_direction, 0) * mix(sea_color, sky(R), F), then
+ * c / (c + 1) and gamma 1/2.2.  sky_cubemap: device, 6 faces (+X, -X, +Y,
+ * -Y, +Z, -Z) of sky_size^2 RGBA floats, looked up as the OpenGL cube-map
+ * table specifies (bilinear within a face, clamp to edge).  vertices: as
+ * ocean_displace_grid writes them (n_vertices * 8 floats).  colors: device,
+ * n_vertices * 4 floats (RGB, 1).  All three 16-byte aligned.  As in the
+ * shader, the result is undefined (NaN) for normals longer than 1 with
+ * N.V > 1, where the Fresnel term goes negative. */
+typedef struct ocean_shade_params {
+    float   camera[3];
+    float   sun_direction[3];   /* direction the sunlight travels (the shader's u_SunDirection) */
+    float   sea_color[3];       /* the shader's u_SeaColor */
+    int32_t sky_size;           /* cube-map face edge in texels */
+} ocean_shade_params;
+
+OCEAN_API int ocean_shade_grid(const float* vertices, int64_t n_vertices, const ocean_shade_params* params,
+                               const float* sky_cubemap, float* colors, void* stream);
+
 /* ---- Adjoint --------------------------------------------------------- */
 
 /* Flags for ocean_backward */

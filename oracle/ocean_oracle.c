@@ -439,6 +439,65 @@ void orc_tess_levels(int n, const double* cam, double* out)
         }
 }
 
+/* Ocean shading (ocean_fs.glsl:11-37) at the displaced grid's vertices:
+ * N = the vertex normal as given (not renormalised, as the shader uses the
+ * interpolated FS_IN_Normal), V = normalize(camera - P), R = reflect(-V, N),
+ * L = -sun_direction, F = F0 + (1 - F0)(1 - max(N.V, 0))^5 with F0 = 0.04,
+ * albedo = mix(sea_color, sky(R), F), color = max(N.L, 0) * albedo, then the
+ * Reinhard tonemap c / (c + 1) and gamma 1/2.2.  sky: a cube map of 6 faces
+ * (+X, -X, +Y, -Y, +Z, -Z) of S x S RGBA texels, face and face coordinates
+ * chosen by the major axis of R as in the OpenGL specification's cube-map
+ * table, bilinear within the face with clamp to edge.
+ * vert: n * 8 (position, normal, texcoord); out: n * 4 (RGB, 1). */
+static void orc_cube_sample(const double* sky, int S, const double* r, double* rgb)
+{
+    double ax = fabs(r[0]), ay = fabs(r[1]), az = fabs(r[2]), ma, sc, tc;
+    int    face;
+    if (ax >= ay && ax >= az) {
+        face = r[0] >= 0 ? 0 : 1; ma = ax; sc = r[0] >= 0 ? -r[2] : r[2]; tc = -r[1];
+    } else if (ay >= az) {
+        face = r[1] >= 0 ? 2 : 3; ma = ay; sc = r[0]; tc = r[1] >= 0 ? r[2] : -r[2];
+    } else {
+        face = r[2] >= 0 ? 4 : 5; ma = az; sc = r[2] >= 0 ? r[0] : -r[0]; tc = -r[1];
+    }
+    double s = 0.5 * (sc / ma + 1.0) * S - 0.5, t = 0.5 * (tc / ma + 1.0) * S - 0.5;
+    double fs = floor(s), ft = floor(t), ws = s - fs, wt = t - ft;
+    int    s0 = (int)fs, t0 = (int)ft;
+    int    sa = s0 < 0 ? 0 : (s0 > S - 1 ? S - 1 : s0), sb = s0 + 1 < 0 ? 0 : (s0 + 1 > S - 1 ? S - 1 : s0 + 1);
+    int    ta = t0 < 0 ? 0 : (t0 > S - 1 ? S - 1 : t0), tb = t0 + 1 < 0 ? 0 : (t0 + 1 > S - 1 ? S - 1 : t0 + 1);
+    const double* f = sky + (size_t)face * S * S * 4;
+    for (int c = 0; c < 3; ++c) {
+        double top = f[((size_t)ta * S + sa) * 4 + c] * (1 - ws) + f[((size_t)ta * S + sb) * 4 + c] * ws;
+        double bot = f[((size_t)tb * S + sa) * 4 + c] * (1 - ws) + f[((size_t)tb * S + sb) * 4 + c] * ws;
+        rgb[c] = top * (1 - wt) + bot * wt;
+    }
+}
+
+void orc_shade(const double* vert, long n, const double* cam, const double* sun, const double* sea, const double* sky,
+               int S, double* out)
+{
+    for (long i = 0; i < n; ++i) {
+        const double* p = vert + 8 * i;
+        const double* N = p + 3;
+        double V[3] = {cam[0] - p[0], cam[1] - p[1], cam[2] - p[2]};
+        double vl = sqrt(V[0] * V[0] + V[1] * V[1] + V[2] * V[2]);
+        for (int c = 0; c < 3; ++c) V[c] /= vl;
+        double nv = N[0] * V[0] + N[1] * V[1] + N[2] * V[2];
+        double R[3] = {2.0 * nv * N[0] - V[0], 2.0 * nv * N[1] - V[1], 2.0 * nv * N[2] - V[2]};
+        double sky_rgb[3];
+        orc_cube_sample(sky, S, R, sky_rgb);
+        double F  = 0.04 + 0.96 * pow(1.0 - (nv > 0 ? nv : 0.0), 5.0);
+        double nl = -(N[0] * sun[0] + N[1] * sun[1] + N[2] * sun[2]);
+        if (nl < 0) nl = 0;
+        for (int c = 0; c < 3; ++c) {
+            double col = nl * (sea[c] * (1.0 - F) + sky_rgb[c] * F);
+            col        = col / (col + 1.0);
+            out[4 * i + c] = pow(col, 1.0 / 2.2);
+        }
+        out[4 * i + 3] = 1.0;
+    }
+}
+
 /* FFT tables of the reference, restated in double.
  * Bit reversal over log2(N) bits: main.cpp:35-64 (reverse_bits) as used by
  * generate_bit_reversed_indices() main.cpp:733-744. */

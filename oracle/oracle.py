@@ -74,6 +74,7 @@ def lib():
         L.orc_twiddle_table.argtypes = [C.c_int, dp]
         L.orc_displace_grid.argtypes = [C.c_int, dp, dp, dp, dp, C.c_int, C.c_double, C.c_double, dp]
         L.orc_tess_levels.argtypes = [C.c_int, dp, dp]
+        L.orc_shade.argtypes = [dp, C.c_long, dp, dp, dp, dp, C.c_int, dp]
         L.orc_count_clamped.argtypes = [pp]
         L.orc_count_clamped.restype = C.c_int
         L.port_create.argtypes = [pp, fp]
@@ -209,6 +210,18 @@ def tess_levels(n: int, camera) -> np.ndarray:
     cam = np.asarray(camera, dtype=np.float64)
     out = np.empty((2 * n * n, 4))
     lib().orc_tess_levels(n, _p(cam, C.c_double), _p(out, C.c_double))
+    return out
+
+
+def shade(vertices: np.ndarray, camera, sun_direction, sea_color, sky: np.ndarray) -> np.ndarray:
+    """ocean_fs.glsl's colour at each vertex (n x 8 -> n x 4): orc_shade.  sky:
+    (6, S, S, 4) cube map, faces +X, -X, +Y, -Y, +Z, -Z."""
+    v = np.ascontiguousarray(vertices, dtype=np.float64)
+    sk = np.ascontiguousarray(sky, dtype=np.float64)
+    vec = [np.asarray(x, dtype=np.float64) for x in (camera, sun_direction, sea_color)]
+    out = np.empty((v.shape[0], 4))
+    lib().orc_shade(_p(v, C.c_double), v.shape[0], *[_p(x, C.c_double) for x in vec], _p(sk, C.c_double),
+                    sk.shape[1], _p(out, C.c_double))
     return out
 
 

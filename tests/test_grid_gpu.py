@@ -99,3 +99,57 @@ def test_grid_argument_errors(torch_cuda, ocean_lib):
     for bad in (ocean_lib.grid_params(3), ocean_lib.grid_params(0), ocean_lib.grid_params(2, float("nan"))):
         with pytest.raises(ocean_lib.OceanError):
             ocean_lib.displace_grid(*maps, bad, out)
+
+
+def test_shade_grid(torch_cuda, ocean_lib, oracle_mod):
+    """ocean_fs.glsl at displaced vertices against the FP64 oracle: random
+    vertices and cube map (1e-5 absolute on the 0..1 colours, 1e-3 where the
+    reflected ray lies within 1e-4 of a cube-map face edge, where the face choice
+    may differ between FP32 and FP64)."""
+    torch = torch_cuda
+    rng = np.random.default_rng(12)
+    n = 20000
+    v = np.zeros((n, 8), dtype=np.float32)
+    v[:, :3] = rng.uniform(-60, 60, (n, 3))
+    nrm = rng.standard_normal((n, 3)) * 0.4 + np.array([0, 1, 0])
+    v[:, 3:6] = nrm / np.linalg.norm(nrm, axis=1)[:, None]      # unit normals, as the normal map holds
+    sky = rng.uniform(0, 3, (6, 16, 16, 4)).astype(np.float32)
+    cam, sun, sea = (2.0, 25.0, -7.0), (0.3, -0.85, 0.2), (0.0, 0.12, 0.3)
+    dev = torch.device("cuda")
+    vt, skt = torch.tensor(v, device=dev), torch.tensor(sky, device=dev)
+    out = torch.empty((n, 4), device=dev)
+    ocean_lib.shade_grid(vt, cam, sun, sea, skt, out)
+    torch.cuda.synchronize()
+    got = out.cpu().numpy().astype(np.float64)
+    want = oracle_mod.shade(v.astype(np.float64), cam, sun, sea, sky.astype(np.float64))
+    err = np.abs(got - want).max(1)
+    Vv = np.asarray(cam) - v[:, :3].astype(np.float64)
+    Vv /= np.linalg.norm(Vv, axis=1)[:, None]
+    N = v[:, 3:6].astype(np.float64)
+    R = 2 * np.sum(N * Vv, 1)[:, None] * N - Vv
+    a = np.sort(np.abs(R), 1)
+    near_edge = (a[:, 2] - a[:, 1]) < 1e-4 * a[:, 2]
+    assert np.isfinite(got).all()
+    assert err[~near_edge].max() < 1e-5
+
+
+def test_frame_grid_shade_pipeline(torch_cuda, ocean_lib, oracle_mod):
+    """frame -> displaced grid -> shaded vertices, end to end on the device."""
+    torch = torch_cuda
+    d = P.c1()
+    N = d["N"]
+    dev = torch.device("cuda")
+    bufs = [torch.empty((N, N), device=dev) for _ in range(3)] + [torch.empty((N, N, 4), device=dev)]
+    with ocean_lib.Ocean(P.lib_params(d), seed=d["seed"]) as oc:
+        oc.update(2.5, *bufs)
+    g = ocean_lib.grid_params(256, 16.0, 0.5, (0.0, 12.0, 0.0))
+    verts = torch.empty((257 * 257, 8), device=dev)
+    ocean_lib.displace_grid(*bufs, g, verts)
+    sky = torch.ones((6, 4, 4, 4), device=dev) * 0.5
+    cols = torch.empty((257 * 257, 4), device=dev)
+    ocean_lib.shade_grid(verts, (0.0, 12.0, 0.0), (0.0, -0.7071, 0.7071), (0.0, 0.1, 0.2), sky, cols)
+    torch.cuda.synchronize()
+    want = oracle_mod.shade(verts.cpu().numpy().astype(np.float64), (0.0, 12.0, 0.0), (0.0, -0.7071, 0.7071),
+                            (0.0, 0.1, 0.2), sky.cpu().numpy().astype(np.float64))
+    assert np.abs(cols.cpu().numpy() - want).max() < 1e-5
+    assert np.isfinite(cols.cpu().numpy()).all()

@@ -59,3 +59,49 @@ def test_tess_levels_match_numpy(oracle_mod):
         got = oracle_mod.tess_levels(n, cam)
         assert np.array_equal(got, _levels_np(n, cam))
         assert set(np.unique(got)) <= {1.0, 5.0, 10.0, 20.0}
+
+
+def _cube_np(sky, r):
+    S = sky.shape[1]
+    ax, ay, az = np.abs(r[:, 0]), np.abs(r[:, 1]), np.abs(r[:, 2])
+    xm = (ax >= ay) & (ax >= az)
+    ym = ~xm & (ay >= az)
+    zm = ~xm & ~ym
+    face = np.where(xm, np.where(r[:, 0] >= 0, 0, 1), np.where(ym, np.where(r[:, 1] >= 0, 2, 3),
+                                                                np.where(r[:, 2] >= 0, 4, 5)))
+    ma = np.where(xm, ax, np.where(ym, ay, az))
+    sc = np.select([face == 0, face == 1, face == 2, face == 3, face == 4], [-r[:, 2], r[:, 2], r[:, 0], r[:, 0], r[:, 0]],
+                   -r[:, 0])
+    tc = np.select([face == 2, face == 3], [r[:, 2], -r[:, 2]], -r[:, 1])
+    s = 0.5 * (sc / ma + 1) * S - 0.5
+    t = 0.5 * (tc / ma + 1) * S - 0.5
+    s0, t0 = np.floor(s), np.floor(t)
+    ws, wt = (s - s0)[:, None], (t - t0)[:, None]
+    cl = lambda i: np.clip(i.astype(np.int64), 0, S - 1)
+    sa, sb, ta, tb = cl(s0), cl(s0 + 1), cl(t0), cl(t0 + 1)
+    f = sky[face]
+    g = lambda tt, ss: f[np.arange(len(r)), tt, ss, :3]
+    return (g(ta, sa) * (1 - ws) + g(ta, sb) * ws) * (1 - wt) + (g(tb, sa) * (1 - ws) + g(tb, sb) * ws) * wt
+
+
+def test_shade_matches_numpy(oracle_mod):
+    rng = np.random.default_rng(8)
+    n = 4000
+    v = np.zeros((n, 8))
+    v[:, :3] = rng.uniform(-50, 50, (n, 3))
+    nrm = rng.standard_normal((n, 3)) * 0.4 + np.array([0, 1, 0])
+    v[:, 3:6] = nrm / np.linalg.norm(nrm, axis=1)[:, None]      # unit normals, as the normal map holds
+    sky = rng.uniform(0, 3, (6, 7, 7, 4))
+    cam, sun, sea = np.array([1.0, 20.0, -3.0]), np.array([0.2, -0.9, 0.3]), np.array([0.0, 0.1, 0.3])
+    got = oracle_mod.shade(v, cam, sun, sea, sky)
+    V = cam - v[:, :3]
+    V /= np.linalg.norm(V, axis=1)[:, None]
+    N = v[:, 3:6]
+    nv = np.sum(N * V, 1)
+    R = 2 * nv[:, None] * N - V
+    F = 0.04 + 0.96 * (1 - np.maximum(nv, 0)) ** 5
+    nl = np.maximum(-(N @ sun), 0)
+    col = nl[:, None] * (sea * (1 - F[:, None]) + _cube_np(sky, R) * F[:, None])
+    want = (col / (col + 1)) ** (1 / 2.2)
+    assert np.abs(got[:, :3] - want).max() < 1e-12
+    assert np.all(got[:, 3] == 1.0)
