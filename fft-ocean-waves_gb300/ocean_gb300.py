@@ -229,6 +229,84 @@ def shade_grid(vertices, camera, sun_direction, sea_color, sky, colors, stream=N
                                   _stream(stream)))
 
 
+def _png_channel0(path: str):
+    """Channel 0 of an 8-bit, non-interlaced PNG (gray, gray+alpha, RGB or
+    RGBA) as a uint8 array (height, width): chunk walk, zlib inflate, per-row
+    filter reversal (filter types 0-4 of the PNG specification)."""
+    import struct
+    import zlib
+    import numpy as np
+    with open(path, "rb") as fh:
+        data = fh.read()
+    if data[:8] != b"\x89PNG\r\n\x1a\n":
+        raise ValueError(f"{path}: not a PNG file")
+    pos, idat, hdr = 8, [], None
+    while pos < len(data):
+        (ln,) = struct.unpack(">I", data[pos:pos + 4])
+        typ, body = data[pos + 4:pos + 8], data[pos + 8:pos + 8 + ln]
+        if typ == b"IHDR":
+            hdr = struct.unpack(">IIBBBBB", body)
+        elif typ == b"IDAT":
+            idat.append(body)
+        elif typ == b"IEND":
+            break
+        pos += 12 + ln
+    if hdr is None:
+        raise ValueError(f"{path}: no IHDR chunk")
+    w, h, depth, ctype, _, _, interlace = hdr
+    chans = {0: 1, 2: 3, 4: 2, 6: 4}.get(ctype)
+    if depth != 8 or chans is None or interlace:
+        raise ValueError(f"{path}: only 8-bit non-interlaced gray/RGB(A) PNGs are supported")
+    raw = np.frombuffer(zlib.decompress(b"".join(idat)), dtype=np.uint8)
+    stride = w * chans
+    raw = raw.reshape(h, stride + 1)
+    img = np.zeros((h, stride), dtype=np.int32)
+    prev = np.zeros(stride, dtype=np.int32)
+    for y in range(h):
+        f, line = raw[y, 0], raw[y, 1:].astype(np.int32)
+        out = np.empty(stride, dtype=np.int32)
+        if f == 0:
+            out[:] = line
+        elif f == 2:
+            out[:] = (line + prev) & 255
+        else:
+            for i in range(stride):
+                left = out[i - chans] if i >= chans else 0
+                up, ul = prev[i], (prev[i - chans] if i >= chans else 0)
+                if f == 1:
+                    pr = left
+                elif f == 3:
+                    pr = (left + up) >> 1
+                elif f == 4:
+                    p_ = left + up - ul
+                    pa, pb, pc = abs(p_ - left), abs(p_ - up), abs(p_ - ul)
+                    pr = left if (pa <= pb and pa <= pc) else (up if pb <= pc else ul)
+                else:
+                    raise ValueError(f"{path}: bad filter type {f}")
+                out[i] = (line[i] + pr) & 255
+        img[y] = out
+        prev = out
+    return img[:, ::chans].astype(np.uint8)
+
+
+def noise_from_pngs(paths, N: int | None = None):
+    """The reference's noise textures (data/noise/LDR_LLL1_{0..3}.png,
+    main.cpp:1085-1088) as ocean_create's noise: 4 planes of N x N floats,
+    channel 0 / 255 (the shaders read .r of an unsigned-normalised texture;
+    tilde_h0_k_cs.glsl clamps to [0.001, 1]).  N defaults to the texture size;
+    another N samples texel floor(x * size / N) (nearest)."""
+    import numpy as np
+    planes = [_png_channel0(p) for p in paths]
+    if len(planes) != 4:
+        raise ValueError("four noise textures are needed")
+    H, W = planes[0].shape
+    if any(p.shape != (H, W) for p in planes):
+        raise ValueError("the noise textures differ in size")
+    N = N or W
+    ys, xs = (np.arange(N) * H) // N, (np.arange(N) * W) // N
+    return np.stack([p[np.ix_(ys, xs)] for p in planes]).astype(np.float32) / np.float32(255.0)
+
+
 def compute_h0(params: Params, noise_dev, h0_dev, stream=None) -> None:
     cp = params.c()
     check(load().ocean_compute_h0(C.byref(cp), _addr(noise_dev), _addr(h0_dev), _stream(stream)))
