@@ -6,8 +6,6 @@
 // intermediate (in place of m_tilde_h0_t_* and m_ping_pong), the twiddle
 // table (in place of m_twiddle_factors) and, optionally, headless output
 // buffers (m_dx, m_dy, m_dz, m_normal_map).
-#include <cuda.h>
-#include <cudaTypedefs.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -57,8 +55,6 @@ int validate(const ocean_params* p)
     if (p->flags & ~OCEAN_FLAG_LITERAL_CONJ) return fail(OCEAN_ERR_INVALID, "unknown flag bits");
     return OCEAN_OK;
 }
-
-// cuTensorMapEncodeTiled through the runtime's driver entry point (no -lcuda).
 
 double gravity_of(const ocean_params& p) { return p.gravity > 0.0f ? (double)p.gravity : 9.81; }
 
@@ -346,11 +342,14 @@ int ocean_set_params(ocean_t* o, const ocean_params* params)
     int rc = validate(params);
     if (rc) return rc;
     if (params->N != o->N) return fail(OCEAN_ERR_INVALID, "ocean_set_params cannot change N");
+    // frames of this handle may be in flight on any stream: they read the
+    // spectrum that is about to be rebuilt
+    cudaError_t e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) return cuda_fail(e, "ocean_set_params: pending work");
     o->p = *params;
     o->set_consts();
     if ((rc = o->build_h0(0)) != OCEAN_OK) return rc;
-    cudaError_t e = cudaStreamSynchronize(0);
-    if (e != cudaSuccess) return cuda_fail(e, "h0 init");
+    if ((e = cudaStreamSynchronize(0)) != cudaSuccess) return cuda_fail(e, "h0 init");
     return OCEAN_OK;
 }
 

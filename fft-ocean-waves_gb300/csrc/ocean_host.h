@@ -1,7 +1,6 @@
 // ocean_host.h -- host-side helpers shared by the C-ABI translation units
 // (single tiles in ocean_abi.cpp, batches in ocean_batch.cpp).
 #pragma once
-#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <string>

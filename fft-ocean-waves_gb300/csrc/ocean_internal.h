@@ -1,7 +1,6 @@
 // ocean_internal.h -- kernel launch interface shared by the host code and the
 // CUDA translation units.  Not part of the public ABI.
 #pragma once
-#include <cuda.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 

@@ -16,7 +16,6 @@
 // until the process exits.  In host code their names are only stand-ins: the
 // device addresses are obtained with cudaGetSymbolAddress once per device, with
 // that device current, on the first call made on that device.
-#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <cmath>

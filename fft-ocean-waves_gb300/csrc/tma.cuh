@@ -1,13 +1,13 @@
 // tma.cuh -- Blackwell asynchronous copies into shared memory (inline PTX):
-// mbarrier transaction barriers, 1-D bulk copies (cp.async.bulk) and 2-D
-// tensor-tiled copies (cp.async.bulk.tensor), plus a bounded barrier wait.
+// mbarrier transaction barriers and 1-D bulk copies (cp.async.bulk; every
+// staged object -- spectrum rows, column-pair blocks, twiddle plans -- is one
+// contiguous run), plus a bounded barrier wait.
 //
 // Every wait is bounded by the global nanosecond timer.  On time-out the waiter
 // records OCEAN_DEVICE_TIMEOUT in the handle's device status word, waits once
 // more (bounded) for its copies in flight, and the block returns as a whole;
 // the host reads the status with ocean_device_status().
 #pragma once
-#include <cuda.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -80,17 +80,6 @@ __device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t by
                      smem_u32(dst)),
                  "l"(src), "r"(bytes), "r"(smem_u32(bar))
                  : "memory");
-}
-
-// 2-D tensor-tiled copy of the box at coordinates (x, y) (x innermost) of
-// `map` into shared memory (dense box, row-major).
-__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, int x, int y, uint64_t* bar)
-{
-    asm volatile(
-        "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], "
-        "[%4];" ::"r"(smem_u32(dst)),
-        "l"(map), "r"(x), "r"(y), "r"(smem_u32(bar))
-        : "memory");
 }
 
 // Block-wide wait executed by thread 0 with the result broadcast through

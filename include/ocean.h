@@ -128,7 +128,9 @@ OCEAN_API int ocean_get_outputs(ocean_t* ocean, ocean_outputs* out);
 /* Replace the spectrum parameters (same N) and rebuild h0 from the stored
  * noise.  The reference reads GUI edits of wind speed and amplitude
  * (main.cpp:348-358) but never re-runs tilde_h0_k(), so they have no effect
- * there; here they do.  Synchronous. */
+ * there; here they do.  Synchronous: it first waits for all work on the
+ * current device (frames of this handle in flight on any stream), then
+ * rebuilds h0 and the combined spectrum and waits for that too. */
 OCEAN_API int ocean_set_params(ocean_t* ocean, const ocean_params* params);
 OCEAN_API int ocean_get_params(const ocean_t* ocean, ocean_params* params);
 
