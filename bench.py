@@ -130,24 +130,28 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
-def dist_init():
+def dist_init(backend="nccl"):
+    """One process per GPU (torchrun env).  Tiles are replicas: the ranks only
+    meet in the timing barriers."""
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
     if world > 1:
         import torch.distributed as dist
         import torch
-        torch.cuda.set_device(local)
-        dist.init_process_group("nccl")
+        if backend == "nccl":
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend)
     return world, rank, local
 
 
-def barrier_max(world, value):
+def barrier_max(world, value, device="cuda"):
+    """Barrier, then the maximum of `value` over the ranks (the job's time)."""
     if world == 1:
         return value
     import torch
     import torch.distributed as dist
-    t = torch.tensor([value], dtype=torch.float64, device="cuda")
+    t = torch.tensor([value], dtype=torch.float64, device=device)
     dist.barrier()
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
