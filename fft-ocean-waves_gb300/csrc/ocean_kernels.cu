@@ -520,11 +520,11 @@ struct ColCfg {
     static_assert(FIELD_BYTES % 16 == 0, "bulk copy size");
 };
 
-// Line triple of column pair (x0, x0+1): line 0 = Dy + i*Dx of column x0,
-// line 1 the same of column x0+1, line 2 = Dz(x0) + i*Dz(x0+1).  Rows y > N/2
-// are the conjugates of rows N-y (the row-transformed spectra are Hermitian in
-// y), so the inputs come from rows 0..N/2 of the intermediate, whose column
-// pairs are contiguous: one 1-D bulk copy per field stages them.
+// Line triple of column pair (x0, x0+1): line f = field f of column x0 + i *
+// field f of column x0+1 (f = 0: Dx, 1: Dy, 2: Dz).  Rows y > N/2 are the
+// conjugates of rows N-y (the row-transformed spectra are Hermitian in y), so
+// the inputs come from rows 0..N/2 of the intermediate, whose column pairs are
+// contiguous: one 1-D bulk copy per field stages them.
 template <int N>
 __global__ void __launch_bounds__(ColCfg<N>::THREADS) k_col_fft(const __grid_constant__ ColArgs a)
 {
@@ -560,31 +560,27 @@ __global__ void __launch_bounds__(ColCfg<N>::THREADS) k_col_fft(const __grid_con
     }
     if (!block_wait(&bar, 0, &wait_ok, a.status)) return;
 
+    // Line li of pair pl holds field f = li % 3 (0: Dx, 1: Dy, 2: Dz) of both
+    // columns, f(x0) + i*f(x0+1): the row-transformed spectra are Hermitian in
+    // y, so the transform's real and imaginary parts are the two columns.
     const int li = tid / L::G, t = tid % L::G;
-    const int kind = li % 3, pl = li / 3;
-    const int x0   = 2 * (pair0 + pl);
+    const int f  = li % 3, pl = li / 3;
+    const int x0 = 2 * (pair0 + pl);
     // Input r of thread t is row y = t + r*G (G = N/R1, t < G): rows below
     // N/2 for r < R1/2, the conjugate of row N - y for r > R1/2, and for
     // r = R1/2 row N/2 - t, conjugated unless t = 0 (y = N/2).  So every
-    // shared-memory offset is a per-thread base plus a constant.
+    // shared-memory offset is a per-thread base plus a constant, and each read
+    // is the 16-byte (column x0, column x0+1) pair of one row.
     constexpr int G = L::G;
-    const float2* fy = work + ((size_t)(1 * CF::PAIRS + pl) * H) * 2 + (kind & 1);   // Dy (x0 or x0+1)
-    const float2* fx = work + ((size_t)(0 * CF::PAIRS + pl) * H) * 2 + (kind & 1);   // Dx
-    const float2* fz = work + ((size_t)(2 * CF::PAIRS + pl) * H) * 2;                // Dz pair
+    const float2* fp = work + ((size_t)(f * CF::PAIRS + pl) * H) * 2;
     float2 v[L::E];
 #pragma unroll
     for (int r = 0; r < L::E; ++r) {
-        const int  ys  = r < L::R1 / 2 ? t + r * G : (r == L::R1 / 2 ? N / 2 - t : N - t - r * G);
-        const bool cj  = r > L::R1 / 2 || (r == L::R1 / 2 && t != 0);
-        float2 p, q;
-        if (kind < 2) {
-            p = fy[2 * ys];
-            q = fx[2 * ys];
-        } else {
-            const float4 z = *reinterpret_cast<const float4*>(fz + 2 * ys);
-            p = make_float2(z.x, z.y);                                     // Dz(x0)
-            q = make_float2(z.z, z.w);                                     // Dz(x0+1)
-        }
+        const int    ys = r < L::R1 / 2 ? t + r * G : (r == L::R1 / 2 ? N / 2 - t : N - t - r * G);
+        const bool   cj = r > L::R1 / 2 || (r == L::R1 / 2 && t != 0);
+        const float4 z  = *reinterpret_cast<const float4*>(fp + 2 * ys);
+        float2       p  = make_float2(z.x, z.y);                          // column x0
+        float2       q  = make_float2(z.z, z.w);                          // column x0+1
         if (cj) { p.y = -p.y; q.y = -q.y; }
         v[r] = make_float2(p.x - q.y, p.y + q.x);                          // p + i*q
     }
@@ -592,31 +588,19 @@ __global__ void __launch_bounds__(ColCfg<N>::THREADS) k_col_fft(const __grid_con
     pdl_launch_dependents();                                 // k_col_out may start its set-up
     line_fft<L, +1>(v, work + li * L::NPAD, tw_s, t, li);
 
-    float* const tm = a.tmap + (size_t)unit * tmap_len(N);
-    const float  sa = cu->scale, sb = cu->scale * cu->lambda;
     // output y = pos(t, e) is t plus an even constant: the (-1)^(x+y) sign is
-    // the thread's
+    // the thread's, and the two columns' signs are opposite.  Dy is scaled by
+    // 1/(2N^2) (the 1/N^2 inversion and the Hermitian half), Dx and Dz also by
+    // lambda.
     static_assert(L::G % 2 == 0 && LineOut<L>::NS % 2 == 0, "even output offsets");
-    if (kind < 2) {
-        const int   x  = x0 + kind;
-        const float sg = ((x + t) & 1) ? -1.0f : 1.0f;
-        const float ka = sg * sa, kb = sg * sb;
-        float* ox = tm + (size_t)x * N + t;                       // Dx column x
-        float* oy = tm + ((size_t)N + x) * N + t;                 // Dy column x
+    float* const tm = a.tmap + (size_t)unit * tmap_len(N);
+    const float  sg = ((x0 + t) & 1) ? -1.0f : 1.0f;
+    const float  k  = sg * (f == 1 ? cu->scale : cu->scale * cu->lambda);
+    float* const o  = tm + ((size_t)f * N + x0) * N + t;     // field f, columns x0 and x0+1
 #pragma unroll
-        for (int e = 0; e < L::E; ++e) {
-            oy[LineOut<L>::pos(0, e)] = ka * v[e].x;
-            ox[LineOut<L>::pos(0, e)] = kb * v[e].y;
-        }
-    } else {
-        const float sg = ((x0 + t) & 1) ? -1.0f : 1.0f;
-        const float kb = sg * sb;
-        float* oz = tm + ((size_t)2 * N + x0) * N + t;            // Dz columns x0, x0+1
-#pragma unroll
-        for (int e = 0; e < L::E; ++e) {
-            oz[LineOut<L>::pos(0, e)]     = kb * v[e].x;
-            oz[N + LineOut<L>::pos(0, e)] = -kb * v[e].y;
-        }
+    for (int e = 0; e < L::E; ++e) {
+        o[LineOut<L>::pos(0, e)]     = k * v[e].x;
+        o[N + LineOut<L>::pos(0, e)] = -k * v[e].y;
     }
 }
 
