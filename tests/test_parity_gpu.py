@@ -163,3 +163,67 @@ def test_back_to_back_frames_bitwise(torch_cuda, ocean_lib, N):
         for k in range(F):
             for a, b in zip(sets[k], ref[k % 2]):
                 assert torch.equal(a, b), (N, k)
+
+
+@pytest.mark.parametrize("N", [64, 1024])
+def test_calm_sea_is_exact(torch_cuda, ocean_lib, N):
+    """Amplitude 0: h0 = 0, so every displacement is exactly 0, every normal
+    exactly (0, 1, 0) and the Jacobian exactly 1, at any time."""
+    d = dict(P.c2(N), amplitude=0.0)
+    _, outs = _run(torch_cuda, ocean_lib, d, [0.0, 123.456])
+    for o in outs:
+        for k in ("dx", "dy", "dz"):
+            assert not np.any(o[k]), k
+        nj = o["nj"]
+        assert np.all(nj[..., 0] == 0.0) and np.all(nj[..., 1] == 1.0) and np.all(nj[..., 2] == 0.0)
+        assert np.all(nj[..., 3] == 1.0)
+
+
+@pytest.mark.parametrize("N", [64, 1024])
+def test_no_choppiness(torch_cuda, ocean_lib, oracle_mod, N):
+    """lambda = 0: the horizontal displacements are exactly 0 and the Jacobian
+    exactly 1; the height field still matches the oracle."""
+    d = dict(P.c2(N), choppiness=0.0)
+    p = P.oracle_params(d)
+    h0ref = oracle_mod.h0(p, oracle_mod.noise(d["seed"], N))
+    _, outs = _run(torch_cuda, ocean_lib, d, [2.5])
+    o = outs[0]
+    assert not np.any(o["dx"]) and not np.any(o["dz"])
+    assert np.all(o["nj"][..., 3] == 1.0)
+    ref = oracle_mod.update(p, h0ref, 2.5)
+    assert rel_l2(o["dy"], ref["dy"]) <= TOL
+    assert rel_l2(o["nj"][..., :3], ref["nj"][..., :3]) <= TOL
+
+
+@pytest.mark.parametrize("N", [32, 1024])
+def test_negative_time(torch_cuda, ocean_lib, oracle_mod, N):
+    """Negative t runs the spectrum backwards, as the formula does."""
+    d = P.c2(N)
+    p = P.oracle_params(d)
+    h0ref = oracle_mod.h0(p, oracle_mod.noise(d["seed"], N))
+    _, outs = _run(torch_cuda, ocean_lib, d, [-3.75])
+    _check(outs[0], oracle_mod.update(p, h0ref, -3.75))
+
+
+def test_update_argument_errors(torch_cuda, ocean_lib):
+    """Non-finite times and misaligned output pointers are refused before any
+    launch; the handle keeps working afterwards."""
+    torch = torch_cuda
+    N = 64
+    d = P.c2(N)
+    dev = torch.device("cuda")
+    with ocean_lib.Ocean(P.lib_params(d), seed=d["seed"]) as oc:
+        dx, dy, dz = (torch.zeros((N, N), device=dev) for _ in range(3))
+        nj = torch.zeros((N, N, 4), device=dev)
+        for t in (float("nan"), float("inf"), -float("inf")):
+            with pytest.raises(ocean_lib.OceanError):
+                oc.update(t, dx, dy, dz, nj)
+        flat = torch.zeros(N * N + 1, device=dev)
+        with pytest.raises(ocean_lib.OceanError):
+            oc.update(1.0, flat[1:].view(N, N), dy, dz, nj)      # 4-byte offset: not 16-byte aligned
+        torch.cuda.synchronize()
+        assert not torch.any(dx) and not torch.any(nj)
+        oc.update(1.0, dx, dy, dz, nj)
+        torch.cuda.synchronize()
+        oc.device_status()
+        assert torch.any(dy)
