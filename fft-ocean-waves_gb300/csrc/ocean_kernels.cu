@@ -3,8 +3,10 @@
 // One frame is three kernels, chained by programmatic dependent launch (the
 // reference dispatches 6*log2(N)+5 full-grid passes, main.cpp:240-244):
 //
-//   k_row_pass  spectrum evolution + choppy multiply (tilde_h0_t_cs.glsl:70-131)
-//               fused into the horizontal inverse FFT (butterfly_cs.glsl:54-91).
+//   k_row_ws    spectrum evolution + choppy multiply (tilde_h0_t_cs.glsl:70-131)
+//   k_row_pass  fused into the horizontal inverse FFT (butterfly_cs.glsl:54-91);
+//               k_row_ws (N >= 512) splits each CTA into prepass and transform
+//               warps, k_row_pass (below 512) runs both on every warp.
 //               Only Re of the 2-D inverse transform is kept
 //               (inversion_cs.glsl:35), so each field is first made Hermitian,
 //               X_H(k) = (X(k) + conj X(-k))/2, which leaves Re unchanged and
@@ -18,8 +20,8 @@
 //
 //   k_col_fft   vertical inverse FFT (butterfly_cs.glsl:95-132) of a column
 //               pair per line triple, two real results packed per complex
-//               transform (Dy + i*Dx per column, Dz of both columns), loaded
-//               straight into registers from the L2-resident intermediate,
+//               transform (one field of both columns per line), staged by
+//               1-D bulk copies from the L2-resident intermediate,
 //               fused with the (-1)^(x+y)/N^2 inversion (inversion_cs.glsl:29-41)
 //               and the lambda scaling; writes the maps column-major.
 //
