@@ -426,6 +426,30 @@ __global__ void __launch_bounds__(RowWsCfg<N, FROM_H0>::THREADS, RowWsCfg<N, FRO
     __syncthreads();
     pdl_launch_dependents();
 
+    // The first job's line inputs are computed by every warp: until they
+    // exist the transform warps have nothing to do.  (Every CTA has a job:
+    // the grid is at most the number of items.)
+    {
+        const int item = blockIdx.x, tile = item / WC::ITEMS, yp = item % WC::ITEMS;
+        if (tid == 0 && !mbar_wait_bounded(&bars[0], 0)) {
+            atomicOr(a.status, kDeviceTimeout);
+            (void)mbar_wait_bounded(&bars[0], 0);
+            wait_ok = 0;
+        }
+        __syncthreads();                                     // the rows are in (or the wait gave up)
+        const FrameConsts fc = MULTI ? a.fcs[tile * a.S] : a.fc0;
+        for (int x = tid; x <= N / 2; x += WC::THREADS)
+            row_position<N, FROM_H0, L::NPAD>(a, ring, bufs, tile, x, yp, fc);
+        __syncthreads();                                     // job 0's inputs are complete
+        if (nsmp == 1 && tid == 0) {                         // stage 0 is consumed: refill it
+            const int next = item + WC::STAGES * gridDim.x;
+            if (next < n_items) {
+                fence_proxy_async_smem();
+                row_issue<N, FROM_H0>(a, ring, &bars[0], next);
+            }
+        }
+    }
+
     if (tid < WC::FFT_THREADS) {
         const int li = tid / L::G, t = tid % L::G;           // line = field 0: Dx, 1: Dy, 2: Dz
         if (tid == 0 && !mbar_wait_bounded(&bar_tw, 0)) {
@@ -437,7 +461,7 @@ __global__ void __launch_bounds__(RowWsCfg<N, FROM_H0>::THREADS, RowWsCfg<N, FRO
             const int b = j & 1, ki = j / nsmp, smp = j - ki * nsmp;
             const int item = blockIdx.x + ki * gridDim.x, tile = item / WC::ITEMS, yp = item % WC::ITEMS;
             const int unit = MULTI ? tile * a.S + smp : 0;
-            named_sync(WC::BAR_FULL + b, WC::THREADS);       // the job's line inputs are complete
+            if (j > 0) named_sync(WC::BAR_FULL + b, WC::THREADS);   // the job's line inputs are complete
             float2* buf = bufs + b * WC::BUF + li * L::NPAD;
             float2  v[L::E];
 #pragma unroll
@@ -452,9 +476,9 @@ __global__ void __launch_bounds__(RowWsCfg<N, FROM_H0>::THREADS, RowWsCfg<N, FRO
         }
     } else {
         const int pt = tid - WC::FFT_THREADS;
-        uint32_t  phase_bits = 0;
-        bool      gave_up    = false;                         // a copy wait timed out: stop waiting
-        for (int j = 0; j < n_jobs; ++j) {
+        uint32_t  phase_bits = 1u;                            // stage 0's first phase went to job 0
+        bool      gave_up    = wait_ok == 0;                  // a copy wait timed out: stop waiting
+        for (int j = 1; j < n_jobs; ++j) {
             const int b = j & 1, ki = j / nsmp, smp = j - ki * nsmp;
             const int item = blockIdx.x + ki * gridDim.x, tile = item / WC::ITEMS, yp = item % WC::ITEMS;
             const int st = ki % WC::STAGES;
