@@ -220,15 +220,22 @@ __device__ __forceinline__ void row_modes(const RowArgs& a, const float2* rA, co
 // the modes (x, yp), (N-x, yp), (N-x, N-yp), (x, N-yp) share |k| (ix^2 and iz^2
 // are even) and so the phase.  rows: the pair's two staged rows (yp, then
 // N-yp); lines: the three line buffers (Dx, Dy, Dz, NPAD apart).
+// The phase part (c, sn = cos, sin of the phase; r = 1/|k| in mode units)
+// depends on the position and the time only, not on the staged rows.
+template <int N>
+__device__ __forceinline__ void row_phase(int x, int yp, const FrameConsts& fc, float& c, float& sn, float& r)
+{
+    const int ix = x - N / 2, iz = yp - N / 2;
+    mode_phase_r(ix * ix + iz * iz, fc, c, sn, r);
+}
+
 template <int N, bool FROM_H0, int NPAD>
 __device__ __forceinline__ void row_position(const RowArgs& a, const float2* rows, float2* lines, int tile, int x,
-                                             int yp, const FrameConsts& fc)
+                                             int yp, const FrameConsts& fc, float c, float sn, float r)
 {
     constexpr int EW = FROM_H0 ? 2 : 1;
     const int yq = (N - yp) & (N - 1), xm = (N - x) & (N - 1);
     const int ix = x - N / 2, iz = yp - N / 2;
-    float c, sn, r;
-    mode_phase_r(ix * ix + iz * iz, fc, c, sn, r);
     float2 g[4], d[4];
     row_modes<N, FROM_H0>(a, rows, rows + N * EW, tile, x, xm, yp, yq, fc.literal_conj, g, d);
     const float2 y0 = herm_sum(g[0], g[1], c, sn);
@@ -251,6 +258,15 @@ __device__ __forceinline__ void row_position(const RowArgs& a, const float2* row
         by[xm] = y1;
         bz[xm] = mul_mi(sz, uz1);
     }
+}
+
+template <int N, bool FROM_H0, int NPAD>
+__device__ __forceinline__ void row_position(const RowArgs& a, const float2* rows, float2* lines, int tile, int x,
+                                             int yp, const FrameConsts& fc)
+{
+    float c, sn, r;
+    row_phase<N>(x, yp, fc, c, sn, r);
+    row_position<N, FROM_H0, NPAD>(a, rows, lines, tile, x, yp, fc, c, sn, r);
 }
 
 // MULTI: more than one (tile, sample) unit per launch (batches).  The single
@@ -431,15 +447,26 @@ __global__ void __launch_bounds__(RowWsCfg<N, FROM_H0>::THREADS, RowWsCfg<N, FRO
     // the grid is at most the number of items.)
     {
         const int item = blockIdx.x, tile = item / WC::ITEMS, yp = item % WC::ITEMS;
+        const FrameConsts fc = MULTI ? a.fcs[tile * a.S] : a.fc0;
+        // the phases do not depend on the rows: computed while they arrive
+        constexpr int PP = (N / 2 + WC::THREADS) / WC::THREADS;   // positions per thread
+        float c[PP], sn[PP], r[PP];
+#pragma unroll
+        for (int k = 0; k < PP; ++k) {
+            const int x = tid + k * WC::THREADS;
+            if (x <= N / 2) row_phase<N>(x, yp, fc, c[k], sn[k], r[k]);
+        }
         if (tid == 0 && !mbar_wait_bounded(&bars[0], 0)) {
             atomicOr(a.status, kDeviceTimeout);
             (void)mbar_wait_bounded(&bars[0], 0);
             wait_ok = 0;
         }
         __syncthreads();                                     // the rows are in (or the wait gave up)
-        const FrameConsts fc = MULTI ? a.fcs[tile * a.S] : a.fc0;
-        for (int x = tid; x <= N / 2; x += WC::THREADS)
-            row_position<N, FROM_H0, L::NPAD>(a, ring, bufs, tile, x, yp, fc);
+#pragma unroll
+        for (int k = 0; k < PP; ++k) {
+            const int x = tid + k * WC::THREADS;
+            if (x <= N / 2) row_position<N, FROM_H0, L::NPAD>(a, ring, bufs, tile, x, yp, fc, c[k], sn[k], r[k]);
+        }
         __syncthreads();                                     // job 0's inputs are complete
         if (nsmp == 1 && tid == 0) {                         // stage 0 is consumed: refill it
             const int next = item + WC::STAGES * gridDim.x;
