@@ -529,9 +529,34 @@ def bench_grid(torch, og, dev, stream, flush, oc_maps, reps=20):
                 lt.append(ev[1].elapsed_time(ev[2]))
     v_ms, l_ms = sum(vt) / len(vt), sum(lt) / len(lt)
     nv = (n + 1) * (n + 1)
+    # the sky environment cube map of render_envmap() (512 x 512 faces) on
+    # seeded stand-in tables, and the shading of the grid's vertices from it
+    import numpy as np
+    rng = np.random.default_rng(5)
+    tr = torch.from_numpy(rng.random((64, 256, 4), dtype=np.float32)).to(dev)
+    ins = torch.from_numpy(rng.random((32, 128, 256, 4), dtype=np.float32) * np.float32(0.05)).to(dev)
+    sky = torch.empty((6, 512, 512, 4), device=dev)
+    colors = torch.empty((nv, 4), device=dev)
+    cam, sun = (0.0, 10.0, 0.0), og.sky_sun_direction(-0.4)
+    st, ct = [], []
+    with torch.cuda.stream(stream):
+        for r in range(reps + 3):
+            flush()
+            ev[0].record(stream)
+            og.sky_envmap(cam, sun, tr, ins, sky, stream=stream)
+            ev[1].record(stream)
+            og.shade_grid(verts, cam, sun, (0.0, 0.2, 0.3), sky, colors, stream=stream)
+            ev[2].record(stream)
+            torch.cuda.synchronize()
+            if r >= 3:
+                st.append(ev[0].elapsed_time(ev[1]))
+                ct.append(ev[1].elapsed_time(ev[2]))
+    s_ms, c_ms = sum(st) / len(st), sum(ct) / len(ct)
     return {"workload": f"grid of {n} squares (UV repeat 64) over N={dy.shape[0]} maps, L2 flushed",
             "vertices": nv, "displace_ms": round(v_ms, 4), "vertices_per_s": round(nv / (v_ms * 1e-3), 1),
-            "tess_levels_ms": round(l_ms, 4), "triangles_per_s": round(2 * n * n / (l_ms * 1e-3), 1)}
+            "tess_levels_ms": round(l_ms, 4), "triangles_per_s": round(2 * n * n / (l_ms * 1e-3), 1),
+            "sky_envmap_ms": round(s_ms, 4), "sky_texels_per_s": round(6 * 512 * 512 / (s_ms * 1e-3), 1),
+            "shade_ms": round(c_ms, 4), "shaded_vertices_per_s": round(nv / (c_ms * 1e-3), 1)}
 
 
 def run_reference(args, world, rank):

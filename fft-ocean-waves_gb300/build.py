@@ -38,6 +38,11 @@ def _deps():
         [os.path.join(ROOT, "include", "ocean.h"), os.path.abspath(__file__)]
 
 
+# Per-file flags: the sky map follows FP32 shader arithmetic without FMA
+# contraction, so that the oracle's plain-FP32 restatement reproduces it.
+PER_FILE_FLAGS = {"ocean_sky.cu": ["--fmad=false"]}
+
+
 def common_flags(extra=()):
     return ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC,-fvisibility=hidden", *GENCODE,
             "-I", os.path.join(ROOT, "include"), "--expt-relaxed-constexpr", *extra]
@@ -54,7 +59,7 @@ def build(force: bool = False, verbose: bool = False, extra_flags=()) -> str:
 
     def compile_one(src):
         obj = os.path.join(BUILD, os.path.basename(src) + ".o")
-        cmd = [nv, *common_flags(extra_flags), "-c", src, "-o", obj]
+        cmd = [nv, *common_flags(extra_flags), *PER_FILE_FLAGS.get(os.path.basename(src), []), "-c", src, "-o", obj]
         if verbose:
             print(" ".join(cmd), flush=True)
         r = subprocess.run(cmd, capture_output=True, text=True)

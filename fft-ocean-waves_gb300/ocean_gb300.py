@@ -36,7 +36,7 @@ EXPORTS = [
     "ocean_fill_noise", "ocean_bit_reversed_indices", "ocean_butterfly_table", "ocean_last_error",
     "ocean_version", "ocean_backward", "ocean_device_status", "ocean_batch_create", "ocean_batch_update",
     "ocean_batch_device_status", "ocean_batch_destroy", "ocean_update_noalloc", "ocean_displace_grid",
-    "ocean_grid_tess_levels", "ocean_shade_grid",
+    "ocean_grid_tess_levels", "ocean_shade_grid", "ocean_sky_envmap",
 ]
 OCEAN_GRAD_ACCUMULATE = 1
 
@@ -129,6 +129,7 @@ def load() -> C.CDLL:
     L.ocean_displace_grid.argtypes = [P(ocean_outputs), C.c_int32, P(ocean_grid_params), vp, vp]
     L.ocean_grid_tess_levels.argtypes = [P(ocean_grid_params), vp, vp]
     L.ocean_shade_grid.argtypes = [vp, C.c_int64, P(ocean_shade_params), vp, vp, vp]
+    L.ocean_sky_envmap.argtypes = [P(ocean_sky_params), vp, vp, vp, vp]
     L.ocean_last_error.restype = C.c_char_p
     for name in EXPORTS:
         if name not in ("ocean_destroy", "ocean_last_error", "ocean_batch_destroy"):
@@ -227,6 +228,59 @@ def shade_grid(vertices, camera, sun_direction, sea_color, sky, colors, stream=N
     p = ocean_shade_params(f3(camera), f3(sun_direction), f3(sea_color), int(sky.shape[1]))
     check(load().ocean_shade_grid(_addr(vertices), int(vertices.shape[0]), C.byref(p), _addr(sky), _addr(colors),
                                   _stream(stream)))
+
+
+class ocean_sky_params(C.Structure):
+    _fields_ = [("camera", C.c_float * 3), ("sun_direction", C.c_float * 3), ("earth_pos", C.c_float * 3),
+                ("beta_r", C.c_float * 3), ("mie_g", C.c_float), ("sun_intensity", C.c_float), ("size", C.c_int32)]
+
+
+# The reference's sky uniforms (main.cpp:80-84,149-158).
+SKY_EARTH_POS = (0.0, 6360010.0, 0.0)
+SKY_BETA_R = (0.0058 / 1000.0, 0.0135 / 1000.0, 0.0331 / 1000.0)
+SKY_MIE_G = 0.75
+SKY_SUN_INTENSITY = 100.0
+
+
+def sky_sun_direction(angle: float):
+    """SUN_DIR for the reference's GUI sun angle (main.cpp:151,157):
+    -normalize(0, sin a, cos a), in FP32 as glm computes it."""
+    import numpy as np
+    v = np.array([0.0, np.sin(np.float32(angle)), np.cos(np.float32(angle))], dtype=np.float32)
+    return tuple(float(x) for x in -(v * (np.float32(1.0) / np.sqrt(np.float32(v @ v)))))
+
+
+def sky_envmap(camera, sun_direction, transmittance, inscatter, cubemap, earth_pos=SKY_EARTH_POS, beta_r=SKY_BETA_R,
+               mie_g=SKY_MIE_G, sun_intensity=SKY_SUN_INTENSITY, stream=None) -> None:
+    """The sky environment cube map of render_envmap(): transmittance (64,
+    256, 4), inscatter (32, 128, 256, 4), cubemap (6, S, S, 4) output; device
+    tensors (float32)."""
+    f3 = lambda v: (C.c_float * 3)(*[float(x) for x in v])
+    p = ocean_sky_params(f3(camera), f3(sun_direction), f3(earth_pos), f3(beta_r), float(mie_g), float(sun_intensity),
+                         int(cubemap.shape[1]))
+    check(load().ocean_sky_envmap(C.byref(p), _addr(transmittance), _addr(inscatter), _addr(cubemap),
+                                  _stream(stream)))
+
+
+def load_sky_tables(texture_dir: str):
+    """The reference's sky tables from its data/texture directory (the .raw
+    files main.cpp:89-143 reads): transmittance (64, 256, 4), irradiance (16,
+    64, 4) and inscatter (32, 128, 256, 4) as float32 arrays, None for a file
+    that is absent (the reference ships without inscatter.raw)."""
+    import os
+    import numpy as np
+    shapes = {"transmittance": (64, 256, 4), "irradiance": (16, 64, 4), "inscatter": (32, 128, 256, 4)}
+    out = {}
+    for name, shape in shapes.items():
+        path = os.path.join(texture_dir, name + ".raw")
+        if not os.path.exists(path):
+            out[name] = None
+            continue
+        a = np.fromfile(path, dtype="<f4")
+        if a.size != int(np.prod(shape)):
+            raise ValueError(f"{path}: {a.size} floats, expected {int(np.prod(shape))}")
+        out[name] = a.reshape(shape)
+    return out
 
 
 def _png_channel0(path: str):

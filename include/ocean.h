@@ -254,6 +254,46 @@ typedef struct ocean_shade_params {
 OCEAN_API int ocean_shade_grid(const float* vertices, int64_t n_vertices, const ocean_shade_params* params,
                                const float* sky_cubemap, float* colors, void* stream);
 
+/* ---- Sky environment cube map (precomputed atmospheric scattering) ----- */
+
+/* Lookup-table sizes of the sky model (main.cpp:66-80): transmittance
+ * [64][256] RGBA (x = view-zenith parameter, y = altitude), inscatter
+ * [32][128][256] RGBA (x = sun-zenith x view-sun, 32 x 8; y = view zenith;
+ * z = altitude).  Row-major float32, as the reference's .raw texture files. */
+#define OCEAN_SKY_TRANSMITTANCE_W 256
+#define OCEAN_SKY_TRANSMITTANCE_H 64
+#define OCEAN_SKY_INSCATTER_W     256
+#define OCEAN_SKY_INSCATTER_H     128
+#define OCEAN_SKY_INSCATTER_D     32
+
+/* Uniforms of the sky model (main.cpp:149-158, atmosphere.glsl:37-41); the
+ * reference's values are earth_pos (0, 6360010, 0), sun_intensity 100,
+ * beta_r (0.0058, 0.0135, 0.0331) / 1000, mie_g 0.75, and sun_direction =
+ * -normalize(0, sin a, cos a) for the GUI sun angle a. */
+typedef struct ocean_sky_params {
+    float   camera[3];          /* u_CameraPos (world units, y up)                 */
+    float   sun_direction[3];   /* SUN_DIR: unit vector the shader dots view rays with */
+    float   earth_pos[3];       /* EARTH_POS                                       */
+    float   beta_r[3];          /* betaR (Rayleigh scattering per unit length)     */
+    float   mie_g;              /* mieG                                            */
+    float   sun_intensity;      /* SUN_INTENSITY                                   */
+    int32_t size;               /* cube-map face edge in texels (the reference: 512) */
+} ocean_sky_params;
+
+/* The sky environment cube map of render_envmap() (main.cpp:500-523,
+ * sky_envmap_fs.glsl:25-38): per texel of the six faces, the sun disk times
+ * the extinction plus SkyRadiance() (atmosphere.glsl:152-199), with the
+ * tables sampled as the reference's GL_LINEAR / CLAMP_TO_EDGE textures.
+ * Faces +X, -X, +Y, -Y, +Z, -Z in the OpenGL cube-map orientation (the
+ * capture views of main.cpp:1463-1470), texel centres; output
+ * [6][size][size] RGBA float32 (alpha 1), the layout ocean_shade_grid reads.
+ * The reference stores the map as RGB16F; this writes float32.
+ * transmittance and inscatter are device tables of the sizes above (the
+ * reference ships transmittance.raw; its inscatter.raw is missing, so the
+ * caller supplies one).  All pointers 16-byte aligned.  One launch. */
+OCEAN_API int ocean_sky_envmap(const ocean_sky_params* params, const float* transmittance, const float* inscatter,
+                               float* cubemap, void* stream);
+
 /* ---- Adjoint --------------------------------------------------------- */
 
 /* Flags for ocean_backward */

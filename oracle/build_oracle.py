@@ -1,8 +1,8 @@
 """Build recipe for the oracle shared library (test infrastructure only).
 
 Compiles oracle/ocean_oracle.c with the host C compiler into
-oracle/_build/libocean_oracle.so (OpenMP enabled, no fast-math).  Portable C:
-builds the same on x86_64 and aarch64.
+oracle/_build/libocean_oracle.so (OpenMP enabled, no fast-math, no FMA
+contraction: the FP32 parts round the same on x86_64 and aarch64).  Portable C.
 """
 import os
 import subprocess
@@ -19,7 +19,7 @@ def build(force: bool = False, quiet: bool = True) -> str:
     if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= os.path.getmtime(SRC):
         return LIB
     cc = os.environ.get("CC", "gcc")
-    cmd = [cc, "-O2", "-std=c11", "-fPIC", "-shared", "-fopenmp", "-fno-fast-math",
+    cmd = [cc, "-O2", "-std=c11", "-fPIC", "-shared", "-fopenmp", "-fno-fast-math", "-ffp-contract=off",
            "-o", LIB + ".tmp", SRC, "-lm"]
     if not quiet:
         print(" ".join(cmd))

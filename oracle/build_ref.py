@@ -20,7 +20,7 @@ REF = os.environ.get("OCEAN_REFERENCE_DIR", "/root/reference")
 OUT = os.path.join(HERE, "_ref")
 LIB = os.path.join(OUT, "libref_glsl.so")
 SHADERS = ["tilde_h0_k_cs.glsl", "tilde_h0_t_cs.glsl", "twiddle_factors_cs.glsl", "butterfly_cs.glsl",
-           "inversion_cs.glsl", "normal_map_cs.glsl"]
+           "inversion_cs.glsl", "normal_map_cs.glsl", "atmosphere.glsl", "sky_envmap_fs.glsl"]
 
 
 def available() -> bool:
@@ -42,6 +42,22 @@ def _extract_reverse_bits() -> str:
     return path
 
 
+def _rewrite_atmosphere() -> str:
+    """oracle/_ref/atmosphere.glsl: the reference's file with its `out vec3`
+    parameters (SkyRadiance, InScattering) as C++ references, so that
+    sky_envmap_fs.glsl's #include <atmosphere.glsl> compiles as C++."""
+    with open(os.path.join(REF, "src", "shader", "atmosphere.glsl")) as fh:
+        src = fh.read()
+    n = src.count("out vec3 ")
+    if n != 2:
+        raise RuntimeError("atmosphere.glsl does not have the two `out vec3` parameters this recipe expects")
+    os.makedirs(OUT, exist_ok=True)
+    path = os.path.join(OUT, "atmosphere.glsl")
+    with open(path, "w") as fh:
+        fh.write(src.replace("out vec3 ", "vec3& "))
+    return path
+
+
 def build(force: bool = False, quiet: bool = True) -> str:
     if not available():
         raise RuntimeError(f"reference sources not found under {REF}")
@@ -50,10 +66,11 @@ def build(force: bool = False, quiet: bool = True) -> str:
     if not force and os.path.exists(LIB) and all(os.path.getmtime(d) <= os.path.getmtime(LIB) for d in deps):
         return LIB
     _extract_reverse_bits()
+    _rewrite_atmosphere()
     cxx = os.environ.get("CXX", "g++")
     cmd = [cxx, "-std=c++20", "-O2", "-fPIC", "-shared", "-fopenmp", "-fsingle-precision-constant",
-           "-ffp-contract=off", "-w", "-I", os.path.join(HERE, "ref_glsl"), "-I", os.path.join(REF, "src", "shader"),
-           "-I", OUT, "-o", LIB + ".tmp", src]
+           "-ffp-contract=off", "-w", "-I", OUT, "-I", os.path.join(HERE, "ref_glsl"),
+           "-I", os.path.join(REF, "src", "shader"), "-o", LIB + ".tmp", src]
     if not quiet:
         print(" ".join(cmd))
     subprocess.check_call(cmd)

@@ -744,3 +744,167 @@ void port_set_threads(int n)
     (void)n;
 #endif
 }
+
+/* ---------------------------------------------------------------------------
+ * Sky environment cube map (sky_envmap_fs.glsl:25-38 with SkyRadiance,
+ * atmosphere.glsl:61-199).  Unlike the rest of the oracle this is FP32 in the
+ * shader's operation order: the shader's float rounding is part of its result
+ * (r*r - Rg*Rg cancels at the sea surface), so an FP64 restatement would not
+ * be the reference.  Built with -ffp-contract=off; every literal is float.
+ * Tables are sampled as GL_LINEAR + CLAMP_TO_EDGE textures with FP32 weights
+ * (main.cpp:168-184).
+ * params: camera[3], sun_direction[3], earth_pos[3], beta_r[3], mie_g,
+ * sun_intensity; trans [64][256][4], insc [32][128][256][4];
+ * out [6][S][S][4] (faces +X, -X, +Y, -Y, +Z, -Z, texel centres).
+ * ------------------------------------------------------------------------- */
+typedef struct { float x, y, z, w; } sky_f4;
+
+static sky_f4 sky_lerp(sky_f4 a, sky_f4 b, float w)
+{
+    float  v = 1.0f - w;
+    sky_f4 r = {a.x * v + b.x * w, a.y * v + b.y * w, a.z * v + b.z * w, a.w * v + b.w * w};
+    return r;
+}
+
+static sky_f4 sky_at(const float* T, size_t i)
+{
+    sky_f4 r = {T[4 * i], T[4 * i + 1], T[4 * i + 2], T[4 * i + 3]};
+    return r;
+}
+
+static void sky_axis(float u, int W, int* i0, int* i1, float* w)
+{
+    float t = u * (float)W - 0.5f;
+    float f = floorf(t);
+    int   i = (int)f;
+    *w      = t - f;
+    *i0     = i < 0 ? 0 : (i > W - 1 ? W - 1 : i);
+    *i1     = i + 1 < 0 ? 0 : (i + 1 > W - 1 ? W - 1 : i + 1);
+}
+
+static sky_f4 sky_tex2d(const float* T, int W, int H, float u, float v)
+{
+    int   x0, x1, y0, y1;
+    float wx, wy;
+    sky_axis(u, W, &x0, &x1, &wx);
+    sky_axis(v, H, &y0, &y1, &wy);
+    sky_f4 a = sky_lerp(sky_at(T, (size_t)y0 * W + x0), sky_at(T, (size_t)y0 * W + x1), wx);
+    sky_f4 b = sky_lerp(sky_at(T, (size_t)y1 * W + x0), sky_at(T, (size_t)y1 * W + x1), wx);
+    return sky_lerp(a, b, wy);
+}
+
+static sky_f4 sky_tex3d(const float* T, int W, int H, int D, float u, float v, float q)
+{
+    int    x0, x1, y0, y1, z0, z1;
+    float  wx, wy, wz;
+    sky_f4 p[2];
+    sky_axis(u, W, &x0, &x1, &wx);
+    sky_axis(v, H, &y0, &y1, &wy);
+    sky_axis(q, D, &z0, &z1, &wz);
+    for (int k = 0; k < 2; ++k) {
+        const float* P = T + (size_t)4 * (k ? z1 : z0) * H * W;
+        sky_f4       a = sky_lerp(sky_at(P, (size_t)y0 * W + x0), sky_at(P, (size_t)y0 * W + x1), wx);
+        sky_f4       b = sky_lerp(sky_at(P, (size_t)y1 * W + x0), sky_at(P, (size_t)y1 * W + x1), wx);
+        p[k]           = sky_lerp(a, b, wy);
+    }
+    return sky_lerp(p[0], p[1], wz);
+}
+
+#define SKY_RG 6360000.0f
+#define SKY_RT 6420000.0f
+
+/* atmosphere.glsl:61-81 */
+static sky_f4 sky_texture4d(const float* T, float r, float mu, float muS, float nu, float tan_mus)
+{
+    const float H     = sqrtf(SKY_RT * SKY_RT - SKY_RG * SKY_RG);
+    const float rho   = sqrtf(r * r - SKY_RG * SKY_RG);
+    const float rmu   = r * mu;
+    const float delta = rmu * rmu - r * r + SKY_RG * SKY_RG;
+    const int   below = rmu < 0.0f && delta > 0.0f;
+    const float c0 = below ? 1.0f : -1.0f, c1 = below ? 0.0f : H * H, c2 = below ? 0.0f : H;
+    const float c3   = below ? 0.5f - 0.5f / 128.0f : 0.5f + 0.5f / 128.0f;
+    const float uR   = 0.5f / 32.0f + rho / H * (1.0f - 1.0f / 32.0f);
+    const float uMu  = c3 + (rmu * c0 + sqrtf(delta + c1)) / (rho + c2) * (0.5f - 1.0f / 128.0f);
+    const float mus  = muS > -0.1975f ? muS : -0.1975f;
+    const float uMuS = 0.5f / 32.0f + (atanf(mus * tan_mus) / 1.1f + (1.0f - 0.26f)) * 0.5f * (1.0f - 1.0f / 32.0f);
+    float       lep  = (nu + 1.0f) / 2.0f * (8.0f - 1.0f);
+    const float uNu  = floorf(lep);
+    lep              = lep - uNu;
+    sky_f4 t0 = sky_tex3d(T, 256, 128, 32, (uNu + uMuS) / 8.0f, uMu, uR);
+    sky_f4 t1 = sky_tex3d(T, 256, 128, 32, (uNu + uMuS + 1.0f) / 8.0f, uMu, uR);
+    float  m  = 1.0f - lep;
+    sky_f4 r4 = {t0.x * m + t1.x * lep, t0.y * m + t1.y * lep, t0.z * m + t1.z * lep, t0.w * m + t1.w * lep};
+    return r4;
+}
+
+void orc_sky_envmap(const float* prm, int S, const float* trans, const float* insc, float* out)
+{
+    const float* cam0 = prm;
+    const float* sun  = prm + 3;
+    const float* ep   = prm + 6;
+    const float* br   = prm + 9;
+    const float  g = prm[12], I = prm[13];
+    const float  tan_mus = tanf(1.26f * 1.1f), tan_mu = tanf(1.5f);
+    const float  cos_sun = cosf(3.141592f / 360.0f);
+    const float  pi      = 3.141592f;
+#pragma omp parallel for schedule(static)
+    for (long idx = 0; idx < 6L * S * S; ++idx) {
+        int   face = (int)(idx / ((long)S * S)), rem = (int)(idx - (long)face * S * S);
+        int   j = rem / S, i = rem - j * S;
+        float sc = 2.0f * (((float)i + 0.5f) / (float)S) - 1.0f, tc = 2.0f * (((float)j + 0.5f) / (float)S) - 1.0f;
+        float d[3];
+        switch (face) {   /* OpenGL cube-map orientation: the inverse of orc_cube_sample's table */
+        case 0: d[0] = 1.0f; d[1] = -tc; d[2] = -sc; break;
+        case 1: d[0] = -1.0f; d[1] = -tc; d[2] = sc; break;
+        case 2: d[0] = sc; d[1] = 1.0f; d[2] = tc; break;
+        case 3: d[0] = sc; d[1] = -1.0f; d[2] = -tc; break;
+        case 4: d[0] = sc; d[1] = -tc; d[2] = 1.0f; break;
+        default: d[0] = -sc; d[1] = -tc; d[2] = -1.0f; break;
+        }
+        float len = sqrtf(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+        float v[3] = {d[0] / len, d[1] / len, d[2] / len};
+        float sunv = (v[0] * sun[0] + v[1] * sun[1] + v[2] * sun[2]) < cos_sun ? 0.0f : 1.0f;
+        float sun_c = sunv * I;
+        float c[3] = {cam0[0] + ep[0], cam0[1] + ep[1], cam0[2] + ep[2]};
+        float r   = sqrtf(c[0] * c[0] + c[1] * c[1] + c[2] * c[2]);
+        float rMu = c[0] * v[0] + c[1] * v[1] + c[2] * v[2];
+        float mu  = rMu / r;
+        float deltaSq = sqrtf(rMu * rMu - r * r + SKY_RT * SKY_RT);
+        float din     = -rMu - deltaSq;
+        if (din < 0.0f) din = 0.0f;
+        if (din > 0.0f) {
+            c[0] = c[0] + din * v[0];
+            c[1] = c[1] + din * v[1];
+            c[2] = c[2] + din * v[2];
+            rMu  = rMu + din;
+            mu   = rMu / SKY_RT;
+            r    = SKY_RT;
+        }
+        float  nu  = v[0] * sun[0] + v[1] * sun[1] + v[2] * sun[2];
+        float  muS = (c[0] * sun[0] + c[1] * sun[1] + c[2] * sun[2]) / r;
+        sky_f4 is  = sky_texture4d(insc, r, rMu / r, muS, nu, tan_mus);
+        /* Transmittance(r, mu), atmosphere.glsl:102-111 */
+        float  tuR  = sqrtf((r - SKY_RG) / (SKY_RT - SKY_RG));
+        float  tuMu = atanf((mu + 0.15f) / (1.0f + 0.15f) * tan_mu) / 1.5f;
+        sky_f4 tr   = sky_tex2d(trans, 256, 64, tuMu, tuR);
+        float  ext[3] = {tr.x, tr.y, tr.z}, res[3] = {0.0f, 0.0f, 0.0f};
+        if (r <= SKY_RT) {
+            float mx = is.x > 1e-4f ? is.x : 1e-4f;
+            float m[3] = {is.x * is.w / mx * (br[0] / br[0]), is.y * is.w / mx * (br[0] / br[1]),
+                          is.z * is.w / mx * (br[0] / br[2])};
+            float pr = (3.0f / (16.0f * pi)) * (1.0f + nu * nu);
+            float pm = 1.5f * 1.0f / (4.0f * pi) * (1.0f - g * g) * powf(1.0f + (g * g) - 2.0f * g * nu, -3.0f / 2.0f) *
+                       (1.0f + nu * nu) / (2.0f + g * g);
+            res[0] = is.x * pr + m[0] * pm;
+            res[1] = is.y * pr + m[1] * pm;
+            res[2] = is.z * pr + m[2] * pm;
+        } else {
+            ext[0] = ext[1] = ext[2] = 1.0f;
+        }
+        float* o = out + 4 * idx;
+        o[0] = sun_c * ext[0] + res[0] * I;
+        o[1] = sun_c * ext[1] + res[1] * I;
+        o[2] = sun_c * ext[2] + res[2] * I;
+        o[3] = 1.0f;
+    }
+}

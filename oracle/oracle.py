@@ -75,6 +75,7 @@ def lib():
         L.orc_displace_grid.argtypes = [C.c_int, dp, dp, dp, dp, C.c_int, C.c_double, C.c_double, dp]
         L.orc_tess_levels.argtypes = [C.c_int, dp, dp]
         L.orc_shade.argtypes = [dp, C.c_long, dp, dp, dp, dp, C.c_int, dp]
+        L.orc_sky_envmap.argtypes = [fp, C.c_int, fp, fp, fp]
         L.orc_count_clamped.argtypes = [pp]
         L.orc_count_clamped.restype = C.c_int
         L.port_create.argtypes = [pp, fp]
@@ -222,6 +223,32 @@ def shade(vertices: np.ndarray, camera, sun_direction, sea_color, sky: np.ndarra
     out = np.empty((v.shape[0], 4))
     lib().orc_shade(_p(v, C.c_double), v.shape[0], *[_p(x, C.c_double) for x in vec], _p(sk, C.c_double),
                     sk.shape[1], _p(out, C.c_double))
+    return out
+
+
+SKY_DEFAULTS = dict(earth_pos=(0.0, 6360010.0, 0.0), beta_r=(0.0058 / 1000, 0.0135 / 1000, 0.0331 / 1000),
+                    mie_g=0.75, sun_intensity=100.0)
+
+
+def sky_sun_direction(angle: float) -> np.ndarray:
+    """SUN_DIR of the reference for its GUI sun angle (main.cpp:151,157):
+    -normalize(0, sin a, cos a) in FP32."""
+    v = np.array([0.0, np.sin(np.float32(angle)), np.cos(np.float32(angle))], dtype=np.float32)
+    return -(v * (np.float32(1.0) / np.sqrt(np.float32(v @ v)))).astype(np.float32)
+
+
+def sky_envmap(camera, sun_direction, transmittance: np.ndarray, inscatter: np.ndarray, S: int,
+               earth_pos=SKY_DEFAULTS["earth_pos"], beta_r=SKY_DEFAULTS["beta_r"], mie_g=SKY_DEFAULTS["mie_g"],
+               sun_intensity=SKY_DEFAULTS["sun_intensity"]) -> np.ndarray:
+    """The sky cube map (6, S, S, 4) of sky_envmap_fs.glsl: orc_sky_envmap
+    (FP32, the shader's operation order).  transmittance (64, 256, 4),
+    inscatter (32, 128, 256, 4), float32."""
+    prm = np.array([*camera, *sun_direction, *earth_pos, *beta_r, mie_g, sun_intensity], dtype=np.float32)
+    tr = np.ascontiguousarray(transmittance, dtype=np.float32)
+    ins = np.ascontiguousarray(inscatter, dtype=np.float32)
+    assert tr.shape == (64, 256, 4) and ins.shape == (32, 128, 256, 4)
+    out = np.empty((6, S, S, 4), dtype=np.float32)
+    lib().orc_sky_envmap(_p(prm, C.c_float), S, _p(tr, C.c_float), _p(ins, C.c_float), _p(out, C.c_float))
     return out
 
 

@@ -31,7 +31,9 @@ def lib():
         L.ref_h0_t.argtypes = [C.c_int, C.c_int, C.c_float, fp, fp, fp, fp, fp]
         L.ref_butterfly_fft.argtypes = [C.c_int, fp, fp, fp, fp]
         L.ref_normal_map.argtypes = [C.c_int, fp, fp]
-        for n in ("ref_bit_reversed", "ref_twiddle", "ref_h0", "ref_h0_t", "ref_butterfly_fft", "ref_normal_map"):
+        L.ref_sky_envmap.argtypes = [fp, C.c_int, fp, fp, fp]
+        for n in ("ref_bit_reversed", "ref_twiddle", "ref_h0", "ref_h0_t", "ref_butterfly_fft", "ref_normal_map",
+                  "ref_sky_envmap"):
             getattr(L, n).restype = None
         _LIB = L
     return _LIB
@@ -81,4 +83,17 @@ def frame(N, L, t, h0k, h0mk):
     normal = np.zeros((N, N, 4), np.float32)
     lib().ref_normal_map(N, _f(out["dy"]), _f(normal))
     out["normal"] = normal
+    return out
+
+
+def sky_envmap(prm, S, transmittance, inscatter):
+    """sky_envmap_fs.glsl (with atmosphere.glsl) over the six capture faces:
+    (6, S, S, 4).  prm: camera[3], sun_direction[3], earth_pos[3], beta_r[3],
+    mie_g, sun_intensity."""
+    p = np.ascontiguousarray(prm, dtype=np.float32)
+    tr = np.ascontiguousarray(transmittance, dtype=np.float32)
+    ins = np.ascontiguousarray(inscatter, dtype=np.float32)
+    assert tr.shape == (64, 256, 4) and ins.shape == (32, 128, 256, 4)
+    out = np.empty((6, S, S, 4), np.float32)
+    lib().ref_sky_envmap(_f(p), S, _f(tr), _f(ins), _f(out))
     return out

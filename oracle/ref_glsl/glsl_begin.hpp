@@ -14,3 +14,5 @@
 #define indices indices_t : glsl::ssbo_base
 #define bit_reversed (*ref_bit_reversed_ptr)
 #define rgba rgba_()
+#define rgbr rgbr_()
+#define out

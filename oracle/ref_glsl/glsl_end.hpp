@@ -10,3 +10,5 @@
 #undef rgba
 #undef LOCAL_SIZE
 #undef M_PI
+#undef rgbr
+#undef out

@@ -68,6 +68,18 @@ REF_SHADER_PROLOGUE
 #include "glsl_end.hpp"
 }  // namespace sh_normal
 
+// The sky: sky_envmap_fs.glsl, which includes atmosphere.glsl.  The build
+// recipe resolves that include to a copy in oracle/_ref/ whose `out vec3`
+// parameters are C++ references (the one rewrite C++ needs); sky_envmap_fs.glsl
+// itself is included unchanged.
+namespace sh_sky {
+using namespace glsl;
+using glsl::abs;   // over the C library's ::abs overloads
+#include "glsl_begin.hpp"
+#include "sky_envmap_fs.glsl"
+#include "glsl_end.hpp"
+}  // namespace sh_sky
+
 namespace {
 
 int ilog2(int n)
@@ -224,6 +236,54 @@ void ref_normal_map(int N, const float* dy, float* normal)
         S::gl_GlobalInvocationID = glsl::uvec3(x, y, 0);
         S::main();
     });
+}
+
+// render_envmap(): main.cpp:500-523 with SkyModel::set_render_uniforms()
+// (:149-158).  The rasteriser's part is restated: the fragment of texel
+// (i, j) of face f of the capture views (:1463-1470) sees the cube-surface
+// point through the texel centre, so PS_IN_WorldPos is that point.
+// prm: camera[3], sun_direction[3], earth_pos[3], beta_r[3], mie_g,
+// sun_intensity.  out [6][S][S][4].
+void ref_sky_envmap(const float* prm, int S, const float* trans, const float* insc, float* out)
+{
+    namespace K = sh_sky;
+    K::u_CameraPos             = glsl::vec3(prm[0], prm[1], prm[2]);
+    K::SUN_DIR                 = glsl::vec3(prm[3], prm[4], prm[5]);
+    K::EARTH_POS               = glsl::vec3(prm[6], prm[7], prm[8]);
+    K::betaR                   = glsl::vec3(prm[9], prm[10], prm[11]);
+    K::mieG                    = prm[12];
+    K::SUN_INTENSITY           = prm[13];
+    K::s_Transmittance.data    = trans;
+    K::s_Transmittance.w       = 256;
+    K::s_Transmittance.h       = 64;
+    K::s_Transmittance.ch      = 4;
+    K::s_Transmittance.linear  = true;
+    K::s_Inscatter.data        = insc;
+    K::s_Inscatter.w           = 256;
+    K::s_Inscatter.h           = 128;
+    K::s_Inscatter.d           = 32;
+    for (int f = 0; f < 6; ++f)
+        for (int j = 0; j < S; ++j)
+            for (int i = 0; i < S; ++i) {
+                const float sc = 2.0f * (((float)i + 0.5f) / (float)S) - 1.0f;
+                const float tc = 2.0f * (((float)j + 0.5f) / (float)S) - 1.0f;
+                glsl::vec3  p;
+                switch (f) {
+                case 0: p = glsl::vec3(1.0f, -tc, -sc); break;
+                case 1: p = glsl::vec3(-1.0f, -tc, sc); break;
+                case 2: p = glsl::vec3(sc, 1.0f, tc); break;
+                case 3: p = glsl::vec3(sc, -1.0f, -tc); break;
+                case 4: p = glsl::vec3(sc, -tc, 1.0f); break;
+                default: p = glsl::vec3(-sc, -tc, -1.0f); break;
+                }
+                K::PS_IN_WorldPos = p;
+                K::main();
+                float* o = out + 4 * (((size_t)f * S + j) * S + i);
+                o[0]     = K::PS_OUT_Color.x;
+                o[1]     = K::PS_OUT_Color.y;
+                o[2]     = K::PS_OUT_Color.z;
+                o[3]     = K::PS_OUT_Color.w;
+            }
 }
 
 }  // extern "C"

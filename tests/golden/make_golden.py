@@ -10,6 +10,10 @@ order src/main.cpp dispatches them, on seeded noise, and writes:
   ref_frame_N32.npz     h0k, h0minusk (tilde_h0_k_cs.glsl) and frames
   ref_frame_N64.npz     (tilde_h0_t_cs + butterfly_cs + inversion_cs +
                         normal_map_cs) at several times
+  ref_sky.npz           sky environment cube maps (sky_envmap_fs.glsl with
+                        atmosphere.glsl) on seeded synthetic tables
+                        (sky_tables(seed): the reference's inscatter.raw is
+                        missing), for two sun angles and camera heights
 
 Each file records its parameters and the sha256 of the shader sources used.
 The shaders' DC mode is NaN (normalize(0), tilde_h0_k_cs.glsl:44); as in the
@@ -39,6 +43,29 @@ CASES = [
     dict(name="ref_frame_N64", N=64, L=1000, A=4.0, V=40.0, wx=1.0, wy=1.0, l=(40.0 ** 2 / 9.81) / 1000.0,
          seed=0, times=[1.0, 7.75]),
 ]
+
+
+SKY_CASES = [
+    # sun 0.4 rad above the horizon, camera 10 m up (sun disk on the -Z face)
+    dict(name="high_sun", camera=(0.0, 10.0, 0.0), angle=-0.4, S=32, seed=5),
+    # sun at the horizon seen from 2 km: rays through the ground and the disk's edge
+    dict(name="low_sun", camera=(30.0, 2000.0, -50.0), angle=-0.02, S=24, seed=6),
+]
+
+
+def sky_tables(seed):
+    """Seeded stand-ins for the sky tables: transmittance U(0,1), inscatter
+    U(0.001, 0.051), float32 (numpy PCG64)."""
+    rng = np.random.default_rng(seed)
+    tr = rng.random((64, 256, 4), dtype=np.float32)
+    ins = (rng.random((32, 128, 256, 4), dtype=np.float32) * np.float32(0.05) + np.float32(1e-3)).astype(np.float32)
+    return tr, ins
+
+
+def sky_prm(c):
+    d = oracle.sky_sun_direction(c["angle"])
+    s = oracle.SKY_DEFAULTS
+    return np.array([*c["camera"], *d, *s["earth_pos"], *s["beta_r"], s["mie_g"], s["sun_intensity"]], np.float32)
 
 
 def shader_hashes():
@@ -80,6 +107,15 @@ def main():
         meta["sha256"] = hashes
         np.savez_compressed(os.path.join(HERE, c["name"] + ".npz"), meta=json.dumps(meta), **arrs)
         print("wrote", c["name"])
+
+    sky = {}
+    for c in SKY_CASES:
+        tr, ins = sky_tables(c["seed"])
+        sky[c["name"] + "_prm"] = sky_prm(c)
+        sky[c["name"]] = ref.sky_envmap(sky[c["name"] + "_prm"], c["S"], tr, ins)
+    np.savez_compressed(os.path.join(HERE, "ref_sky.npz"), meta=json.dumps({"cases": SKY_CASES, "sha256": hashes}),
+                        **sky)
+    print("wrote ref_sky")
 
 
 if __name__ == "__main__":
