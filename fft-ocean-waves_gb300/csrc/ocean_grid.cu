@@ -23,6 +23,7 @@
 #include <stdint.h>
 
 #include <cmath>
+#include <utility>
 
 #include "ocean.h"
 #include "ocean_host.h"
@@ -140,6 +141,28 @@ __device__ __forceinline__ float3 cube_sample(const float4* __restrict__ sky, in
                        a.z * w00 + b.z * w01 + c.z * w10 + d.z * w11);
 }
 
+// sky_vs.glsl + sky_fs.glsl: the far-plane point of each pixel centre
+// through inverse(projection * mat4(mat3(view))) (column-major m), the cube
+// map there, Reinhard and gamma.
+struct SkyboxArgs {
+    float m[16];
+    int   S, W, H;
+};
+
+__global__ void k_skybox(SkyboxArgs a, const float4* __restrict__ sky, float4* __restrict__ img)
+{
+    const long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (idx >= (long long)a.W * a.H) return;
+    const int   y = (int)(idx / a.W), x = (int)(idx - (long long)y * a.W);
+    const float cx = 2.0f * ((float)x + 0.5f) / (float)a.W - 1.0f, cy = 2.0f * ((float)y + 0.5f) / (float)a.H - 1.0f;
+    float d[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) d[i] = a.m[i] * cx + a.m[4 + i] * cy + a.m[8 + i] + a.m[12 + i];
+    const float3 c = cube_sample(sky, a.S, make_float3(d[0] / d[3], d[1] / d[3], d[2] / d[3]));
+    auto tone = [](float v) { return powf(v / (v + 1.0f), 1.0f / 2.2f); };
+    img[idx] = make_float4(tone(c.x), tone(c.y), tone(c.z), 1.0f);
+}
+
 struct ShadeArgs {
     float3 cam, sun, sea;
     int    S;
@@ -251,5 +274,59 @@ extern "C" int ocean_shade_grid(const float* vertices, int64_t n_vertices, const
         reinterpret_cast<float4*>(colors));
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return cuda_fail(e, "shading launch");
+    return OCEAN_OK;
+}
+
+extern "C" int ocean_render_skybox(const float* sky_cubemap, int32_t sky_size, const float* view, const float* projection,
+                                   int32_t width, int32_t height, float* image, void* stream)
+{
+    using namespace ocean::host;
+    if (!sky_cubemap || !view || !projection || !image) return fail(OCEAN_ERR_INVALID, "NULL pointer");
+    if (sky_size < 1 || sky_size > 16384) return fail(OCEAN_ERR_INVALID, "sky_size must be in [1, 16384]");
+    if (width < 1 || height < 1 || width > 32768 || height > 32768)
+        return fail(OCEAN_ERR_INVALID, "width and height must be in [1, 32768]");
+    if ((reinterpret_cast<uintptr_t>(sky_cubemap) | reinterpret_cast<uintptr_t>(image)) % 16)
+        return fail(OCEAN_ERR_INVALID, "sky_cubemap and image must be 16-byte aligned");
+    // M = projection * mat4(mat3(view)), column-major, in double; then its inverse
+    double R[16] = {0}, M[16], A[4][8];
+    for (int c = 0; c < 3; ++c)
+        for (int r = 0; r < 3; ++r) R[c * 4 + r] = view[c * 4 + r];
+    R[15] = 1.0;
+    for (int c = 0; c < 4; ++c)
+        for (int r = 0; r < 4; ++r) {
+            double s = 0.0;
+            for (int k = 0; k < 4; ++k) s += (double)projection[k * 4 + r] * R[c * 4 + k];
+            M[c * 4 + r] = s;
+        }
+    for (int r = 0; r < 4; ++r)
+        for (int c = 0; c < 8; ++c) A[r][c] = c < 4 ? M[c * 4 + r] : (c - 4 == r ? 1.0 : 0.0);
+    for (int col = 0; col < 4; ++col) {   // Gauss-Jordan with partial pivoting
+        int piv = col;
+        for (int r = col + 1; r < 4; ++r)
+            if (std::fabs(A[r][col]) > std::fabs(A[piv][col])) piv = r;
+        if (!(std::fabs(A[piv][col]) > 1e-300)) return fail(OCEAN_ERR_INVALID, "projection * view is singular");
+        for (int c = 0; c < 8; ++c) std::swap(A[col][c], A[piv][c]);
+        const double p = A[col][col];
+        for (int c = 0; c < 8; ++c) A[col][c] /= p;
+        for (int r = 0; r < 4; ++r)
+            if (r != col) {
+                const double f = A[r][col];
+                for (int c = 0; c < 8; ++c) A[r][c] -= f * A[col][c];
+            }
+    }
+    SkyboxArgs a;
+    for (int c = 0; c < 4; ++c)
+        for (int r = 0; r < 4; ++r) {
+            a.m[c * 4 + r] = (float)A[r][4 + c];
+            if (!std::isfinite(a.m[c * 4 + r])) return fail(OCEAN_ERR_INVALID, "view and projection must be finite");
+        }
+    a.S = sky_size;
+    a.W = width;
+    a.H = height;
+    const long long n = (long long)width * height;
+    k_skybox<<<(unsigned)((n + 255) / 256), 256, 0, static_cast<cudaStream_t>(stream)>>>(
+        a, reinterpret_cast<const float4*>(sky_cubemap), reinterpret_cast<float4*>(image));
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return cuda_fail(e, "skybox launch");
     return OCEAN_OK;
 }

@@ -36,7 +36,7 @@ EXPORTS = [
     "ocean_fill_noise", "ocean_bit_reversed_indices", "ocean_butterfly_table", "ocean_last_error",
     "ocean_version", "ocean_backward", "ocean_device_status", "ocean_batch_create", "ocean_batch_update",
     "ocean_batch_device_status", "ocean_batch_destroy", "ocean_update_noalloc", "ocean_displace_grid",
-    "ocean_grid_tess_levels", "ocean_shade_grid", "ocean_sky_envmap",
+    "ocean_grid_tess_levels", "ocean_shade_grid", "ocean_sky_envmap", "ocean_render_skybox",
 ]
 OCEAN_GRAD_ACCUMULATE = 1
 
@@ -130,6 +130,7 @@ def load() -> C.CDLL:
     L.ocean_grid_tess_levels.argtypes = [P(ocean_grid_params), vp, vp]
     L.ocean_shade_grid.argtypes = [vp, C.c_int64, P(ocean_shade_params), vp, vp, vp]
     L.ocean_sky_envmap.argtypes = [P(ocean_sky_params), vp, vp, vp, vp]
+    L.ocean_render_skybox.argtypes = [vp, C.c_int32, P(C.c_float), P(C.c_float), C.c_int32, C.c_int32, vp, vp]
     L.ocean_last_error.restype = C.c_char_p
     for name in EXPORTS:
         if name not in ("ocean_destroy", "ocean_last_error", "ocean_batch_destroy"):
@@ -260,6 +261,17 @@ def sky_envmap(camera, sun_direction, transmittance, inscatter, cubemap, earth_p
                          int(cubemap.shape[1]))
     check(load().ocean_sky_envmap(C.byref(p), _addr(transmittance), _addr(inscatter), _addr(cubemap),
                                   _stream(stream)))
+
+
+def render_skybox(sky, view, projection, image, stream=None) -> None:
+    """sky_fs.glsl into a headless image: sky (6, S, S, 4) cube map, view and
+    projection 4x4 column-major (glm; (4, 4) arrays indexed [column][row] or
+    16 floats), image (H, W, 4); device tensors for sky and image."""
+    import numpy as np
+    v = (C.c_float * 16)(*[float(x) for x in np.asarray(view, dtype=np.float32).reshape(16)])
+    p = (C.c_float * 16)(*[float(x) for x in np.asarray(projection, dtype=np.float32).reshape(16)])
+    check(load().ocean_render_skybox(_addr(sky), int(sky.shape[1]), v, p, int(image.shape[1]), int(image.shape[0]),
+                                     _addr(image), _stream(stream)))
 
 
 def load_sky_tables(texture_dir: str):

@@ -294,6 +294,17 @@ typedef struct ocean_sky_params {
 OCEAN_API int ocean_sky_envmap(const ocean_sky_params* params, const float* transmittance, const float* inscatter,
                                float* cubemap, void* stream);
 
+/* The skybox of render_skybox() (main.cpp:527-547, sky_vs.glsl, sky_fs.glsl)
+ * into a headless image: per pixel centre of a width x height framebuffer
+ * (row 0 at the bottom, as GL's), the direction through the far plane of
+ * projection * mat4(mat3(view)), the cube map sampled there (level 0,
+ * bilinear within the face, as ocean_shade_grid), then c / (c + 1) and
+ * gamma 1/2.2.  view and projection are 4x4 column-major (glm) host arrays;
+ * sky_cubemap [6][sky_size][sky_size] RGBA as ocean_sky_envmap writes it;
+ * image [height][width] RGBA float32 (alpha 1).  16-byte aligned. */
+OCEAN_API int ocean_render_skybox(const float* sky_cubemap, int32_t sky_size, const float* view, const float* projection,
+                                  int32_t width, int32_t height, float* image, void* stream);
+
 /* ---- Adjoint --------------------------------------------------------- */
 
 /* Flags for ocean_backward */

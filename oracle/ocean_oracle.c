@@ -473,6 +473,24 @@ static void orc_cube_sample(const double* sky, int S, const double* r, double* r
     }
 }
 
+/* render_skybox(): sky_vs.glsl + sky_fs.glsl per pixel centre of a W x H
+ * framebuffer (row 0 at the bottom): minv = inverse(projection *
+ * mat4(mat3(view))) column-major; the far-plane point's direction; the cube
+ * map there; c / (c + 1), gamma 1/2.2 (sky_fs.glsl:14-20). */
+void orc_skybox(const double* sky, int S, const double* minv, int W, int H, double* out)
+{
+    for (int y = 0; y < H; ++y)
+        for (int x = 0; x < W; ++x) {
+            double cx = 2.0 * (x + 0.5) / W - 1.0, cy = 2.0 * (y + 0.5) / H - 1.0, d[4], rgb[3];
+            for (int i = 0; i < 4; ++i) d[i] = minv[i] * cx + minv[4 + i] * cy + minv[8 + i] + minv[12 + i];
+            double r[3] = {d[0] / d[3], d[1] / d[3], d[2] / d[3]};
+            orc_cube_sample(sky, S, r, rgb);
+            double* o = out + 4 * ((size_t)y * W + x);
+            for (int c = 0; c < 3; ++c) o[c] = pow(rgb[c] / (rgb[c] + 1.0), 1.0 / 2.2);
+            o[3] = 1.0;
+        }
+}
+
 void orc_shade(const double* vert, long n, const double* cam, const double* sun, const double* sea, const double* sky,
                int S, double* out)
 {

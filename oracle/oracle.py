@@ -76,6 +76,7 @@ def lib():
         L.orc_tess_levels.argtypes = [C.c_int, dp, dp]
         L.orc_shade.argtypes = [dp, C.c_long, dp, dp, dp, dp, C.c_int, dp]
         L.orc_sky_envmap.argtypes = [fp, C.c_int, fp, fp, fp]
+        L.orc_skybox.argtypes = [dp, C.c_int, dp, C.c_int, C.c_int, dp]
         L.orc_count_clamped.argtypes = [pp]
         L.orc_count_clamped.restype = C.c_int
         L.port_create.argtypes = [pp, fp]
@@ -249,6 +250,27 @@ def sky_envmap(camera, sun_direction, transmittance: np.ndarray, inscatter: np.n
     assert tr.shape == (64, 256, 4) and ins.shape == (32, 128, 256, 4)
     out = np.empty((6, S, S, 4), dtype=np.float32)
     lib().orc_sky_envmap(_p(prm, C.c_float), S, _p(tr, C.c_float), _p(ins, C.c_float), _p(out, C.c_float))
+    return out
+
+
+def skybox_matrix(view, projection) -> np.ndarray:
+    """inverse(projection * mat4(mat3(view))) for 4x4 column-major (glm)
+    matrices given as (4, 4) arrays indexed [column][row]; returned the same
+    way, float64."""
+    V = np.asarray(view, np.float64).T          # [row][column]
+    P = np.asarray(projection, np.float64).T
+    R = np.eye(4)
+    R[:3, :3] = V[:3, :3]
+    return np.linalg.inv(P @ R).T
+
+
+def skybox(sky: np.ndarray, view, projection, W: int, H: int) -> np.ndarray:
+    """sky_fs.glsl's colour per pixel (H, W, 4): orc_skybox on a (6, S, S, 4)
+    cube map."""
+    sk = np.ascontiguousarray(sky, dtype=np.float64)
+    m = np.ascontiguousarray(skybox_matrix(view, projection).reshape(16))
+    out = np.empty((H, W, 4))
+    lib().orc_skybox(_p(sk, C.c_double), sk.shape[1], _p(m, C.c_double), W, H, _p(out, C.c_double))
     return out
 
 

@@ -97,3 +97,39 @@ def test_sky_envmap_argument_errors(torch_cuda, ocean_lib):
     ocean_lib.sky_envmap((0.0, 1.0, 0.0), sun, tr, ins, out)
     torch.cuda.synchronize()
     assert torch.isfinite(out).all()
+
+
+@pytest.mark.parametrize("cam", [0, 1])
+def test_skybox_matches_oracle(torch_cuda, ocean_lib, oracle_mod, cam):
+    """ocean_render_skybox of a sky from ocean_sky_envmap against orc_skybox
+    on the same cube map (FP32 against FP64: rtol 1e-4)."""
+    from test_sky_oracle import SKYBOX_CAMERAS, look_at, perspective
+    torch = torch_cuda
+    dev = torch.device("cuda")
+    eye, center, up, fovy = SKYBOX_CAMERAS[cam]
+    W, H = 160, 96
+    tr, ins = make_golden.sky_tables(8)
+    sky = torch.empty((6, 128, 128, 4), device=dev)
+    ocean_lib.sky_envmap(eye, ocean_lib.sky_sun_direction(-0.3), torch.from_numpy(tr).to(dev),
+                         torch.from_numpy(ins).to(dev), sky)
+    V, P = look_at(eye, center, up), perspective(fovy, W / H, 0.1, 1000.0)
+    img = torch.empty((H, W, 4), device=dev)
+    ocean_lib.render_skybox(sky, V.astype(np.float32), P.astype(np.float32), img)
+    torch.cuda.synchronize()
+    want = oracle_mod.skybox(sky.cpu().numpy().astype(np.float64), V.astype(np.float32), P.astype(np.float32), W, H)
+    assert np.allclose(img.cpu().numpy(), want, rtol=1e-4, atol=1e-5)
+
+
+def test_skybox_argument_errors(torch_cuda, ocean_lib):
+    torch = torch_cuda
+    dev = torch.device("cuda")
+    sky = torch.zeros((6, 8, 8, 4), device=dev)
+    img = torch.empty((4, 4, 4), device=dev)
+    eye = np.eye(4, dtype=np.float32)
+    with pytest.raises(ocean_lib.OceanError):
+        ocean_lib.render_skybox(sky, eye, np.zeros((4, 4), np.float32), img)      # singular
+    with pytest.raises(ocean_lib.OceanError):
+        ocean_lib.render_skybox(sky, eye, eye, torch.empty((0, 4, 4), device=dev))
+    ocean_lib.render_skybox(sky, eye, eye, img)
+    torch.cuda.synchronize()
+    assert torch.all(img[..., 3] == 1.0)

@@ -114,3 +114,83 @@ def test_constant_inscatter_is_phase_functions(oracle_mod):
     want = I * (c * pr[..., None] + c * (br[0] / br)[None, None, None, :] * pm[..., None])
     away = nu < 0.99
     assert np.allclose(m[..., :3][away], want[away], rtol=2e-5, atol=0)
+
+
+def look_at(eye, center, up):
+    """glm::lookAt (right-handed) as a (4, 4) array indexed [column][row]."""
+    eye, center, up = (np.asarray(v, np.float64) for v in (eye, center, up))
+    f = center - eye
+    f /= np.linalg.norm(f)
+    s = np.cross(f, up)
+    s /= np.linalg.norm(s)
+    u = np.cross(s, f)
+    M = np.eye(4)
+    M[0, 0], M[1, 0], M[2, 0] = s
+    M[0, 1], M[1, 1], M[2, 1] = u
+    M[0, 2], M[1, 2], M[2, 2] = -f
+    M[3, 0], M[3, 1], M[3, 2] = -s @ eye, -u @ eye, f @ eye
+    return M
+
+
+def perspective(fovy, aspect, near, far):
+    """glm::perspective (right-handed, depth -1..1), [column][row]."""
+    t = np.tan(fovy / 2)
+    P = np.zeros((4, 4))
+    P[0, 0], P[1, 1] = 1 / (aspect * t), 1 / t
+    P[2, 2], P[2, 3], P[3, 2] = -(far + near) / (far - near), -1.0, -2 * far * near / (far - near)
+    return P
+
+
+def np_cube_sample(sky, d):
+    """Independent cube-map lookup (OpenGL face selection and orientation,
+    bilinear within the face, edges clamped) for directions d (..., 3)."""
+    S = sky.shape[1]
+    x, y, z = d[..., 0], d[..., 1], d[..., 2]
+    ax, ay, az = np.abs(x), np.abs(y), np.abs(z)
+    xm = (ax >= ay) & (ax >= az)
+    ym = ~xm & (ay >= az)
+    face = np.where(xm, np.where(x >= 0, 0, 1), np.where(ym, np.where(y >= 0, 2, 3), np.where(z >= 0, 4, 5)))
+    ma = np.where(xm, ax, np.where(ym, ay, az))
+    sc = np.select([face == 0, face == 1, face == 2, face == 3, face == 4], [-z, z, x, x, x], -x)
+    tc = np.select([face == 0, face == 1, face == 2, face == 3, face == 4], [-y, -y, z, -z, -y], -y)
+    s = 0.5 * (sc / ma + 1) * S - 0.5
+    t = 0.5 * (tc / ma + 1) * S - 0.5
+    s0, t0 = np.floor(s), np.floor(t)
+    ws, wt = (s - s0)[..., None], (t - t0)[..., None]
+    cl = lambda v: np.clip(v, 0, S - 1).astype(int)
+    a, b = cl(s0), cl(s0 + 1)
+    c, e = cl(t0), cl(t0 + 1)
+    top = sky[face, c, a, :3] * (1 - ws) + sky[face, c, b, :3] * ws
+    bot = sky[face, e, a, :3] * (1 - ws) + sky[face, e, b, :3] * ws
+    return top * (1 - wt) + bot * wt
+
+
+def np_skybox(sky, eye, center, up, fovy, W, H):
+    """Per pixel: the view-space ray (x t a, y t, -1) rotated to world by the
+    transpose of the view's rotation (no matrix inverse), the cube map, tone."""
+    t = np.tan(fovy / 2)
+    xs = (2 * (np.arange(W) + 0.5) / W - 1) * t * (W / H)
+    ys = (2 * (np.arange(H) + 0.5) / H - 1) * t
+    X, Y = np.meshgrid(xs, ys)
+    v = np.stack([X, Y, -np.ones_like(X)], -1)
+    Rm = look_at(eye, center, up).T[:3, :3]          # [row][column]
+    w = v @ Rm                                       # = (Rm^T v) per pixel
+    c = np_cube_sample(sky, w)
+    out = np.ones((H, W, 4))
+    out[..., :3] = (c / (c + 1)) ** (1 / 2.2)
+    return out
+
+
+SKYBOX_CAMERAS = [((0.0, 10.0, 0.0), (1.0, 9.5, -2.0), (0.0, 1.0, 0.0), 1.0),
+                  ((5.0, 2.0, 3.0), (-3.0, 8.0, 1.0), (0.0, 1.0, 0.0), 0.6)]
+
+
+@pytest.mark.parametrize("cam", range(len(SKYBOX_CAMERAS)))
+def test_skybox_oracle_vs_numpy(oracle_mod, cam):
+    eye, center, up, fovy = SKYBOX_CAMERAS[cam]
+    W, H = 48, 32
+    rng = np.random.default_rng(cam)
+    sky = rng.random((6, 24, 24, 4)) * 5.0
+    V, P = look_at(eye, center, up), perspective(fovy, W / H, 0.1, 1000.0)
+    got = oracle_mod.skybox(sky, V, P, W, H)
+    assert np.allclose(got, np_skybox(sky, eye, center, up, fovy, W, H), rtol=1e-9, atol=1e-12)
