@@ -227,3 +227,22 @@ def test_update_argument_errors(torch_cuda, ocean_lib):
         torch.cuda.synchronize()
         oc.device_status()
         assert torch.any(dy)
+
+
+def test_outputs_in_pinned_host_memory(torch_cuda, ocean_lib):
+    """Output pointers may be pinned host memory (unified addressing): the
+    output kernel then writes across the host link, with the same values as
+    into device buffers."""
+    torch = torch_cuda
+    N = 256
+    d = P.c2(N)
+    dev = torch.device("cuda")
+    with ocean_lib.Ocean(P.lib_params(d), seed=d["seed"]) as oc:
+        dv = [torch.empty((N, N), device=dev) for _ in range(3)] + [torch.empty((N, N, 4), device=dev)]
+        hv = [torch.empty((N, N), pin_memory=True) for _ in range(3)] + [torch.empty((N, N, 4), pin_memory=True)]
+        oc.update(3.5, *dv)
+        oc.update(3.5, *hv)
+        torch.cuda.synchronize()
+        oc.device_status()
+        for a, b in zip(dv, hv):
+            assert torch.equal(a.cpu(), b)
