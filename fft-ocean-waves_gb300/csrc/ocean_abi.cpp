@@ -8,7 +8,10 @@
 // buffers (m_dx, m_dy, m_dz, m_normal_map).
 #include <cuda_runtime.h>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
@@ -38,6 +41,37 @@ int cuda_fail(cudaError_t e, const char* what)
 }
 
 bool is_pow2(int n) { return n > 0 && (n & (n - 1)) == 0; }
+
+// ocean_debug_fail_allocations: allocations left before the injected failures (< 0: off)
+static std::atomic<int> g_alloc_budget{-1};
+
+static bool alloc_injected_failure()
+{
+    int b = g_alloc_budget.load();
+    while (b >= 0) {
+        if (b == 0) return true;
+        if (g_alloc_budget.compare_exchange_weak(b, b - 1)) return false;
+    }
+    return false;
+}
+
+cudaError_t dev_alloc_bytes(void** p, size_t bytes)
+{
+    if (alloc_injected_failure()) {
+        *p = nullptr;
+        return cudaErrorMemoryAllocation;
+    }
+    return cudaMalloc(p, bytes);
+}
+
+cudaError_t host_alloc_bytes(void** p, size_t bytes)
+{
+    if (alloc_injected_failure()) {
+        *p = nullptr;
+        return cudaErrorMemoryAllocation;
+    }
+    return cudaMallocHost(p, bytes);
+}
 
 int validate(const ocean_params* p)
 {
@@ -91,7 +125,7 @@ int check_device()
 int upload_twiddles(float2** d, int N)
 {
     cudaError_t e;
-    if ((e = cudaMalloc(d, ocean::twiddle_len(N) * sizeof(float2))) != cudaSuccess) {
+    if ((e = dev_alloc(d, ocean::twiddle_len(N) * sizeof(float2))) != cudaSuccess) {
         *d = nullptr;
         return fail(OCEAN_ERR_NOMEM, std::string("device allocation failed: ") + cudaGetErrorString(e));
     }
@@ -200,6 +234,8 @@ extern "C" {
 
 const char* ocean_last_error(void) { return g_err.c_str(); }
 
+void ocean_debug_fail_allocations(int32_t after) { g_alloc_budget.store(after < 0 ? -1 : after); }
+
 int ocean_version(void) { return 100; }
 
 int ocean_fill_noise(uint64_t seed, int32_t N, float* host_out)
@@ -283,12 +319,12 @@ int ocean_create(const ocean_params* params, const float* noise_host, ocean_t** 
     o->N = params->N;
     o->set_consts();
     const size_t N = (size_t)o->N;
-    if ((e = cudaMalloc(&o->h0, N * N * sizeof(float4))) != cudaSuccess ||
-        (e = cudaMalloc(&o->spec, ocean::spec_len(o->N) * sizeof(float2))) != cudaSuccess ||
-        (e = cudaMalloc(&o->inter, ocean::inter_len(o->N) * sizeof(float2))) != cudaSuccess ||
-        (e = cudaMalloc(&o->tmap, ocean::tmap_len(o->N) * sizeof(float))) != cudaSuccess ||
-        (e = cudaMalloc(&o->status, sizeof(unsigned))) != cudaSuccess ||
-        (e = cudaMalloc(&o->noise, 4 * N * N * sizeof(float))) != cudaSuccess) {
+    if ((e = dev_alloc(&o->h0, N * N * sizeof(float4))) != cudaSuccess ||
+        (e = dev_alloc(&o->spec, ocean::spec_len(o->N) * sizeof(float2))) != cudaSuccess ||
+        (e = dev_alloc(&o->inter, ocean::inter_len(o->N) * sizeof(float2))) != cudaSuccess ||
+        (e = dev_alloc(&o->tmap, ocean::tmap_len(o->N) * sizeof(float))) != cudaSuccess ||
+        (e = dev_alloc(&o->status, sizeof(unsigned))) != cudaSuccess ||
+        (e = dev_alloc(&o->noise, 4 * N * N * sizeof(float))) != cudaSuccess) {
         delete o;
         return fail(OCEAN_ERR_NOMEM, std::string("device allocation failed: ") + cudaGetErrorString(e));
     }
@@ -376,7 +412,7 @@ int ocean_get_outputs(ocean_t* o, ocean_outputs* out)
     if (!o || !out) return fail(OCEAN_ERR_INVALID, "NULL argument");
     const size_t NN = (size_t)o->N * o->N;
     if (!o->out) {
-        cudaError_t e = cudaMalloc(&o->out, NN * 7 * sizeof(float));
+        cudaError_t e = dev_alloc(&o->out, NN * 7 * sizeof(float));
         if (e != cudaSuccess) {
             o->out = nullptr;
             return fail(OCEAN_ERR_NOMEM, std::string("output allocation failed: ") + cudaGetErrorString(e));
@@ -403,7 +439,10 @@ int ocean_update_rows(ocean_t* o, double t, void* stream)
     ra.fc0        = o->frame(t);
     ra.tiles      = 1;
     ra.S          = 1;
+    // NVTX ranges name the stages as the reference's GL debug groups do (main.cpp:623,644,665,689)
+    nvtxRangePushA("ocean rows: evolution + horizontal FFT");
     cudaError_t e = ocean::launch_row_pass(o->N, ra, static_cast<cudaStream_t>(stream));
+    nvtxRangePop();
     if (e != cudaSuccess) return cuda_fail(e, "row pass launch");
     return OCEAN_OK;
 }
@@ -440,7 +479,9 @@ int ocean_update_columns(ocean_t* o, void* stream)
 {
     if (!o) return fail(OCEAN_ERR_INVALID, "ocean is NULL");
     const ocean_outputs none{};
+    nvtxRangePushA("ocean columns: vertical FFT + inversion");
     cudaError_t e = ocean::launch_col_fft(o->N, 1, col_args(o, none), static_cast<cudaStream_t>(stream), o->pdl_next);
+    nvtxRangePop();
     if (e != cudaSuccess) return cuda_fail(e, "column transform launch");
     return OCEAN_OK;
 }
@@ -451,7 +492,9 @@ int ocean_update_outputs(ocean_t* o, const ocean_outputs* out, void* stream)
     ocean_outputs res;
     int rc = resolve_outputs(o, out, &res);
     if (rc) return rc;
+    nvtxRangePushA("ocean outputs: normal map + Jacobian");
     cudaError_t e = ocean::launch_col_out(o->N, 1, col_args(o, res), static_cast<cudaStream_t>(stream), o->pdl_next);
+    nvtxRangePop();
     if (e != cudaSuccess) return cuda_fail(e, "output launch");
     return OCEAN_OK;
 }
@@ -508,11 +551,11 @@ int ocean_backward(ocean_t* o, const double* times, int32_t T, const float* g_dx
         cudaFree(o->adj);
         o->adj        = nullptr;
         o->adj_frames = 0;
-        if ((e = cudaMalloc(&o->adj, per_frame * chunk)) != cudaSuccess)
+        if ((e = dev_alloc(&o->adj, per_frame * chunk)) != cudaSuccess)
             return fail(OCEAN_ERR_NOMEM, std::string("adjoint scratch allocation failed: ") + cudaGetErrorString(e));
         o->adj_frames = chunk;
     }
-    if (!o->sums && (e = cudaMalloc(&o->sums, 4 * sizeof(double))) != cudaSuccess) {
+    if (!o->sums && (e = dev_alloc(&o->sums, 4 * sizeof(double))) != cudaSuccess) {
         o->sums = nullptr;
         return fail(OCEAN_ERR_NOMEM, std::string("allocation failed: ") + cudaGetErrorString(e));
     }

@@ -216,12 +216,12 @@ int ocean_batch_create(const ocean_params* params, const uint64_t* seeds, int32_
     float*             d_noise = nullptr;
     float4*            d_h0    = nullptr;
     const int          maxN    = b->groups.front().N;
-    if ((e = cudaMalloc(&b->status, sizeof(unsigned))) != cudaSuccess ||
+    if ((e = dev_alloc(&b->status, sizeof(unsigned))) != cudaSuccess ||
         (e = cudaMemset(b->status, 0, sizeof(unsigned))) != cudaSuccess ||
-        (e = cudaMalloc(&b->d_desc, b->desc_bytes)) != cudaSuccess ||
-        (e = cudaMallocHost(&b->h_desc, b->desc_bytes)) != cudaSuccess ||
-        (e = cudaMalloc(&d_noise, 4 * (size_t)maxN * maxN * sizeof(float))) != cudaSuccess ||
-        (e = cudaMalloc(&d_h0, (size_t)maxN * maxN * sizeof(float4))) != cudaSuccess) {
+        (e = dev_alloc(&b->d_desc, b->desc_bytes)) != cudaSuccess ||
+        (e = host_alloc(&b->h_desc, b->desc_bytes)) != cudaSuccess ||
+        (e = dev_alloc(&d_noise, 4 * (size_t)maxN * maxN * sizeof(float))) != cudaSuccess ||
+        (e = dev_alloc(&d_h0, (size_t)maxN * maxN * sizeof(float4))) != cudaSuccess) {
         cudaFree(d_noise);
         cudaFree(d_h0);
         delete b;
@@ -231,9 +231,9 @@ int ocean_batch_create(const ocean_params* params, const uint64_t* seeds, int32_
         const size_t N = (size_t)g.N, NN = N * N, T = g.tiles.size();
         plan_waves(g, samples);
         const size_t W = (size_t)g.wave_units;
-        if ((e = cudaMalloc(&g.spec, T * ocean::spec_len(g.N) * sizeof(float2))) != cudaSuccess ||
-            (e = cudaMalloc(&g.inter, W * ocean::inter_len(g.N) * sizeof(float2))) != cudaSuccess ||
-            (e = cudaMalloc(&g.tmap, W * ocean::tmap_len(g.N) * sizeof(float))) != cudaSuccess) {
+        if ((e = dev_alloc(&g.spec, T * ocean::spec_len(g.N) * sizeof(float2))) != cudaSuccess ||
+            (e = dev_alloc(&g.inter, W * ocean::inter_len(g.N) * sizeof(float2))) != cudaSuccess ||
+            (e = dev_alloc(&g.tmap, W * ocean::tmap_len(g.N) * sizeof(float))) != cudaSuccess) {
             cudaFree(d_noise);
             cudaFree(d_h0);
             delete b;

@@ -37,6 +37,7 @@ EXPORTS = [
     "ocean_version", "ocean_backward", "ocean_device_status", "ocean_batch_create", "ocean_batch_update",
     "ocean_batch_device_status", "ocean_batch_destroy", "ocean_update_noalloc", "ocean_displace_grid",
     "ocean_grid_tess_levels", "ocean_shade_grid", "ocean_sky_envmap", "ocean_render_skybox",
+    "ocean_debug_fail_allocations",
 ]
 OCEAN_GRAD_ACCUMULATE = 1
 
@@ -132,6 +133,8 @@ def load() -> C.CDLL:
     L.ocean_sky_envmap.argtypes = [P(ocean_sky_params), vp, vp, vp, vp]
     L.ocean_render_skybox.argtypes = [vp, C.c_int32, P(C.c_float), P(C.c_float), C.c_int32, C.c_int32, vp, vp]
     L.ocean_last_error.restype = C.c_char_p
+    L.ocean_debug_fail_allocations.argtypes = [C.c_int32]
+    L.ocean_debug_fail_allocations.restype = None
     for name in EXPORTS:
         if name not in ("ocean_destroy", "ocean_last_error", "ocean_batch_destroy"):
             getattr(L, name).restype = C.c_int
@@ -272,6 +275,12 @@ def render_skybox(sky, view, projection, image, stream=None) -> None:
     p = (C.c_float * 16)(*[float(x) for x in np.asarray(projection, dtype=np.float32).reshape(16)])
     check(load().ocean_render_skybox(_addr(sky), int(sky.shape[1]), v, p, int(image.shape[1]), int(image.shape[0]),
                                      _addr(image), _stream(stream)))
+
+
+def debug_fail_allocations(after: int) -> None:
+    """Test hook: the library's allocations succeed `after` more times, then
+    fail with OCEAN_ERR_NOMEM; after < 0 turns it off."""
+    load().ocean_debug_fail_allocations(int(after))
 
 
 def load_sky_tables(texture_dir: str):

@@ -121,6 +121,12 @@ OCEAN_API int ocean_update_outputs(ocean_t* ocean, const ocean_outputs* out, voi
  * never checks its dispatches. */
 OCEAN_API int ocean_device_status(ocean_t* ocean, void* stream);
 
+/* Test hook for failure paths: from now on the library's device and pinned
+ * host allocations succeed `after` more times and then fail (the calling
+ * function returns OCEAN_ERR_NOMEM and releases what it had allocated) until
+ * the hook is set again; after < 0, the default, turns it off.  Process-wide. */
+OCEAN_API void ocean_debug_fail_allocations(int32_t after);
+
 /* Handle-owned output buffers (allocated on first use); the headless
  * stand-ins for the reference's GL textures m_dx/m_dy/m_dz/m_normal_map. */
 OCEAN_API int ocean_get_outputs(ocean_t* ocean, ocean_outputs* out);

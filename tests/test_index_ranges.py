@@ -1,0 +1,121 @@
+"""The hot-path kernels' index arithmetic replayed on the CPU for every N
+(compute-sanitizer is closed on the GPU pool): every global access stays
+inside its buffer and every element of each output is written exactly once,
+so no two threads race on a store.  Mirrors csrc/ocean_kernels.cu:
+inter_index, LineOut::pos, the row-pass stores, k_col_fft's row gather, tile
+copies and column-map stores, and k_col_out's staged loads and output stores."""
+import numpy as np
+import pytest
+
+# LineFor / ColLineFor decompositions (R1, R2, R3) of csrc/fft_line.cuh and ocean_kernels.cu
+LINE_FOR = {32: (8, 4, 1), 64: (8, 8, 1), 128: (16, 8, 1), 256: (16, 16, 1), 512: (16, 16, 2),
+            1024: (16, 16, 4), 2048: (16, 16, 8)}
+COL_LINE_FOR = {**LINE_FOR, 1024: (32, 32, 1), 2048: (32, 8, 8)}
+SIZES = sorted(LINE_FOR)
+
+
+def line(N, R):
+    R1, R2, R3 = R
+    G, E = N // R1, R1
+    RL = R3 if R3 > 1 else R2
+    NS = N // RL
+    t = np.arange(G)[:, None]
+    e = np.arange(E)[None, :]
+    return G, E, R1, (e // RL) * G + (e % RL) * NS, t        # pos(0, e) and the thread index
+
+
+def inter_rows(N):
+    return N // 2 + 1
+
+
+def inter_len(N):
+    return 3 * inter_rows(N) * N
+
+
+def inter_index(N, f, x, y):
+    return ((f * (N // 2) + (x >> 1)) * inter_rows(N) + y) * 2 + (x & 1)
+
+
+@pytest.mark.parametrize("N", SIZES)
+def test_row_pass_stores_cover_the_intermediate_once(N):
+    G, E, R1, pos, t = line(N, LINE_FOR[N])
+    H = inter_rows(N)
+    x = t + pos                                                  # (G, E) output positions of a line
+    assert np.array_equal(np.sort(x.ravel()), np.arange(N))
+    assert np.all(pos % 2 == 0)
+    hits = np.zeros(inter_len(N), np.int64)
+    for f in range(3):
+        for yp in range(H):
+            idx = inter_index(N, f, t, yp) + (pos >> 1) * (2 * H)     # the kernels' store address
+            assert np.array_equal(idx, inter_index(N, f, x, yp))
+            np.add.at(hits, idx.ravel(), 1)
+    assert np.all(hits == 1)
+
+
+@pytest.mark.parametrize("N", SIZES)
+def test_col_fft_gather_rows(N):
+    """Input r of thread t is row y = t + r*G: read from row ys <= N/2,
+    conjugated exactly when y > N/2 (the Hermitian half)."""
+    G, E, R1, _, t = line(N, COL_LINE_FOR[N])
+    r = np.arange(E)[None, :]
+    y = t + r * G
+    assert np.array_equal(np.sort(y.ravel()), np.arange(N))
+    ys = np.where(r < R1 // 2, t + r * G, np.where(r == R1 // 2, N // 2 - t, N - t - r * G))
+    cj = (r > R1 // 2) | ((r == R1 // 2) & (t != 0))
+    assert np.array_equal(ys, np.where(y <= N // 2, y, N - y))
+    assert np.array_equal(cj, y > N // 2)
+    assert ys.min() >= 0 and ys.max() <= N // 2
+
+
+@pytest.mark.parametrize("N", SIZES)
+def test_col_fft_tile_copies_and_map_stores(N):
+    G, E, R1, pos, t = line(N, COL_LINE_FOR[N])
+    H = inter_rows(N)
+    pairs = 1 if G >= 32 else 32 // G                             # ColCfg::PAIRS
+    ctas = (N // 2) // pairs
+    # three 1-D bulk copies per CTA: field f, pairs pair0 .. pair0+PAIRS-1, rows 0..N/2
+    hits = np.zeros(inter_len(N), np.int64)
+    for b in range(ctas):
+        for f in range(3):
+            s = inter_index(N, f, 2 * b * pairs, 0)
+            hits[s:s + pairs * H * 2] += 1
+    assert np.all(hits == 1)
+    # column maps [3][N (x)][N (y)]: line f of pair (x0, x0+1) writes y = t + pos for both columns
+    maps = np.zeros(3 * N * N, np.int64)
+    for b in range(ctas):
+        for pl in range(pairs):
+            x0 = 2 * (b * pairs + pl)
+            for f in range(3):
+                o = (f * N + x0) * N + t + pos
+                np.add.at(maps, o.ravel(), 1)
+                np.add.at(maps, (o + N).ravel(), 1)
+    assert np.all(maps == 1)
+
+
+@pytest.mark.parametrize("N", SIZES)
+def test_col_out_loads_and_stores(N):
+    T, W, TH = 32, 34, 256                                       # kOutT, kOutW, kOutTh
+    rows = T * T // TH
+    ncol = 3 * W
+    tid = np.arange(TH)
+    out = np.zeros(N * N, np.int64)
+    for bx in range(N // T):
+        for by in range(N // T):
+            x0, y0 = bx * T, by * T
+            i = np.arange(ncol * 8)
+            c = i >> 3
+            f, xx = c // W, c % W
+            ld = (f * N + ((x0 - 1 + xx) & (N - 1))) * N + y0 + 4 * (i & 7)
+            assert ld.min() >= 0 and ld.max() + 3 < 3 * N * N and np.all(ld % 4 == 0)
+            i = np.arange(2 * ncol)
+            c = i >> 1
+            f, xx = c // W, c % W
+            yy = np.where(i & 1, (y0 + T) & (N - 1), (y0 - 1) & (N - 1))
+            ld = (f * N + ((x0 - 1 + xx) & (N - 1))) * N + yy
+            assert ld.min() >= 0 and ld.max() < 3 * N * N
+            xs = tid % T + 1
+            yb = (tid // T) * rows
+            for k in range(rows):
+                o = (y0 + yb + k) * N + x0 + xs - 1
+                np.add.at(out, o, 1)
+    assert np.all(out == 1)
