@@ -374,9 +374,12 @@ __global__ void __launch_bounds__(RowCfg<N, FROM_H0>::THREADS, RowCfg<N, FROM_H0
 // other of two line-buffer sets; each set is the inputs, then the FFT's
 // exchange space.  Hand-off by named barriers: FULL[b] (prepass arrives,
 // transform waits) and EMPTY[b] (transform arrives, prepass waits before
-// refilling set b).  Both sides walk the same job sequence and execute the
-// same number of barrier operations whatever happens, so a timed-out copy
-// wait (flagged in the status word) never leaves a warp waiting.
+// refilling set b).  The first job's inputs are computed by every warp
+// before the split (its phases while its rows are still arriving), so the
+// transform warps start on job 0 without a FULL wait and the prepass warps
+// start at job 1.  Both sides walk the same job sequence and execute matching
+// barrier operations whatever happens, so a timed-out copy wait (flagged in
+// the status word) never leaves a warp waiting.
 // ---------------------------------------------------------------------------
 template <int N, bool FROM_H0>
 struct RowWsCfg {
