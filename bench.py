@@ -376,6 +376,7 @@ def run_gpu(args, world, rank, local):
     if not args.no_extra:
         out["grid"] = grid_stats
         out["adjoint"] = bench_adjoint(torch, og, dev, stream)
+        out["adjoint_large"] = bench_adjoint_large(torch, og, dev, stream)
         out["batched"] = bench_batched(torch, og, dev, stream, flush)
     if not args.no_cpu:
         out["cpu_baseline"] = cpu_baseline(N, args.cpu_seconds)
@@ -421,6 +422,54 @@ def bench_adjoint(torch, og, dev, stream, reps=5):
             "backward_ms": round(b, 4), "fwd_frames_per_s": round(T / (f * 1e-3), 1),
             "fwd_adj_frames_per_s": round(T / ((f + b) * 1e-3), 1), "adj_over_fwd": round((f + b) / f, 3),
             "gpu_launches_per_step": 3 * T + 2}
+
+
+def bench_adjoint_large(torch, og, dev, stream, n_sets=16, T=64, dt=0.05):
+    """Full-spectrum adjoint at N=2048: 16 parameter sets (L=3000, A~U(1,6),
+    V~U(10,35), theta~U(0,2pi), lambda~U(0.5,1.5), seeds 10..25), T=64 frames
+    at dt=0.05 s.  Per set: the 64 forward frames, then ocean_backward with
+    dL/dh0 for every mode (frames are not stored: the adjoint reads only h0).
+    Upstream gradients are seeded standard normals.  Reports frames/s of
+    both and the device memory the library holds per set (handle + adjoint
+    scratch)."""
+    import numpy as np
+    N = 2048
+    rng = np.random.default_rng(10)
+    times = [dt * j for j in range(T)]
+    G = torch.randn((3, T, N, N), device=dev, generator=torch.Generator(device=dev).manual_seed(10))
+    dh0 = torch.empty((N, N, 4), device=dev)
+    outs = [torch.empty((N, N), device=dev) for _ in range(3)] + [torch.empty((N, N, 4), device=dev)]
+    fwd_ms, bwd_ms, mem = 0.0, 0.0, 0
+    f = lambda v: float(np.float32(v))
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+    with torch.cuda.stream(stream):
+        for s in range(n_sets):
+            a = rng.uniform(0, 2 * math.pi)
+            p = og.Params(N=N, L=3000.0, amplitude=f(rng.uniform(1, 6)), wind_speed=f(rng.uniform(10, 35)),
+                          wind_dir_x=f(math.cos(a)), wind_dir_y=f(math.sin(a)), choppiness=f(rng.uniform(0.5, 1.5)),
+                          suppression=f(0.1), gravity=f(9.81))
+            torch.cuda.synchronize()
+            free0 = torch.cuda.mem_get_info()[0]
+            oc = og.Ocean(p, seed=10 + s)
+            oc.backward(times[:2], G[0, :2], G[1, :2], G[2, :2], dh0=dh0, stream=stream)   # allocates the scratch
+            torch.cuda.synchronize()
+            mem = max(mem, free0 - torch.cuda.mem_get_info()[0])
+            ev[0].record(stream)
+            for t in times:
+                oc.update(t, *outs, stream=stream)
+            ev[1].record(stream)
+            oc.backward(times, G[0], G[1], G[2], dh0=dh0, stream=stream)
+            ev[2].record(stream)
+            torch.cuda.synchronize()
+            fwd_ms += ev[0].elapsed_time(ev[1])
+            bwd_ms += ev[1].elapsed_time(ev[2])
+            oc.close()
+    del G
+    return {"workload": f"{n_sets} parameter sets, N={N}, T={T} frames at dt={dt} s, dL/dh0 per mode",
+            "forward_frames_per_s": round(n_sets * T / (fwd_ms * 1e-3), 1),
+            "backward_frames_per_s": round(n_sets * T / (bwd_ms * 1e-3), 1),
+            "fwd_adj_over_fwd": round((fwd_ms + bwd_ms) / fwd_ms, 3),
+            "device_bytes_per_set": int(mem), "frames_stored": 0}
 
 
 def batched_tiles(og, n_tiles=64, seed=2):
