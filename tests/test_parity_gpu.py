@@ -246,3 +246,25 @@ def test_outputs_in_pinned_host_memory(torch_cuda, ocean_lib):
         oc.device_status()
         for a, b in zip(dv, hv):
             assert torch.equal(a.cpu(), b)
+
+
+@pytest.mark.parametrize("N", [1024, 2048])
+def test_amplitude_scaling_is_exact(torch_cuda, ocean_lib, N):
+    """Size-independent property at full size.  h0 is proportional to
+    sqrt(A). Away from the +-4000 clamp, 4A therefore doubles h0 exactly, and
+    every later step is linear with scalings by 2 that commute with FP32
+    rounding, so dx, dy and dz double bit for bit."""
+    torch = torch_cuda
+    dev = torch.device("cuda")
+    outs = []
+    for A in (0.02, 0.08):
+        d = dict(P.c2(N), amplitude=A)
+        with ocean_lib.Ocean(P.lib_params(d), seed=d["seed"]) as oc:
+            o = [torch.empty((N, N), device=dev) for _ in range(3)] + [torch.empty((N, N, 4), device=dev)]
+            oc.update(123.25, *o)
+            torch.cuda.synchronize()
+            oc.device_status()
+            outs.append(o)
+    for a, b in zip(outs[0][:3], outs[1][:3]):
+        assert torch.any(a != 0)
+        assert torch.equal(2.0 * a, b)
