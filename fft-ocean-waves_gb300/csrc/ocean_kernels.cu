@@ -614,7 +614,13 @@ __global__ void __launch_bounds__(ColCfg<N>::THREADS) k_col_fft(const __grid_con
         for (int f = 0; f < 3; ++f)
             bulk_g2s(work + (size_t)f * CF::PAIRS * H * 2, in + inter_index(N, f, 2 * pair0, 0), CF::FIELD_BYTES, &bar);
     }
-    if (!block_wait(&bar, 0, &wait_ok, a.status)) return;
+    if (!block_wait(&bar, 0, &wait_ok, a.status)) {
+        // the twiddle copy may still be in flight: let it land (bounded) before
+        // the block's shared memory is released
+        if (tid == 0) (void)mbar_wait_bounded(&bar_tw, 0);
+        __syncthreads();
+        return;
+    }
 
     // Line li of pair pl holds field f = li % 3 (0: Dx, 1: Dy, 2: Dz) of both
     // columns, f(x0) + i*f(x0+1): the row-transformed spectra are Hermitian in
