@@ -471,7 +471,7 @@ __global__ void __launch_bounds__(RowWsCfg<N, FROM_H0>::THREADS, RowWsCfg<N, FRO
             if (x <= N / 2) row_position<N, FROM_H0, L::NPAD>(a, ring, bufs, tile, x, yp, fc, c[k], sn[k], r[k]);
         }
         __syncthreads();                                     // job 0's inputs are complete
-        if (nsmp == 1 && tid == 0) {                         // stage 0 is consumed: refill it
+        if (nsmp == 1 && tid == 0 && wait_ok) {              // stage 0 is consumed: refill it
             const int next = item + WC::STAGES * gridDim.x;
             if (next < n_items) {
                 fence_proxy_async_smem();
@@ -507,14 +507,16 @@ __global__ void __launch_bounds__(RowWsCfg<N, FROM_H0>::THREADS, RowWsCfg<N, FRO
     } else {
         const int pt = tid - WC::FFT_THREADS;
         uint32_t  phase_bits = 1u;                            // stage 0's first phase went to job 0
-        bool      gave_up    = wait_ok == 0;                  // a copy wait timed out: stop waiting
+        bool      gave_up    = wait_ok == 0;                  // a copy wait timed out: issue no more copies
         for (int j = 1; j < n_jobs; ++j) {
             const int b = j & 1, ki = j / nsmp, smp = j - ki * nsmp;
             const int item = blockIdx.x + ki * gridDim.x, tile = item / WC::ITEMS, yp = item % WC::ITEMS;
             const int st = ki % WC::STAGES;
             float2* stage = ring + (size_t)st * 2 * N * WC::EW;
-            if (smp == 0) {                                  // the item's rows (and, first, the twiddles)
-                if (pt == 0 && !gave_up) {
+            if (smp == 0) {                                  // the item's rows
+                // every issued copy is waited for (bounded), so none is in
+                // flight when the block exits
+                if (pt == 0) {
                     if (!mbar_wait_bounded(&bars[st], (phase_bits >> st) & 1u)) {
                         atomicOr(a.status, kDeviceTimeout);
                         (void)mbar_wait_bounded(&bars[st], (phase_bits >> st) & 1u);
@@ -533,7 +535,7 @@ __global__ void __launch_bounds__(RowWsCfg<N, FROM_H0>::THREADS, RowWsCfg<N, FRO
             named_arrive(WC::BAR_FULL + b, WC::THREADS);
             if (smp == nsmp - 1) {                           // every prepass thread is done with the stage
                 named_sync(WC::BAR_PRE, WC::PRE_THREADS);
-                if (pt == 0) {
+                if (pt == 0 && !gave_up) {
                     const int next = item + WC::STAGES * gridDim.x;
                     if (next < n_items) {
                         fence_proxy_async_smem();
