@@ -86,3 +86,31 @@ def test_null_arguments(ocean_lib):
     assert b"NULL" in lib.ocean_last_error()
     assert lib.ocean_fill_noise(0, 32, None) == ocean_lib.OCEAN_ERR_INVALID
     lib.ocean_destroy(None)
+
+
+def test_header_is_c99_and_links(ocean_lib, tmp_path):
+    """include/ocean.h compiles as strict C99 with warnings as errors, and a C
+    program taking the address of every declared entry point links against
+    the library (what a C host's binding would do)."""
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    names = _declared_functions()
+    src = tmp_path / "abi.c"
+    src.write_text('#include "ocean.h"\n#include <stdio.h>\n'
+                   "typedef void (*fn)(void);\n"
+                   "static const fn table[] = {\n" + ",\n".join(f"    (fn){n}" for n in names) + "\n};\n"
+                   "int main(void)\n{\n"
+                   "    printf(\"%d %u\\n\", ocean_version(), (unsigned)(sizeof table / sizeof table[0]));\n"
+                   "    return 0;\n}\n")
+    lib_dir = os.path.dirname(ocean_lib.LIB_PATH)
+    exe = tmp_path / "abi"
+    r = subprocess.run([cc, "-std=c99", "-Wall", "-Wextra", "-Werror", "-pedantic", "-Wno-pedantic", "-I",
+                        os.path.join(ROOT, "include"), str(src), "-o", str(exe), "-L", lib_dir, "-locean_gb300",
+                        f"-Wl,-rpath,{lib_dir}"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    out = subprocess.run([str(exe)], capture_output=True, text=True)
+    assert out.returncode == 0, out.stderr
+    assert out.stdout.split() == ["100", str(len(names))]
