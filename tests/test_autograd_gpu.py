@@ -75,7 +75,7 @@ def test_h0_loss_gradient_matches_oracle(torch_cuda, ocean_lib, oracle_mod):
             res[k].append(2.0 / n * (a[k] - b[k]))
             L64 += np.sum((a[k] - b[k]) ** 2) / n
     dh0_ref, _ = oracle_mod.backward(op, ha, times, np.array(res["dx"]), np.array(res["dy"]), np.array(res["dz"]))
-    assert abs(float(loss) - L64) < 1e-4 * L64
+    assert abs(float(loss.detach()) - L64) < 1e-4 * L64
     assert rel_l2(h0.grad.cpu().numpy(), dh0_ref) < 1e-4
     oc.close()
     tgt.close()
