@@ -126,6 +126,29 @@ def test_hermitian_h0_gives_real_transform(oracle_mod):
     assert np.abs(full.imag).max() < 1e-12 * np.abs(full.real).max()
 
 
+@pytest.mark.parametrize("literal", [False, True])
+def test_translation_and_superposition(oracle_mod, literal):
+    """A phase ramp on h0 shifts every output map by whole texels. With
+    phi = 2 pi (ix sx + iz sz) / N, h0k takes e^{-i phi}. h0minusk takes e^{+i phi},
+    because it enters conjugated; with the literal conjugate it takes e^{-i phi}.
+    dx, dy, dz are also linear in h0.  The GPU tests check both properties at
+    full size."""
+    N, sx, sz, t = 32, 5, -3, 7.25
+    p = P.oracle_params(P.c2(N), literal_conj=literal)
+    h = oracle_mod.h0(p, oracle_mod.noise(1, N))
+    ix = np.arange(N) - N // 2
+    w = np.exp(1j * 2 * np.pi * (ix[None, :] * sx + ix[:, None] * sz) / N)
+    hk = (h[..., 0] + 1j * h[..., 1]) * np.conj(w)
+    hm = (h[..., 2] + 1j * h[..., 3]) * (np.conj(w) if literal else w)
+    hs = np.stack([hk.real, hk.imag, hm.real, hm.imag], -1)
+    a, b = oracle_mod.update(p, h, t), oracle_mod.update(p, hs, t)
+    for k in ("dx", "dy", "dz", "nj"):
+        assert rel_l2(b[k], np.roll(a[k], (sz, sx), axis=(0, 1))) < 1e-13
+    c = oracle_mod.update(p, h + hs, t)
+    for k in ("dx", "dy", "dz"):
+        assert rel_l2(c[k], a[k] + b[k]) < 1e-13
+
+
 def test_outputs_stencils(oracle_mod):
     """finish(): lambda scaling, Sobel normal and Jacobian against direct numpy."""
     N = 16

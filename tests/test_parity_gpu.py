@@ -268,3 +268,66 @@ def test_amplitude_scaling_is_exact(torch_cuda, ocean_lib, N):
     for a, b in zip(outs[0][:3], outs[1][:3]):
         assert torch.any(a != 0)
         assert torch.equal(2.0 * a, b)
+
+
+def _frame(torch, oc, N, t):
+    dev = torch.device("cuda")
+    o = [torch.empty((N, N), device=dev) for _ in range(3)] + [torch.empty((N, N, 4), device=dev)]
+    oc.update(t, *o)
+    torch.cuda.synchronize()
+    oc.device_status()
+    return o
+
+
+def _rel(torch, a, b):
+    a, b = a.double(), b.double()
+    return float(torch.linalg.vector_norm(a - b) / torch.linalg.vector_norm(b))
+
+
+def _maps(o):
+    """dx, dy, dz, the normal (xyz) and the Jacobian of one frame."""
+    return [o[0], o[1], o[2], o[3][..., :3], o[3][..., 3]]
+
+
+@pytest.mark.parametrize("N,literal", [(2048, False), (1024, True)])
+def test_translation_full_size(torch_cuda, ocean_lib, N, literal):
+    """Size-independent property at full size.  With phi = 2 pi (ix sx + iz sz) / N,
+    multiply h0k by e^{-i phi} and h0minusk by e^{+i phi}; with the literal conjugate,
+    h0minusk also takes e^{-i phi}, because it enters unconjugated.  This shifts every
+    output map by (sx, sz) texels: dx, dy, dz, the Sobel normal and the Jacobian."""
+    torch = torch_cuda
+    d = P.c2(N)
+    sx, sz, t = 5, -3, 77.5
+    with ocean_lib.Ocean(P.lib_params(d, literal_conj=literal), seed=d["seed"]) as oc:
+        h0 = torch.empty((N, N, 4), device="cuda")
+        oc.get_h0(h0)
+        a = _frame(torch, oc, N, t)
+        ix = torch.arange(N, dtype=torch.float64, device="cuda") - N // 2
+        phi = 2.0 * math.pi * (ix[None, :] * sx + ix[:, None] * sz) / N
+        w = torch.polar(torch.ones_like(phi), phi)
+        hk = torch.complex(h0[..., 0].double(), h0[..., 1].double()) * w.conj()
+        hm = torch.complex(h0[..., 2].double(), h0[..., 3].double()) * (w.conj() if literal else w)
+        oc.set_h0(torch.stack([hk.real, hk.imag, hm.real, hm.imag], -1).float().contiguous())
+        b = _frame(torch, oc, N, t)
+    for x, y in zip(_maps(a), _maps(b)):
+        assert _rel(torch, y, torch.roll(x, (sz, sx), dims=(0, 1))) < 2 * TOL
+
+
+def test_superposition_full_size(torch_cuda, ocean_lib):
+    """Size-independent property at full size: dx, dy, dz are linear in h0, so
+    the frame of h0a + h0b is the sum of the frames of h0a and h0b."""
+    torch = torch_cuda
+    N, t = 2048, 31.0
+    frames, h0s = [], []
+    for seed in (1, 2):
+        d = dict(P.c2(N), seed=seed)
+        with ocean_lib.Ocean(P.lib_params(d), seed=seed) as oc:
+            h0 = torch.empty((N, N, 4), device="cuda")
+            oc.get_h0(h0)
+            h0s.append(h0)
+            frames.append(_frame(torch, oc, N, t))
+    with ocean_lib.Ocean(P.lib_params(P.c2(N)), seed=1) as oc:
+        oc.set_h0((h0s[0] + h0s[1]).contiguous())
+        s = _frame(torch, oc, N, t)
+    for k in range(3):
+        assert _rel(torch, s[k], frames[0][k] + frames[1][k]) < 2 * TOL
