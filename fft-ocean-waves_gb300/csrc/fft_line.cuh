@@ -193,8 +193,9 @@ __device__ __forceinline__ void line_sync(int li)
 // One exchange + pass: the registers hold the outputs of a pass of radix RP
 // with stride NSP; they are written to `buf`, re-read as the inputs of a pass
 // of radix RN (stride NSP*RP), twiddled and transformed.  Contains two line
-// barriers (see line_sync).
-template <class C, int RP, int NSP, int RN, int SIGN, bool NAMED>
+// barriers (see line_sync); without TAIL_SYNC only the first, and a thread may
+// then leave while others of its line still read `buf`.
+template <class C, int RP, int NSP, int RN, int SIGN, bool NAMED, bool TAIL_SYNC = true>
 __device__ __forceinline__ void stockham_pass(float2* v, float2* buf, const float2* tw, int t, bool active, int li)
 {
     constexpr int N   = C::N;
@@ -217,7 +218,7 @@ __device__ __forceinline__ void stockham_pass(float2* v, float2* buf, const floa
             for (int r = 0; r < RN; ++r) v[b * RN + r] = buf[C::pad(j + r * (N / RN))];
         }
     }
-    line_sync<C, NAMED>(li);
+    if constexpr (TAIL_SYNC) line_sync<C, NAMED>(li);
     if (!active) return;
     // twiddle plan of this pass: entry r*NSN + k
     const float2* T = NSP == 1 ? tw : tw + TwPlan<C>::P2;
@@ -239,16 +240,19 @@ __device__ __forceinline__ void stockham_pass(float2* v, float2* buf, const floa
 // Full line transform of line `li` (barrier id 1 + li, so li < 15; NAMED as
 // in line_sync).  On entry
 // v[r] = x[t + r*N/R1]; on exit v[b*RL + r] = X[(t + b*G) + r*(N/RL)] with RL
-// the last radix.  tw: the decomposition's twiddle plan (TwPlan<C>).  On return every thread of the line has finished reading
-// `buf`.  Threads with active == false do no work; for lines of >= 32 threads
+// the last radix.  tw: the decomposition's twiddle plan (TwPlan<C>).  With
+// TAIL_SYNC, on return every thread of the line has finished reading `buf`.
+// Without it the final line barrier is left out: for callers that do not
+// write `buf` again, or that order the reuse by a barrier of their own.
+// Threads with active == false do no work; for lines of >= 32 threads
 // they may skip the call entirely, for smaller lines they must call it (the
 // barrier is then the block's).
-template <class C, int SIGN, bool NAMED = true>
+template <class C, int SIGN, bool NAMED = true, bool TAIL_SYNC = true>
 __device__ __forceinline__ void line_fft(float2* v, float2* buf, const float2* tw, int t, int li, bool active = true)
 {
     if (active) dft<C::R1, SIGN>(v);
-    stockham_pass<C, C::R1, 1, C::R2, SIGN, NAMED>(v, buf, tw, t, active, li);
-    if constexpr (C::R3 > 1) stockham_pass<C, C::R2, C::R1, C::R3, SIGN, NAMED>(v, buf, tw, t, active, li);
+    stockham_pass<C, C::R1, 1, C::R2, SIGN, NAMED, (C::R3 > 1) || TAIL_SYNC>(v, buf, tw, t, active, li);
+    if constexpr (C::R3 > 1) stockham_pass<C, C::R2, C::R1, C::R3, SIGN, NAMED, TAIL_SYNC>(v, buf, tw, t, active, li);
 }
 
 template <class C>

@@ -497,8 +497,10 @@ __global__ void __launch_bounds__(RowWsCfg<N, FROM_H0>::THREADS, RowWsCfg<N, FRO
 #pragma unroll
             for (int r = 0; r < L::E; ++r) v[r] = buf[t + r * L::G];
             line_sync<L, true>(li);
-            line_fft<L, +1>(v, buf, tw_s, t, li);
-            named_arrive(WC::BAR_EMPTY + b, WC::THREADS);    // every thread of the line is done with buf
+            // no final line barrier: the prepass refills buf only after every
+            // transform thread has arrived on EMPTY, each after its own reads
+            line_fft<L, +1, true, false>(v, buf, tw_s, t, li);
+            named_arrive(WC::BAR_EMPTY + b, WC::THREADS);    // this thread is done with buf
             static_assert(L::G % 2 == 0 && LineOut<L>::NS % 2 == 0, "even output offsets");
             float2* out = a.inter + (size_t)unit * inter_len(N) + inter_index(N, li, t, yp);
 #pragma unroll
@@ -650,7 +652,7 @@ __global__ void __launch_bounds__(ColCfg<N>::THREADS) k_col_fft(const __grid_con
     }
     if (!block_wait(&bar_tw, 0, &wait_ok, a.status)) return;   // also: the tile is consumed
     pdl_launch_dependents();                                 // k_col_out may start its set-up
-    line_fft<L, +1>(v, work + li * L::NPAD, tw_s, t, li);
+    line_fft<L, +1, true, false>(v, work + li * L::NPAD, tw_s, t, li);   // no final barrier: work is not reused
 
     // output y = pos(t, e) is t plus an even constant: the (-1)^(x+y) sign is
     // the thread's, and the two columns' signs are opposite.  Dy is scaled by
