@@ -106,7 +106,7 @@ def test_parameter_fit_converges(torch_cuda, ocean_lib):
         loss = ((D - target) ** 2).mean()
         loss.backward()
         opt.step()
-        losses.append(float(loss))
+        losses.append(float(loss.detach()))
     model.close()
     sigma2 = 0.02 ** 2
     assert losses[0] > 10 * sigma2
