@@ -186,6 +186,8 @@ def cpu_baseline(N, seconds, threads=None):
 
 
 def parity_check(N, gpu_frame, t):
+    """Part of the CPU leg, after the timed region: the FP64 oracle checks one
+    GPU frame (err_vs_fp64).  Nothing timed runs through the oracle."""
     from oracle import oracle
     import numpy as np
     d = c2_params(N)
