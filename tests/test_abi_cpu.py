@@ -114,3 +114,69 @@ def test_header_is_c99_and_links(ocean_lib, tmp_path):
     out = subprocess.run([str(exe)], capture_output=True, text=True)
     assert out.returncode == 0, out.stderr
     assert out.stdout.split() == ["100", str(len(names))]
+
+
+STRUCTS = ["ocean_params", "ocean_outputs", "ocean_grads", "ocean_grid_params", "ocean_shade_params",
+           "ocean_sky_params"]
+
+
+def _c_layout(tmp_path, structs):
+    """sizeof and every field's offsetof, as a C compiler lays out the
+    structs of include/ocean.h: {struct: (size, {field: offset})}."""
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    lines = ['#include "ocean.h"', "#include <stddef.h>", "#include <stdio.h>", "int main(void)", "{"]
+    for name, fields in structs.items():
+        lines.append(f'    printf("{name} .sizeof %zu\\n", sizeof({name}));')   # no field is named so
+        for f in fields:
+            lines.append(f'    printf("{name} {f} %zu\\n", offsetof({name}, {f}));')
+    lines += ["    return 0;", "}"]
+    src, exe = tmp_path / "layout.c", tmp_path / "layout"
+    src.write_text("\n".join(lines) + "\n")
+    r = subprocess.run([cc, "-std=c99", "-Wall", "-Werror", "-I", os.path.join(ROOT, "include"), str(src), "-o",
+                        str(exe)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split("\n")
+    res = {}
+    for ln in filter(None, out):
+        name, key, val = ln.split()
+        entry = res.setdefault(name, [0, {}])
+        if key == ".sizeof":
+            entry[0] = int(val)
+        else:
+            entry[1][key] = int(val)
+    return {k: (v[0], v[1]) for k, v in res.items()}
+
+
+def test_ctypes_structs_match_the_header(ocean_lib, tmp_path):
+    """Every ctypes structure of the binding has the C header's size, field
+    names, field order and field offsets (a mismatch would pass arguments
+    silently wrong)."""
+    import ctypes
+    structs = {n: [f[0] for f in getattr(ocean_lib, n)._fields_] for n in STRUCTS}
+    c = _c_layout(tmp_path, structs)
+    for n in STRUCTS:
+        cls = getattr(ocean_lib, n)
+        size, offs = c[n]
+        assert ctypes.sizeof(cls) == size, n
+        assert [getattr(cls, f).offset for f in structs[n]] == [offs[f] for f in structs[n]], n
+        # the header declares no fields beyond these: the last one ends the struct
+        last = structs[n][-1]
+        assert offs[last] + ctypes.sizeof(dict(cls._fields_)[last]) <= size
+        assert size - (offs[last] + ctypes.sizeof(dict(cls._fields_)[last])) < 8, n
+
+
+def test_integration_snippet_structs_match_the_binding(ocean_lib):
+    """The ctypes structures a maintainer copies from INTEGRATION.md are the
+    binding's (same field names and types in the same order)."""
+    import ctypes
+    text = open(os.path.join(ROOT, "INTEGRATION.md")).read()
+    block = text.split("```python", 1)[1].split("```", 1)[0]
+    ns = {}
+    exec("\n".join(ln for ln in block.splitlines() if not ln.startswith(("lib", "h =", "p =", "assert", "outs"))),
+         {"C": ctypes, "ctypes": ctypes}, ns)
+    for n in ("ocean_params", "ocean_outputs"):
+        assert ns[n]._fields_ == getattr(ocean_lib, n)._fields_, n
