@@ -135,8 +135,10 @@ def load() -> C.CDLL:
     L.ocean_last_error.restype = C.c_char_p
     L.ocean_debug_fail_allocations.argtypes = [C.c_int32]
     L.ocean_debug_fail_allocations.restype = None
+    not_int = ("ocean_destroy", "ocean_batch_destroy", "ocean_debug_fail_allocations",   # void
+               "ocean_last_error")                                                      # const char*
     for name in EXPORTS:
-        if name not in ("ocean_destroy", "ocean_last_error", "ocean_batch_destroy"):
+        if name not in not_int:
             getattr(L, name).restype = C.c_int
     _lib = L
     return L

@@ -180,3 +180,48 @@ def test_integration_snippet_structs_match_the_binding(ocean_lib):
          {"C": ctypes, "ctypes": ctypes}, ns)
     for n in ("ocean_params", "ocean_outputs"):
         assert ns[n]._fields_ == getattr(ocean_lib, n)._fields_, n
+
+
+def _c_kind(t):
+    """Canonical kind of a C parameter or return type of include/ocean.h."""
+    t = " ".join(t.replace("const", " ").split())
+    if "*" in t:
+        return "ptr"
+    return {"void": None, "int": "i32", "int32_t": "i32", "uint32_t": "u32", "int64_t": "i64",
+            "uint64_t": "u64", "float": "f32", "double": "f64"}[t]
+
+
+def _ctypes_kind(t):
+    if t is None:
+        return None
+    if t in (C.c_void_p, C.c_char_p) or isinstance(t, type(C.POINTER(C.c_int))):
+        return "ptr"
+    for kind, ts in (("i32", (C.c_int, C.c_int32)), ("u32", (C.c_uint32,)), ("i64", (C.c_int64,)),
+                     ("u64", (C.c_uint64,)), ("f32", (C.c_float,)), ("f64", (C.c_double,))):
+        if t in ts:
+            return kind
+    raise AssertionError(f"unexpected ctypes type {t}")
+
+
+def test_ctypes_signatures_match_the_header(ocean_lib):
+    """Each entry point's ctypes argtypes and restype in the binding have the
+    kinds (pointer, 32/64-bit integer, float, double) of its prototype in
+    include/ocean.h.  A double passed where the C side expects an int would
+    otherwise go through silently."""
+    src = open(os.path.join(ROOT, "include", "ocean.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    protos = re.findall(r"OCEAN_API\s+([\w\s\*]+?)\s*\b(ocean_\w+)\s*\(([^)]*)\)\s*;", src)
+    assert len(protos) == len(_declared_functions())
+    lib = ocean_lib.load()
+    for ret, name, params in protos:
+        params = " ".join(params.split())
+        kinds = [] if params in ("", "void") else [
+            _c_kind(re.sub(r"\b\w+$", "", p.strip()) if not p.strip().endswith("*") else p) for p in params.split(",")]
+        fn = getattr(lib, name)
+        if fn.argtypes is None:
+            assert kinds == [], f"{name}: the binding sets no argtypes for {kinds}"
+        else:
+            assert [_ctypes_kind(t) for t in fn.argtypes] == kinds, name
+        want = _c_kind(ret)
+        got = _ctypes_kind(fn.restype)
+        assert got == want, f"{name}: restype {got} vs {want}"
