@@ -3,7 +3,9 @@
 inside its buffer and every element of each output is written exactly once,
 so no two threads race on a store.  Mirrors csrc/ocean_kernels.cu:
 inter_index, LineOut::pos, the row-pass stores, k_col_fft's row gather, tile
-copies and column-map stores, and k_col_out's staged loads and output stores."""
+copies and column-map stores, k_col_out's staged loads and output stores, and
+the adjoint's column-pass loads and stores and row-pass dh0 updates
+(csrc/ocean_adjoint.cu)."""
 import numpy as np
 import pytest
 
@@ -119,3 +121,67 @@ def test_col_out_loads_and_stores(N):
                 o = (y0 + yb + k) * N + x0 + xs - 1
                 np.add.at(out, o, 1)
     assert np.all(out == 1)
+
+
+@pytest.mark.parametrize("N", SIZES)
+def test_adjoint_column_pass_loads_and_stores(N):
+    """k_adj_col_pass (csrc/ocean_adjoint.cu): C columns per CTA, gy + i*gx
+    lines per column and gz lines per column pair. Loads stay in the frame;
+    every (field, ky <= N/2, x) of the frame's adjoint slab [3][H][N] is
+    written once; the float4 Dz stores are 16-byte aligned."""
+    G, E, R1, _, _ = line(N, LINE_FOR[N])
+    C = 4 if N >= 2048 else 8
+    WL, ZL = C, C // 2
+    H = inter_rows(N)
+    hits = np.zeros(3 * H * N, np.int64)
+    for bx in range(N // C):
+        x0 = bx * C
+        u = np.arange(WL * G)                                     # gy + i*gx lines
+        lane, t = u % WL, u // WL
+        y = t[:, None] + np.arange(E)[None, :] * (N // R1)
+        x = x0 + lane
+        assert y.max() < N and x.max() < N
+        u = np.arange(ZL * G)                                     # gz pair lines, float2 loads
+        lane, t = u % ZL, u // ZL
+        x = x0 + 2 * lane
+        assert x.max() + 1 < N and np.all(x % 2 == 0)
+        ky = np.arange(H)
+        for c in range(WL):
+            for f in (0, 1):
+                np.add.at(hits, (f * H + ky) * N + x0 + c, 1)
+        for p in range(ZL):
+            o = (2 * H + ky) * N + x0 + 2 * p                     # float2 units
+            assert np.all(o % 2 == 0)                             # 16-byte aligned float4 store
+            np.add.at(hits, o, 1)
+            np.add.at(hits, o + 1, 1)
+    assert np.all(hits == 1)
+
+
+@pytest.mark.parametrize("N", SIZES)
+def test_adjoint_row_pass_accumulators_and_dh0(N):
+    """k_adj_row_pass: within a frame each shared accumulator (pair, side,
+    mx) has one writer. Across the CTAs, dh0 gets exactly one
+    read-modify-write per (y, x): rows 0 and N/2 are their own mirrors and
+    skip side 1."""
+    G = N // LINE_FOR[N][0]
+    pairs = 1 if G >= 32 else 32 // G
+    H = inter_rows(N)
+    dh0 = np.zeros(N * N, np.int64)
+    for b in range((H + pairs - 1) // pairs):
+        acc = np.zeros(2 * pairs * N, np.int64)
+        for pl in range(pairs):
+            yp = b * pairs + pl
+            if yp >= H:
+                continue
+            yq = (N - yp) & (N - 1)
+            kx = np.arange(N)
+            np.add.at(acc, (pl * 2 + 0) * N + kx, 1)
+            if yq != yp:
+                np.add.at(acc, (pl * 2 + 1) * N + ((N - kx) & (N - 1)), 1)
+            for side in (0, 1):
+                y = yq if side else yp
+                if side and y == yp:
+                    continue
+                np.add.at(dh0, y * N + kx, 1)
+        assert acc.max() <= 1
+    assert np.all(dh0 == 1)
