@@ -199,6 +199,10 @@ int check_grid(const ocean_grid_params* g)
         return fail(OCEAN_ERR_INVALID, "squares must be even and in [2, 16384]");
     if (!std::isfinite(g->texcoord_scale) || !std::isfinite(g->displacement_scale))
         return fail(OCEAN_ERR_INVALID, "grid scales must be finite");
+    // bounds the texel step (scale * N / squares <= 3.3e10) so that it and its
+    // per-vertex multiples stay exact integers (the reference uses 64)
+    if (std::fabs(g->texcoord_scale) > 1.0e6f)
+        return fail(OCEAN_ERR_INVALID, "texcoord_scale must be within +-1e6");
     return OCEAN_OK;
 }
 

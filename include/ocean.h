@@ -217,7 +217,7 @@ OCEAN_API int ocean_update_noalloc(const ocean_params* params, const float* h0_d
  * i0+squares+2). */
 typedef struct ocean_grid_params {
     int32_t squares;            /* even, 2..16384; the reference uses 1024 */
-    float   texcoord_scale;     /* texture repeats over the grid; the reference uses 64 */
+    float   texcoord_scale;     /* texture repeats over the grid, |.| <= 1e6; the reference uses 64 */
     float   displacement_scale; /* vertical scale of Dy; the reference's default 0.5 (main.cpp:1632) */
     float   camera[3];          /* eye position for the tessellation levels */
 } ocean_grid_params;

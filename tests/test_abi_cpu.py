@@ -225,3 +225,20 @@ def test_ctypes_signatures_match_the_header(ocean_lib):
         want = _c_kind(ret)
         got = _ctypes_kind(fn.restype)
         assert got == want, f"{name}: restype {got} vs {want}"
+
+
+def test_grid_parameter_validation_before_any_device_call(ocean_lib):
+    """ocean_displace_grid / ocean_grid_tess_levels check their parameters
+    first: odd or out-of-range square counts, non-finite scales and texture
+    scales beyond +-1e6 (whose texel step would leave the integer range) are
+    rejected without a CUDA call."""
+    lib = ocean_lib.load()
+    bad = [ocean_lib.grid_params(3), ocean_lib.grid_params(0), ocean_lib.grid_params(32768),
+           ocean_lib.grid_params(2, float("nan")), ocean_lib.grid_params(2, 64.0, float("inf")),
+           ocean_lib.grid_params(2, 1.0e30), ocean_lib.grid_params(2, -2.0e6)]
+    for g in bad:
+        assert lib.ocean_displace_grid(None, 32, C.byref(g), None, None) == ocean_lib.OCEAN_ERR_INVALID
+        assert lib.ocean_grid_tess_levels(C.byref(g), None, None) == ocean_lib.OCEAN_ERR_INVALID
+    rc = lib.ocean_grid_tess_levels(C.byref(ocean_lib.grid_params(2, 1.0e30)), None, None)
+    assert rc == ocean_lib.OCEAN_ERR_INVALID
+    assert "texcoord_scale" in lib.ocean_last_error().decode()
