@@ -259,7 +259,8 @@ extern "C" int ocean_shade_grid(const float* vertices, int64_t n_vertices, const
 {
     using namespace ocean::host;
     if (!vertices || !p || !sky_cubemap || !colors) return fail(OCEAN_ERR_INVALID, "NULL pointer");
-    if (n_vertices < 0) return fail(OCEAN_ERR_INVALID, "n_vertices must be >= 0");
+    if (n_vertices < 0 || n_vertices > (int64_t)0x7fffffff * 256)   // one launch of 256-thread blocks
+        return fail(OCEAN_ERR_INVALID, "n_vertices must be in [0, 2^31 * 256)");
     if (p->sky_size < 1 || p->sky_size > 16384) return fail(OCEAN_ERR_INVALID, "sky_size must be in [1, 16384]");
     if ((reinterpret_cast<uintptr_t>(vertices) | reinterpret_cast<uintptr_t>(sky_cubemap) |
          reinterpret_cast<uintptr_t>(colors)) % 16)

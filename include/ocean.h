@@ -246,7 +246,8 @@ OCEAN_API int ocean_grid_tess_levels(const ocean_grid_params* grid, float* level
  * c / (c + 1) and gamma 1/2.2.  sky_cubemap: device, 6 faces (+X, -X, +Y,
  * -Y, +Z, -Z) of sky_size^2 RGBA floats, looked up as the OpenGL cube-map
  * table specifies (bilinear within a face, clamp to edge).  vertices: as
- * ocean_displace_grid writes them (n_vertices * 8 floats).  colors: device,
+ * ocean_displace_grid writes them (n_vertices * 8 floats, 0 <= n_vertices <
+ * 2^31 * 256: one launch).  colors: device,
  * n_vertices * 4 floats (RGB, 1).  All three 16-byte aligned.  As in the
  * shader, the result is undefined (NaN) for normals longer than 1 with
  * N.V > 1, where the Fresnel term goes negative. */

@@ -239,6 +239,11 @@ def test_grid_parameter_validation_before_any_device_call(ocean_lib):
     for g in bad:
         assert lib.ocean_displace_grid(None, 32, C.byref(g), None, None) == ocean_lib.OCEAN_ERR_INVALID
         assert lib.ocean_grid_tess_levels(C.byref(g), None, None) == ocean_lib.OCEAN_ERR_INVALID
+    # shading: a vertex count beyond one launch's 2^31 blocks of 256 (the
+    # device addresses are never touched before the count is checked)
+    sp = ocean_lib.ocean_shade_params((C.c_float * 3)(0, 10, 0), (C.c_float * 3)(0, -1, 0), (C.c_float * 3)(0, 0, 1), 16)
+    for n in (-1, 0x7fffffff * 256 + 1):
+        assert lib.ocean_shade_grid(16, n, C.byref(sp), 16, 16, None) == ocean_lib.OCEAN_ERR_INVALID
     rc = lib.ocean_grid_tess_levels(C.byref(ocean_lib.grid_params(2, 1.0e30)), None, None)
     assert rc == ocean_lib.OCEAN_ERR_INVALID
     assert "texcoord_scale" in lib.ocean_last_error().decode()
