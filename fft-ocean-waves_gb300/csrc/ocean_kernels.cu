@@ -32,6 +32,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <atomic>
+
 #include "fft_line.cuh"
 #include "ocean_device.cuh"
 #include "ocean_internal.h"
@@ -845,7 +847,10 @@ template <int N, bool MULTI, bool FROM_H0>
 static cudaError_t row_pass_nm(const RowArgs& a, cudaStream_t s)
 {
     using RC = RowCfg<N, FROM_H0>;
-    static int grid = 0;   // persistent grid: resident CTAs per SM x SMs
+    // persistent grid (resident CTAs per SM x SMs), found on the first launch;
+    // threads racing here set the same attribute and store the same value
+    static std::atomic<int> cached{0};
+    int grid = cached.load(std::memory_order_acquire);
     if (!grid) {
         cudaError_t e = cudaFuncSetAttribute(k_row_pass<N, MULTI, FROM_H0>,
                                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)RC::SMEM);
@@ -858,6 +863,7 @@ static cudaError_t row_pass_nm(const RowArgs& a, cudaStream_t s)
         if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
         if (per_sm < 1) return cudaErrorInvalidConfiguration;
         grid = per_sm * sms;
+        cached.store(grid, std::memory_order_release);
     }
     const int items = a.tiles * RC::ITEMS;
     k_row_pass<N, MULTI, FROM_H0><<<grid < items ? grid : items, RC::THREADS, RC::SMEM, s>>>(a);
@@ -868,7 +874,10 @@ template <int N, bool MULTI, bool FROM_H0>
 static cudaError_t row_ws_nm(const RowArgs& a, cudaStream_t s)
 {
     using WC = RowWsCfg<N, FROM_H0>;
-    static int grid = 0;   // resident CTAs per SM x SMs
+    // resident CTAs per SM x SMs, found on the first launch; threads racing
+    // here set the same attribute and store the same value
+    static std::atomic<int> cached{0};
+    int grid = cached.load(std::memory_order_acquire);
     if (!grid) {
         cudaError_t e = cudaFuncSetAttribute(k_row_ws<N, MULTI, FROM_H0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              (int)WC::SMEM);
@@ -881,6 +890,7 @@ static cudaError_t row_ws_nm(const RowArgs& a, cudaStream_t s)
         if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
         if (per_sm < 1) return cudaErrorInvalidConfiguration;
         grid = per_sm * sms;
+        cached.store(grid, std::memory_order_release);
     }
     const int items = a.tiles * WC::ITEMS;
     k_row_ws<N, MULTI, FROM_H0><<<grid < items ? grid : items, WC::THREADS, WC::SMEM, s>>>(a);
@@ -916,11 +926,11 @@ template <int N>
 static cudaError_t col_fft_n(int units, const ColArgs& a, cudaStream_t s, bool pdl)
 {
     using CF = ColCfg<N>;
-    static bool attr = false;
-    if (!attr) {
+    static std::atomic<bool> attr{false};   // set once; racing threads set the same value
+    if (!attr.load(std::memory_order_acquire)) {
         cudaError_t e = cudaFuncSetAttribute(k_col_fft<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)CF::SMEM);
         if (e != cudaSuccess) return e;
-        attr = true;
+        attr.store(true, std::memory_order_release);
     }
     cudaLaunchAttribute at[1] = {pdl_attr()};
     cudaLaunchConfig_t  cfg   = {};
