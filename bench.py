@@ -2,13 +2,26 @@
 
 Workload (default): the plain drop-in tile at N=1024 -- L=2000 m, A=2, wind
 30 m/s at 30 deg, lambda=1.3, l=0.1, seeded uniform noise (seed 1) -- advanced
-frame by frame at dt = 1/60 s from t = 0.  A step is one frame: the row pass
-(evolution + choppy + horizontal FFT) and the column pass (vertical FFT +
-inversion + lambda + normal + Jacobian), both our kernels.  Between steps L2 is
-flushed (a 512 MiB buffer written, then a 512 MiB buffer read, which leaves L2
-holding clean lines of the flush buffer), so every frame starts from HBM as it
-would inside a renderer's frame.  Each frame is timed with CUDA events on the
-launching stream; `value` = frames / sum of frame times.
+frame by frame at dt = 1/60 s from t = 0 (workloads.plain).  A step is one
+frame: the row pass (evolution + choppy + horizontal FFT) and the column pass
+(vertical FFT + inversion + lambda + normal + Jacobian), our kernels only.
+
+value: K frames back to back on one stream, timed by two CUDA events around
+all of them.  The frames rotate over R = 8 tiles with their own spectrum,
+scratch and output maps (8 x 97 MB, well above the 129 MB L2), so a frame's
+spectrum was last touched 7 frames (about 600 MB of traffic) earlier and is
+read from HBM, as in a renderer's frame; no L2 flush runs inside the timed
+region.  A device-side sleep before the first timed frame lets the host queue
+the frames ahead of the GPU, so the device never waits for a launch.
+
+isolated: the same frames one at a time, L2 flushed before each (a 512 MiB
+buffer written, then a 512 MiB buffer read) and each frame bracketed by its own
+CUDA events, so every frame also pays the launch of its first kernel.
+
+kernel_ms: each stage launched K times back to back over the R tiles between
+two events (the average launch duration on the stream); the row stage's
+spectrum comes from HBM as in a frame, the column stages' inputs (which a live
+frame finds in L2) come from HBM too, so theirs are upper bounds.
 
 e2e: the same frames through the C ABI (ocean_update) with every output map
 copied back to pinned host memory inside the timed region; the per-frame input
@@ -16,13 +29,13 @@ is the time value (a by-value argument).  The headline e2e pipelines the
 frames (two device output sets, the copies on their own stream, so frame i+1
 computes while frame i's 29 MB cross the host link; no L2 flush, the link
 sets the rate); `serial_value` runs compute and copies one after the other,
-L2 flushed before each frame as in the device-timed loop.
+L2 flushed before each frame.
 
 --impl reference: the reference's algorithm (FP32 C++ port of the shader
 passes, oracle/ocean_oracle.c port_*) on the host cores, same config/metric.
 
 Multi-GPU (torchrun): tiles do not exchange data, so every rank advances its
-own tile (replicas, weak scaling); time = max over ranks.
+own tiles (replicas, weak scaling); time = max over ranks.
 """
 from __future__ import annotations
 
@@ -54,12 +67,16 @@ def row_kernel(N):
 
 
 def c2_params(N):
-    import ocean_gb300 as og
-    import numpy as np
-    a = math.radians(30.0)
-    f = lambda v: float(np.float32(v))
-    return og.Params(N=N, L=2000.0, amplitude=2.0, wind_speed=30.0, wind_dir_x=f(math.cos(a)),
-                     wind_dir_y=f(math.sin(a)), choppiness=f(1.3), suppression=f(0.1), gravity=f(9.81))
+    import workloads
+    return workloads.plain(N)
+
+
+def bench_config(N, world):
+    """The workload description both arms print (identical dicts)."""
+    return {"workload": f"plain tile N={N}, L=2000 m, A=2, V=30 m/s @30deg, lambda=1.3, l=0.1, "
+                        f"frames at dt=1/60 s", "N": N, "fields": 3,
+            "l2": "inputs larger than L2: frames rotate over 8 tiles (8 x 97 MB), no flush in the timed region",
+            "parallelism": f"replicas x{world}"}
 
 
 def peak_hbm():
@@ -203,6 +220,9 @@ def parity_check(N, gpu_frame, t):
     return {k: float(f"{v:.3g}") for k, v in errs.items()}
 
 
+RING = 8   # tiles the timed frames rotate over (8 x 97 MB: every frame's inputs come from HBM)
+
+
 def run_gpu(args, world, rank, local):
     import numpy as np
     import torch
@@ -215,9 +235,17 @@ def run_gpu(args, world, rank, local):
     stream = torch.cuda.Stream(device=dev)
     N = args.size
     p = c2_params(N)
-    oc = og.Ocean(p, seed=1 + rank)
-    dx, dy, dz = (torch.empty((N, N), dtype=torch.float32, device=dev) for _ in range(3))
-    nj = torch.empty((N, N, 4), dtype=torch.float32, device=dev)
+
+    def maps():
+        return (torch.empty((N, N), dtype=torch.float32, device=dev), torch.empty((N, N), dtype=torch.float32, device=dev),
+                torch.empty((N, N), dtype=torch.float32, device=dev),
+                torch.empty((N, N, 4), dtype=torch.float32, device=dev))
+
+    # R tiles of the same workload (same spectrum, own state and outputs)
+    ring = [og.Ocean(p, seed=1 + rank) for _ in range(RING)]
+    ring_out = [maps() for _ in range(RING)]
+    oc = ring[0]
+    dx, dy, dz, nj = ring_out[0]
     fl_w = torch.empty(128 << 20, dtype=torch.float32, device=dev)   # 512 MiB
     fl_r = torch.ones(128 << 20, dtype=torch.float32, device=dev)
     fl_sink = torch.empty((), dtype=torch.float32, device=dev)
@@ -226,36 +254,65 @@ def run_gpu(args, world, rank, local):
         fl_w.zero_()
         torch.sum(fl_r, dim=(0,), out=fl_sink)
 
+    def prime():
+        """Keep the device busy while the host queues the timed launches."""
+        torch.cuda._sleep(4_000_000)   # ~2 ms at 2 GHz
+
+    K = args.steps
     launches = 0
     with torch.cuda.stream(stream):
-        for i in range(args.warmup):
+        for i in range(max(args.warmup, RING)):
             flush()
-            oc.update(i / 60.0, dx, dy, dz, nj, stream=stream)
+            ring[i % RING].update(i / 60.0, *ring_out[i % RING], stream=stream)
         torch.cuda.synchronize()
-        K = args.steps
-        ev = [[torch.cuda.Event(enable_timing=True) for _ in range(2)] for _ in range(K)]
         with ClockSampler(local) as clk:
             if world > 1:
                 torch.distributed.barrier()
             torch.cuda.synchronize()
             wall0 = time.perf_counter()
-            # headline: whole frames through ocean_update (three kernels chained
-            # by programmatic dependent launch)
+            # headline: K whole frames through ocean_update back to back (three
+            # kernels each, chained by programmatic dependent launch), rotating
+            # over the R tiles
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            prime()
+            e0.record(stream)
             for i in range(K):
-                flush()
-                t = (args.warmup + i) / 60.0
-                ev[i][0].record(stream)
-                oc.update(t, dx, dy, dz, nj, stream=stream)
-                ev[i][1].record(stream)
+                j = i % RING
+                ring[j].update((args.warmup + i) / 60.0, *ring_out[j], stream=stream)
                 launches += 3
+            e1.record(stream)
             torch.cuda.synchronize()
             wall = time.perf_counter() - wall0
             if world > 1:
                 torch.distributed.barrier()
-            frame_ms = [ev[i][0].elapsed_time(ev[i][1]) for i in range(K)]
-            total_s = barrier_max(world, sum(frame_ms) / 1e3)
-            # per-kernel durations: the three stages launched one by one with
-            # events between them (no launch overlap)
+            total_s = barrier_max(world, e0.elapsed_time(e1) / 1e3)
+
+            # isolated frames: L2 flushed before each, each bracketed by events
+            ev = [[torch.cuda.Event(enable_timing=True) for _ in range(2)] for _ in range(K)]
+            for i in range(K):
+                flush()
+                ev[i][0].record(stream)
+                oc.update((args.warmup + i) / 60.0, dx, dy, dz, nj, stream=stream)
+                ev[i][1].record(stream)
+            torch.cuda.synchronize()
+            iso_s = barrier_max(world, sum(ev[i][0].elapsed_time(ev[i][1]) for i in range(K)) / 1e3)
+
+            # per-stage average launch durations: each stage K times back to
+            # back over the R tiles between two events
+            kernel_ms = {}
+            for name, call in ((row_kernel(N), lambda j, t: ring[j].update_rows(t, stream=stream)),
+                               ("k_col_fft", lambda j, t: ring[j].update_columns(stream=stream)),
+                               ("k_col_out", lambda j, t: ring[j].update_outputs(*ring_out[j], stream=stream))):
+                a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                prime()
+                a.record(stream)
+                for i in range(K):
+                    call(i % RING, (args.warmup + i) / 60.0)
+                b.record(stream)
+                torch.cuda.synchronize()
+                kernel_ms[name] = a.elapsed_time(b) / K
+            # the same stages with events between them inside flushed frames
+            # (each then also pays its own launch)
             kv = [[torch.cuda.Event(enable_timing=True) for _ in range(4)] for _ in range(K)]
             for i in range(K):
                 flush()
@@ -268,8 +325,8 @@ def run_gpu(args, world, rank, local):
                 oc.update_outputs(dx, dy, dz, nj, stream=stream)
                 kv[i][3].record(stream)
             torch.cuda.synchronize()
-            kernel_ms = {name: sum(kv[i][j].elapsed_time(kv[i][j + 1]) for i in range(K)) / K
-                         for j, name in enumerate((row_kernel(N), "k_col_fft", "k_col_out"))}
+            kernel_iso_ms = {name: sum(kv[i][j].elapsed_time(kv[i][j + 1]) for i in range(K)) / K
+                             for j, name in enumerate((row_kernel(N), "k_col_fft", "k_col_out"))}
 
             # e2e: C-ABI call + all outputs copied to pinned host memory, every frame.
             hdx, hdy, hdz = (torch.empty((N, N), dtype=torch.float32, pin_memory=True) for _ in range(3))
@@ -280,7 +337,6 @@ def run_gpu(args, world, rank, local):
                 for hsrc, hdst in ((dx, hdx), (dy, hdy), (dz, hdz), (nj, hnj)):
                     hdst.copy_(hsrc, non_blocking=True)
             torch.cuda.synchronize()
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             ee = []
             for i in range(E):
                 flush()
@@ -302,7 +358,7 @@ def run_gpu(args, world, rank, local):
             # compute stream inside the timed region, and the rate is set by the
             # host link (29 MB per frame) with the compute hidden under it.
             copy_stream = torch.cuda.Stream()
-            dsets = [(dx, dy, dz, nj), tuple(torch.empty_like(b) for b in (dx, dy, dz, nj))]
+            dsets = [(dx, dy, dz, nj), ring_out[1]]
             hsets = [(hdx, hdy, hdz, hnj),
                      tuple(torch.empty(b.shape, dtype=torch.float32, pin_memory=True) for b in (dx, dy, dz, nj))]
             computed = [torch.cuda.Event(), torch.cuda.Event()]
@@ -337,14 +393,18 @@ def run_gpu(args, world, rank, local):
         t_chk = 1000 / 60.0
         oc.update(t_chk, dx, dy, dz, nj, stream=stream)
         torch.cuda.synchronize()
+        oc.device_status()
         frame = {"dx": dx.cpu().numpy(), "dy": dy.cpu().numpy(), "dz": dz.cpu().numpy(), "nj": nj.cpu().numpy()}
         grid_stats = None if args.no_extra else bench_grid(torch, og, dev, stream, flush, (dx, dy, dz, nj))
-    oc.close()
+    for r in ring:
+        r.close()
+    del ring_out
 
     if rank != 0:
         return None
     value = world * K / total_s
     ms = 1e3 * total_s / K
+    iso_ms = 1e3 * iso_s / K
     dominant = max(kernel_ms, key=kernel_ms.get)
     dom_ms = kernel_ms[dominant]
     dom_bytes = KERNEL_BYTES[dominant] * N * N
@@ -352,19 +412,22 @@ def run_gpu(args, world, rank, local):
     achieved = dom_bytes / (dom_ms * 1e-3) / 1e9
     traffic = traffic_table().get(f"{dominant}@{N}")
     frame_gbs = BYTES_PER_TEXEL * N * N / (ms * 1e-3) / 1e9
+    iso_gbs = BYTES_PER_TEXEL * N * N / (iso_ms * 1e-3) / 1e9
     out = {
         "metric": METRIC, "value": round(value, 1), "unit": "frames/s", "n_gpus": world, "steps": K,
         "warmup": args.warmup, "ms_per_step": round(ms, 5), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded splitmix64 uniform noise, seed 1)",
-        "config": {"workload": f"plain tile N={N}, L=2000 m, A=2, V=30 m/s @30deg, lambda=1.3, l=0.1, "
-                               f"frames at dt=1/60 s", "N": N, "fields": 3,
-                   "l2": "flushed between frames (512 MiB write + 512 MiB read)", "parallelism": f"replicas x{world}"},
+        "config": bench_config(N, world),
         "kernel_ms": {k: round(v, 5) for k, v in kernel_ms.items()},
+        "kernel_ms_isolated": {k: round(v, 5) for k, v in kernel_iso_ms.items()},
         "roofline": {"bound": "hbm", "kernel": dominant, "achieved": round(achieved, 1), "peak": peak,
                      "unit": "GB/s", "frac": round(achieved / peak, 4), "peak_source": peak_kind,
                      "algorithmic_bytes_per_launch": dom_bytes, "traffic": traffic},
         "roofline_frame": {"bytes_per_frame": BYTES_PER_TEXEL * N * N, "achieved": round(frame_gbs, 1),
                            "frac": round(frame_gbs / peak, 4)},
+        "isolated": {"value": round(world * K / iso_s, 1), "unit": "frames/s", "ms_per_frame": round(iso_ms, 5),
+                     "frac": round(iso_gbs / peak, 4),
+                     "how": "one frame at a time, L2 flushed before each, CUDA events around each frame"},
         "e2e": {"value": round(world * E / e2e_s, 1), "unit": "frames/s", "h2d_bytes_per_step": 8,
                 "d2h_bytes_per_step": 28 * N * N,
                 "path": "ocean_update (C ABI) + D2H of dx, dy, dz, normal_j to pinned host buffers; "
@@ -386,21 +449,14 @@ def run_gpu(args, world, rank, local):
     return out
 
 
-def c4_params(og, A=3.0, V=22.0, theta_deg=50.0, lam=1.1):
-    import numpy as np
-    f = lambda v: float(np.float32(v))
-    a = math.radians(theta_deg)
-    return og.Params(N=512, L=1500.0, amplitude=A, wind_speed=V, wind_dir_x=f(math.cos(a)), wind_dir_y=f(math.sin(a)),
-                     choppiness=f(lam), suppression=f(0.1), gravity=f(9.81))
-
-
 def bench_adjoint(torch, og, dev, stream, reps=5):
     """Parameter-fit workload: N=512, T=32 frames at dt=0.1 s.  Forward = the
     32 frames into a (T, 3, N, N) buffer; backward = ocean_backward over the
     32 frames' upstream gradients (one call, no stored or recomputed frames)."""
+    import workloads
     N, T = 512, 32
     times = [0.1 * j for j in range(T)]
-    oc = og.Ocean(c4_params(og), seed=3)
+    oc = og.Ocean(workloads.fit_params(), seed=3)
     D = torch.empty((T, 3, N, N), device=dev)
     nj = torch.empty((N, N, 4), device=dev)
     G = torch.randn((3, T, N, N), device=dev)
@@ -426,77 +482,94 @@ def bench_adjoint(torch, og, dev, stream, reps=5):
             "gpu_launches_per_step": 3 * T + 2}
 
 
-def bench_adjoint_large(torch, og, dev, stream, n_sets=16, T=64, dt=0.05):
-    """Full-spectrum adjoint at N=2048: 16 parameter sets (L=3000, A~U(1,6),
-    V~U(10,35), theta~U(0,2pi), lambda~U(0.5,1.5), seeds 10..25), T=64 frames
-    at dt=0.05 s.  Per set: the 64 forward frames, then ocean_backward with
-    dL/dh0 for every mode (frames are not stored: the adjoint reads only h0).
-    Upstream gradients are seeded standard normals.  Reports frames/s of
-    both and the device memory the library holds per set (handle + adjoint
-    scratch)."""
-    import numpy as np
-    N = 2048
-    rng = np.random.default_rng(10)
+def bench_adjoint_large(torch, og, dev, stream, n_sets=16, chunk=16):
+    """Full-spectrum adjoint at N=2048 (workloads.adjoint_sets): per set, the
+    MSE over T=64 frames (dt=0.05 s) of the displacement maps against a target
+    sequence generated on the device from the 5 %-perturbed h0, and dL/dh0 for
+    every mode.
+
+    forward: per frame, the model frame and the target frame (two
+    ocean_update calls) and the squared residual summed on the device: the
+    loss.  backward: frames are recomputed from h0 (only h0 is kept) in chunks
+    of 16: model and target frames, residual * 2/M as the upstream gradient,
+    ocean_backward accumulating dL/dh0.  Device memory is taken from
+    cudaMemGetInfo at the peak of each phase, relative to before the set."""
+    import workloads as W
+    N, T, dt = W.ADJ_N, W.ADJ_T, W.ADJ_DT
     times = [dt * j for j in range(T)]
-    G = torch.randn((3, T, N, N), device=dev, generator=torch.Generator(device=dev).manual_seed(10))
-    dh0 = torch.empty((N, N, 4), device=dev)
-    outs = [torch.empty((N, N), device=dev) for _ in range(3)] + [torch.empty((N, N, 4), device=dev)]
-    fwd_ms, bwd_ms, mem = 0.0, 0.0, 0
-    f = lambda v: float(np.float32(v))
+    M = 3.0 * T * N * N
+    fwd_ms = bwd_ms = 0.0
+    fwd_mem = bwd_mem = 0
+    losses = []
     ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
     with torch.cuda.stream(stream):
-        for s in range(n_sets):
-            a = rng.uniform(0, 2 * math.pi)
-            p = og.Params(N=N, L=3000.0, amplitude=f(rng.uniform(1, 6)), wind_speed=f(rng.uniform(10, 35)),
-                          wind_dir_x=f(math.cos(a)), wind_dir_y=f(math.sin(a)), choppiness=f(rng.uniform(0.5, 1.5)),
-                          suppression=f(0.1), gravity=f(9.81))
+        for s, (p, seed) in enumerate(W.adjoint_sets(n_sets)):
             torch.cuda.synchronize()
             free0 = torch.cuda.mem_get_info()[0]
-            oc = og.Ocean(p, seed=10 + s)
-            oc.backward(times[:2], G[0, :2], G[1, :2], G[2, :2], dh0=dh0, stream=stream)   # allocates the scratch
+            model = og.Ocean(p, seed=seed)
+            target = og.Ocean(p, seed=seed)
+            h0 = torch.empty((N, N, 4), device=dev)
+            model.get_h0(h0, stream=stream)
+            gen = torch.Generator(device=dev).manual_seed(W.perturb_seed(s))
+            h0t = h0 * (1.0 + 0.05 * torch.randn(h0.shape, device=dev, generator=gen))
+            target.set_h0(h0t, stream=stream)
+            del h0, h0t
+            D = [torch.empty((N, N), device=dev) for _ in range(3)] + [torch.empty((N, N, 4), device=dev)]
+            Tg = [torch.empty((N, N), device=dev) for _ in range(3)] + [torch.empty((N, N, 4), device=dev)]
+            acc = torch.zeros((), dtype=torch.float64, device=dev)
             torch.cuda.synchronize()
-            mem = max(mem, free0 - torch.cuda.mem_get_info()[0])
             ev[0].record(stream)
             for t in times:
-                oc.update(t, *outs, stream=stream)
+                model.update(t, *D, stream=stream)
+                target.update(t, *Tg, stream=stream)
+                for f in range(3):
+                    acc += torch.sum(torch.square(D[f] - Tg[f]), dtype=torch.float64)
             ev[1].record(stream)
-            oc.backward(times, G[0], G[1], G[2], dh0=dh0, stream=stream)
+            torch.cuda.synchronize()
+            fwd_mem = max(fwd_mem, free0 - torch.cuda.mem_get_info()[0])
+            losses.append(acc.item() / M)
+            G = torch.empty((3, chunk, N, N), device=dev)
+            nj = torch.empty((N, N, 4), device=dev)
+            dh0 = torch.zeros((N, N, 4), device=dev)
+            model.backward(times[:1], G[0, :1], G[1, :1], G[2, :1], dh0=dh0, stream=stream)   # adjoint scratch
+            torch.cuda.synchronize()
+            ev[1].record(stream)
+            for c0 in range(0, T, chunk):
+                n = min(chunk, T - c0)
+                for j in range(n):
+                    model.update(times[c0 + j], G[0, j], G[1, j], G[2, j], nj, stream=stream)
+                    target.update(times[c0 + j], *Tg, stream=stream)
+                    for f in range(3):
+                        G[f, j].sub_(Tg[f]).mul_(2.0 / M)
+                model.backward(times[c0:c0 + n], G[0, :n], G[1, :n], G[2, :n], dh0=dh0, accumulate=c0 > 0,
+                               stream=stream)
             ev[2].record(stream)
             torch.cuda.synchronize()
+            bwd_mem = max(bwd_mem, free0 - torch.cuda.mem_get_info()[0])
             fwd_ms += ev[0].elapsed_time(ev[1])
             bwd_ms += ev[1].elapsed_time(ev[2])
-            oc.close()
-    del G
-    return {"workload": f"{n_sets} parameter sets, N={N}, T={T} frames at dt={dt} s, dL/dh0 per mode",
+            model.device_status()
+            model.close()
+            target.close()
+            del D, Tg, G, nj, dh0
+    return {"workload": f"{n_sets} parameter sets, N={N}, T={T} frames at dt={dt} s: MSE of the displacement maps "
+                        f"against the target of the 5%-perturbed h0 (generated on the device), dL/dh0 per mode",
             "forward_frames_per_s": round(n_sets * T / (fwd_ms * 1e-3), 1),
-            "backward_frames_per_s": round(n_sets * T / (bwd_ms * 1e-3), 1),
+            "forward_ms_per_set": round(fwd_ms / n_sets, 3),
+            "backward_ms_per_set": round(bwd_ms / n_sets, 3),
             "fwd_adj_over_fwd": round((fwd_ms + bwd_ms) / fwd_ms, 3),
-            "device_bytes_per_set": int(mem), "frames_stored": 0}
-
-
-def batched_tiles(og, n_tiles=64, seed=2):
-    """64 tiles: N uniform in {128..2048}, L~U(100,4000), A~U(0.5,8),
-    V~U(5,40), theta~U(0,2pi), lambda~U(0,2), own noise; numpy seed 2."""
-    import numpy as np
-    rng = np.random.default_rng(seed)
-    f = lambda v: float(np.float32(v))
-    tiles, seeds = [], []
-    for i in range(n_tiles):
-        N = int(rng.choice([128, 256, 512, 1024, 2048]))
-        th = rng.uniform(0, 2 * math.pi)
-        tiles.append(og.Params(N=N, L=f(rng.uniform(100, 4000)), amplitude=f(rng.uniform(0.5, 8)),
-                               wind_speed=f(rng.uniform(5, 40)), wind_dir_x=f(math.cos(th)), wind_dir_y=f(math.sin(th)),
-                               choppiness=f(rng.uniform(0, 2)), suppression=f(0.1), gravity=f(9.81)))
-        seeds.append(1000 + i)
-    return tiles, seeds, rng
+            "fwd_mem_bytes": int(fwd_mem), "bwd_mem_bytes": int(bwd_mem),
+            "loss_mean": float(f"{sum(losses) / len(losses):.6g}"), "frames_stored": 0,
+            "how": "forward = model + target frame and the squared residual per frame; backward = frames recomputed "
+                   "from h0 in chunks of 16 (model + target + residual) and ocean_backward (dL/dh0 accumulated)"}
 
 
 def bench_batched(torch, og, dev, stream, flush, S=8, reps=3):
     """Batched mixed-size launch vs looping the plain per-tile update over the
     same 64 tiles x 8 time samples (t ~ U(0, 600) s)."""
-    tiles, seeds, rng = batched_tiles(og)
+    import workloads
+    tiles, seeds, times = workloads.batched_tiles(samples=S)
     n = len(tiles)
-    times = rng.uniform(0, 600, size=n * S).tolist()
     outs = []
     bufs = []
     for p in tiles:
@@ -636,8 +709,7 @@ def run_reference(args, world, rank):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * total / args.steps, 3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded splitmix64 uniform noise, seed 1)",
-        "config": {"workload": f"plain tile N={N}, L=2000 m, A=2, V=30 m/s @30deg, lambda=1.3, l=0.1, "
-                               f"frames at dt=1/60 s", "N": N, "fields": 3},
+        "config": bench_config(N, world),
         "cpu_baseline": {"value": round(value, 3), "unit": "frames/s", "cores": cores, "kind": "port",
                          "sample": f"{args.steps} consecutive N={N} frames; FP32 port of the reference's GLSL passes "
                                    f"(the GL path itself is unavailable on this box)"},

@@ -31,9 +31,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
-#include <atomic>
-
 #include "fft_line.cuh"
+#include "launch_setup.cuh"
 #include "ocean_device.cuh"
 #include "ocean_internal.h"
 
@@ -298,12 +297,9 @@ template <int N>
 static cudaError_t adj_col_n(int T, const AdjColArgs& a, cudaStream_t s)
 {
     using CF = AdjColCfg<N>;
-    static std::atomic<bool> attr{false};   // set once; racing threads set the same value
-    if (!attr.load(std::memory_order_acquire)) {
-        cudaError_t e = cudaFuncSetAttribute(k_adj_col_pass<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)CF::SMEM);
-        if (e != cudaSuccess) return e;
-        attr.store(true, std::memory_order_release);
-    }
+    static PerDevice attr;
+    cudaError_t e = smem_setup(attr, k_adj_col_pass<N>, CF::SMEM);
+    if (e != cudaSuccess) return e;
     k_adj_col_pass<N><<<dim3(N / CF::C, T), CF::THREADS, CF::SMEM, s>>>(a);
     return cudaGetLastError();
 }
@@ -312,12 +308,9 @@ template <int N>
 static cudaError_t adj_row_n(const AdjRowArgs& a, cudaStream_t s)
 {
     using CF = AdjRowCfg<N>;
-    static std::atomic<bool> attr{false};   // set once; racing threads set the same value
-    if (!attr.load(std::memory_order_acquire)) {
-        cudaError_t e = cudaFuncSetAttribute(k_adj_row_pass<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)CF::SMEM);
-        if (e != cudaSuccess) return e;
-        attr.store(true, std::memory_order_release);
-    }
+    static PerDevice attr;
+    cudaError_t e = smem_setup(attr, k_adj_row_pass<N>, CF::SMEM);
+    if (e != cudaSuccess) return e;
     k_adj_row_pass<N><<<CF::GRID, CF::THREADS, CF::SMEM, s>>>(a);
     return cudaGetLastError();
 }

@@ -32,9 +32,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
-#include <atomic>
-
 #include "fft_line.cuh"
+#include "launch_setup.cuh"
 #include "ocean_device.cuh"
 #include "ocean_internal.h"
 #include "tma.cuh"
@@ -290,6 +289,10 @@ __global__ void __launch_bounds__(RowCfg<N, FROM_H0>::THREADS, RowCfg<N, FROM_H0
 
     const int tid = threadIdx.x;
     const int n_items = a.tiles * RC::ITEMS;
+    // Launched as a programmatic dependent of the stream's previous kernel
+    // (its launch overlaps that kernel's tail): nothing is read or written
+    // before that kernel has finished.
+    pdl_wait_prior();
     // Thread 0 starts every copy at once: the twiddle table rides on the first
     // stage's barrier (the first item waits for it before its transform).
     if (tid == 0) {
@@ -427,6 +430,7 @@ __global__ void __launch_bounds__(RowWsCfg<N, FROM_H0>::THREADS, RowWsCfg<N, FRO
     const int n_items = a.tiles * WC::ITEMS;
     const int nsmp    = MULTI ? a.S : 1;
     const int n_jobs  = (n_items - (int)blockIdx.x + (int)gridDim.x - 1) / (int)gridDim.x * nsmp;
+    pdl_wait_prior();   // as in k_row_pass: the previous kernel of the stream has finished
     if (tid == 0) {
         // issue order = need order: the first rows (prepass), the twiddles
         // (transforms), the next rows
@@ -843,58 +847,56 @@ cudaError_t launch_spec_combine(int N, int tiles, const float4* h0, int literal_
     return cudaGetLastError();
 }
 
+static cudaLaunchAttribute pdl_attr()
+{
+    cudaLaunchAttribute at;
+    at.id                                         = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at.val.programmaticStreamSerializationAllowed = 1;
+    return at;
+}
+
+// Launch `kernel`, as a programmatic dependent of the stream's previous kernel
+// when `pdl` (the kernel itself then waits for that kernel with
+// griddepcontrol.wait before touching memory).
+template <class Args>
+static cudaError_t launch_pdl(void (*kernel)(Args), dim3 grid, dim3 block, size_t smem, cudaStream_t s, bool pdl,
+                              const Args& a)
+{
+    cudaLaunchAttribute at[1] = {pdl_attr()};
+    cudaLaunchConfig_t  cfg   = {};
+    cfg.gridDim               = grid;
+    cfg.blockDim              = block;
+    cfg.dynamicSmemBytes      = smem;
+    cfg.stream                = s;
+    cfg.attrs                 = at;
+    cfg.numAttrs              = pdl ? 1 : 0;
+    return cudaLaunchKernelEx(&cfg, kernel, a);
+}
+
 template <int N, bool MULTI, bool FROM_H0>
 static cudaError_t row_pass_nm(const RowArgs& a, cudaStream_t s)
 {
     using RC = RowCfg<N, FROM_H0>;
-    // persistent grid (resident CTAs per SM x SMs), found on the first launch;
-    // threads racing here set the same attribute and store the same value
-    static std::atomic<int> cached{0};
-    int grid = cached.load(std::memory_order_acquire);
-    if (!grid) {
-        cudaError_t e = cudaFuncSetAttribute(k_row_pass<N, MULTI, FROM_H0>,
-                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)RC::SMEM);
-        if (e != cudaSuccess) return e;
-        int per_sm = 0, dev = 0, sms = 0;
-        if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_row_pass<N, MULTI, FROM_H0>, RC::THREADS,
-                                                                RC::SMEM)) != cudaSuccess)
-            return e;
-        if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
-        if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
-        if (per_sm < 1) return cudaErrorInvalidConfiguration;
-        grid = per_sm * sms;
-        cached.store(grid, std::memory_order_release);
-    }
+    static PerDevice cache;   // persistent grid per device, found on its first launch
+    int grid = 0;
+    cudaError_t e = persistent_setup(cache, k_row_pass<N, MULTI, FROM_H0>, RC::THREADS, RC::SMEM, &grid);
+    if (e != cudaSuccess) return e;
     const int items = a.tiles * RC::ITEMS;
-    k_row_pass<N, MULTI, FROM_H0><<<grid < items ? grid : items, RC::THREADS, RC::SMEM, s>>>(a);
-    return cudaGetLastError();
+    return launch_pdl(k_row_pass<N, MULTI, FROM_H0>, dim3(grid < items ? grid : items), dim3(RC::THREADS), RC::SMEM,
+                      s, true, a);
 }
 
 template <int N, bool MULTI, bool FROM_H0>
 static cudaError_t row_ws_nm(const RowArgs& a, cudaStream_t s)
 {
     using WC = RowWsCfg<N, FROM_H0>;
-    // resident CTAs per SM x SMs, found on the first launch; threads racing
-    // here set the same attribute and store the same value
-    static std::atomic<int> cached{0};
-    int grid = cached.load(std::memory_order_acquire);
-    if (!grid) {
-        cudaError_t e = cudaFuncSetAttribute(k_row_ws<N, MULTI, FROM_H0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)WC::SMEM);
-        if (e != cudaSuccess) return e;
-        int per_sm = 0, dev = 0, sms = 0;
-        if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_row_ws<N, MULTI, FROM_H0>, WC::THREADS,
-                                                                WC::SMEM)) != cudaSuccess)
-            return e;
-        if ((e = cudaGetDevice(&dev)) != cudaSuccess) return e;
-        if ((e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return e;
-        if (per_sm < 1) return cudaErrorInvalidConfiguration;
-        grid = per_sm * sms;
-        cached.store(grid, std::memory_order_release);
-    }
+    static PerDevice cache;   // persistent grid per device, found on its first launch
+    int grid = 0;
+    cudaError_t e = persistent_setup(cache, k_row_ws<N, MULTI, FROM_H0>, WC::THREADS, WC::SMEM, &grid);
+    if (e != cudaSuccess) return e;
     const int items = a.tiles * WC::ITEMS;
-    k_row_ws<N, MULTI, FROM_H0><<<grid < items ? grid : items, WC::THREADS, WC::SMEM, s>>>(a);
-    return cudaGetLastError();
+    return launch_pdl(k_row_ws<N, MULTI, FROM_H0>, dim3(grid < items ? grid : items), dim3(WC::THREADS), WC::SMEM, s,
+                      true, a);
 }
 
 template <int N>
@@ -914,24 +916,13 @@ static cudaError_t row_pass_n(const RowArgs& a, cudaStream_t s)
     }
 }
 
-static cudaLaunchAttribute pdl_attr()
-{
-    cudaLaunchAttribute at;
-    at.id                                         = cudaLaunchAttributeProgrammaticStreamSerialization;
-    at.val.programmaticStreamSerializationAllowed = 1;
-    return at;
-}
-
 template <int N>
 static cudaError_t col_fft_n(int units, const ColArgs& a, cudaStream_t s, bool pdl)
 {
     using CF = ColCfg<N>;
-    static std::atomic<bool> attr{false};   // set once; racing threads set the same value
-    if (!attr.load(std::memory_order_acquire)) {
-        cudaError_t e = cudaFuncSetAttribute(k_col_fft<N>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)CF::SMEM);
-        if (e != cudaSuccess) return e;
-        attr.store(true, std::memory_order_release);
-    }
+    static PerDevice attr;
+    cudaError_t e = smem_setup(attr, k_col_fft<N>, CF::SMEM);
+    if (e != cudaSuccess) return e;
     cudaLaunchAttribute at[1] = {pdl_attr()};
     cudaLaunchConfig_t  cfg   = {};
     cfg.gridDim               = dim3(CF::CTAS, units);

@@ -103,6 +103,16 @@ extern "C" int ocean_update_noalloc(const ocean_params* params, const float* h0_
 
     std::lock_guard<std::mutex> lock(g_mu);
     DeviceScratch&              d = g_dev[dev];
+    if (!d.ready || d.tw_N != N) {
+        // The set-up and a twiddle rebuild are recorded as done when they are
+        // enqueued; inside a stream capture they would only run when the graph
+        // is launched, and a later direct call would read a stale table.
+        cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+        if ((e = cudaStreamIsCapturing(s, &cs)) != cudaSuccess) return cuda_fail(e, "cudaStreamIsCapturing");
+        if (cs != cudaStreamCaptureStatusNone)
+            return fail(OCEAN_ERR_INVALID, "ocean_update_noalloc: the first call on a device, and the first call "
+                                           "after a change of N, must not be made inside a stream capture");
+    }
     if (!d.ready && (rc = setup(dev, d, s)) != OCEAN_OK) return rc;
     if (d.tw_N != N) {                 // the table holds another size's twiddles
         if (ocean::twiddle_len(N) > kStaticTwLen) return fail(OCEAN_ERR_UNSUPPORTED, "twiddle plan exceeds its static array");
@@ -145,5 +155,27 @@ extern "C" int ocean_update_noalloc(const ocean_params* params, const float* h0_
     ca.u0.pad_   = 0.0f;
     if ((e = ocean::launch_col_fft(N, 1, ca, s, true)) != cudaSuccess) return cuda_fail(e, "column transform launch");
     if ((e = ocean::launch_col_out(N, 1, ca, s, true)) != cudaSuccess) return cuda_fail(e, "output launch");
+    return OCEAN_OK;
+}
+
+extern "C" int ocean_noalloc_device_status(void* stream)
+{
+    int         dev = 0;
+    cudaError_t e   = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
+    if (dev < 0 || dev >= kMaxDevices) return fail(OCEAN_ERR_UNSUPPORTED, "device ordinal out of range");
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    unsigned*    status;
+    {
+        std::lock_guard<std::mutex> lock(g_mu);
+        if (!g_dev[dev].ready) return OCEAN_OK;   // no frame has run on this device
+        status = g_dev[dev].status;
+    }
+    unsigned h = 0;
+    if ((e = cudaMemcpyAsync(&h, status, sizeof(h), cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
+        (e = cudaMemsetAsync(status, 0, sizeof(unsigned), s)) != cudaSuccess ||
+        (e = cudaStreamSynchronize(s)) != cudaSuccess)
+        return cuda_fail(e, "noalloc device status");
+    if (h) return fail(OCEAN_ERR_TIMEOUT, "a kernel of ocean_update_noalloc gave up a bounded wait for its TMA copies");
     return OCEAN_OK;
 }

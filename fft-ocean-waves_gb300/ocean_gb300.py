@@ -37,7 +37,7 @@ EXPORTS = [
     "ocean_version", "ocean_backward", "ocean_device_status", "ocean_batch_create", "ocean_batch_update",
     "ocean_batch_device_status", "ocean_batch_destroy", "ocean_update_noalloc", "ocean_displace_grid",
     "ocean_grid_tess_levels", "ocean_shade_grid", "ocean_sky_envmap", "ocean_render_skybox",
-    "ocean_debug_fail_allocations",
+    "ocean_debug_fail_allocations", "ocean_noalloc_device_status",
 ]
 OCEAN_GRAD_ACCUMULATE = 1
 
@@ -127,6 +127,7 @@ def load() -> C.CDLL:
     L.ocean_batch_destroy.argtypes = [vp]
     L.ocean_batch_destroy.restype = None
     L.ocean_update_noalloc.argtypes = [P(ocean_params), vp, C.c_double, P(ocean_outputs), vp]
+    L.ocean_noalloc_device_status.argtypes = [vp]
     L.ocean_displace_grid.argtypes = [P(ocean_outputs), C.c_int32, P(ocean_grid_params), vp, vp]
     L.ocean_grid_tess_levels.argtypes = [P(ocean_grid_params), vp, vp]
     L.ocean_shade_grid.argtypes = [vp, C.c_int64, P(ocean_shade_params), vp, vp, vp]
@@ -197,6 +198,12 @@ def update_noalloc(params: Params, h0_dev, t: float, dx, dy, dz, normal_j, strea
     cp = params.c()
     o = ocean_outputs(_addr(dx), _addr(dy), _addr(dz), _addr(normal_j))
     check(load().ocean_update_noalloc(C.byref(cp), _addr(h0_dev), float(t), C.byref(o), _stream(stream)))
+
+
+def noalloc_device_status(stream=None) -> None:
+    """Raise OceanError (OCEAN_ERR_TIMEOUT) if a kernel of ocean_update_noalloc
+    on the current device gave up a bounded wait; clears the status."""
+    check(load().ocean_noalloc_device_status(_stream(stream)))
 
 
 class ocean_grid_params(C.Structure):

@@ -201,12 +201,22 @@ OCEAN_API void ocean_batch_destroy(ocean_batch_t* batch);
  * compiled into the library, sized for N <= 1024; every GPU that loads the
  * library holds them until the process exits.  N > 1024 is rejected with
  * OCEAN_ERR_INVALID.  The first call on a device resolves the arrays' addresses
- * (cudaGetSymbolAddress) and clears the status word: make that first call
- * before any stream capture.  Every call uses the same arrays, so calls whose
- * work overlaps on the GPU (other streams, other threads) race: serialise
- * them.  Calls no cudaMalloc/cudaFree.  No counterpart in the reference. */
+ * (cudaGetSymbolAddress) and clears the status word, and the first call after
+ * a change of N rebuilds the twiddle table: such a call made inside a stream
+ * capture is refused with OCEAN_ERR_INVALID (make it before the capture).
+ * Every call uses the same arrays, so calls whose work overlaps on the GPU
+ * (other streams, other threads) race: serialise them.  Calls no
+ * cudaMalloc/cudaFree.  No counterpart in the reference. */
 OCEAN_API int ocean_update_noalloc(const ocean_params* params, const float* h0_dev, double t,
                                    const ocean_outputs* out, void* stream);
+
+/* The device status of ocean_update_noalloc on the current device, as
+ * ocean_device_status reports a handle's: synchronises `stream`, returns
+ * OCEAN_ERR_TIMEOUT if a kernel of an earlier call gave up a bounded wait for
+ * its TMA copies (that frame's outputs are incomplete), else OCEAN_OK, and
+ * clears the status word.  OCEAN_OK when no call has run on the device.
+ * Allocates nothing.  No counterpart in the reference. */
+OCEAN_API int ocean_noalloc_device_status(void* stream);
 
 /* ---- Displaced grid (the consumer of the maps) ------------------------ */
 

@@ -16,7 +16,9 @@ import subprocess
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF = os.environ.get("OCEAN_REFERENCE_DIR", "/root/reference")
+# The reference checkout: OCEAN_REFERENCE_DIR, else a `reference` directory
+# beside this repository's root.
+REF = os.environ.get("OCEAN_REFERENCE_DIR") or os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference")
 OUT = os.path.join(HERE, "_ref")
 LIB = os.path.join(OUT, "libref_glsl.so")
 SHADERS = ["tilde_h0_k_cs.glsl", "tilde_h0_t_cs.glsl", "twiddle_factors_cs.glsl", "butterfly_cs.glsl",

@@ -194,6 +194,33 @@ static void orc_fft1(double* a, int n, int stride, int sg)
         }
 }
 
+/* In-place 2-D FFT of an N x N complex field [y][x][2]: every row, then every
+ * column.  Lines are independent and run in parallel; a column is gathered
+ * into a contiguous buffer, transformed with the same arithmetic as in place,
+ * and scattered back, so the result does not depend on the thread count. */
+static void orc_fft2(double* a, int N, int sg)
+{
+#pragma omp parallel
+    {
+        double* col = (double*)malloc(2 * (size_t)N * sizeof(double));
+#pragma omp for schedule(static)
+        for (int y = 0; y < N; ++y) orc_fft1(a + 2 * (size_t)y * N, N, 1, sg);
+#pragma omp for schedule(static)
+        for (int x = 0; x < N; ++x) {
+            for (int y = 0; y < N; ++y) {
+                col[2 * y]     = a[2 * ((size_t)y * N + x)];
+                col[2 * y + 1] = a[2 * ((size_t)y * N + x) + 1];
+            }
+            orc_fft1(col, N, 1, sg);
+            for (int y = 0; y < N; ++y) {
+                a[2 * ((size_t)y * N + x)]     = col[2 * y];
+                a[2 * ((size_t)y * N + x) + 1] = col[2 * y + 1];
+            }
+        }
+        free(col);
+    }
+}
+
 /* Re of the unnormalised 2-D inverse DFT (positive exponent) that the
  * butterfly passes compute (butterfly_cs.glsl:54-132), followed by the
  * (-1)^(x+y)/N^2 of inversion_cs.glsl:29-41.  spec_f: one field [y][x][2]. */
@@ -202,8 +229,7 @@ void orc_ifft2_real(int N, const double* spec_f, double* d)
     size_t  NN = (size_t)N * N;
     double* a  = (double*)malloc(2 * NN * sizeof(double));
     memcpy(a, spec_f, 2 * NN * sizeof(double));
-    for (int y = 0; y < N; ++y) orc_fft1(a + 2 * (size_t)y * N, N, 1, +1);
-    for (int x = 0; x < N; ++x) orc_fft1(a + 2 * (size_t)x, N, N, +1);
+    orc_fft2(a, N, +1);
     double inv = 1.0 / ((double)N * N);
     for (int y = 0; y < N; ++y)
         for (int x = 0; x < N; ++x) {
@@ -294,10 +320,10 @@ void orc_backward(const orc_params* p, const double* h0, const double* times, in
                     a[2 * i]     = gs[f] ? s * gs[f][i] : 0.0;
                     a[2 * i + 1] = 0.0;
                 }
-            for (int y = 0; y < N; ++y) orc_fft1(a + 2 * (size_t)y * N, N, 1, -1);
-            for (int x = 0; x < N; ++x) orc_fft1(a + 2 * (size_t)x, N, N, -1);
+            orc_fft2(a, N, -1);
         }
         double t = times[j];
+#pragma omp parallel for schedule(static) reduction(+ : dlam)
         for (int y = 0; y < N; ++y)
             for (int x = 0; x < N; ++x) {
                 size_t i  = (size_t)y * N + x;

@@ -47,3 +47,11 @@ def lib_params(d, literal_conj=False):
     return ocean_gb300.Params(N=d["N"], L=d["L"], amplitude=d["amplitude"], wind_speed=d["wind_speed"],
                               wind_dir_x=d["wind_x"], wind_dir_y=d["wind_y"], choppiness=d["choppiness"],
                               suppression=d["suppression"], gravity=f32(9.81), literal_conj=literal_conj)
+
+
+def oracle_from_lib(p):
+    """oracle.Params carrying exactly an ocean_gb300.Params' values."""
+    from oracle import oracle
+    return oracle.Params(N=p.N, L=p.L, amplitude=p.amplitude, wind_speed=p.wind_speed, wind_x=p.wind_dir_x,
+                         wind_y=p.wind_dir_y, choppiness=p.choppiness, suppression=p.suppression,
+                         gravity=p.gravity, literal_conj=p.literal_conj)

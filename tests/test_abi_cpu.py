@@ -169,17 +169,16 @@ def test_ctypes_structs_match_the_header(ocean_lib, tmp_path):
         assert size - (offs[last] + ctypes.sizeof(dict(cls._fields_)[last])) < 8, n
 
 
-def test_integration_snippet_structs_match_the_binding(ocean_lib):
-    """The ctypes structures a maintainer copies from INTEGRATION.md are the
-    binding's (same field names and types in the same order)."""
-    import ctypes
-    text = open(os.path.join(ROOT, "INTEGRATION.md")).read()
-    block = text.split("```python", 1)[1].split("```", 1)[0]
-    ns = {}
-    exec("\n".join(ln for ln in block.splitlines() if not ln.startswith(("lib", "h =", "p =", "assert", "outs"))),
-         {"C": ctypes, "ctypes": ctypes}, ns)
+def test_ctypes_stub_matches_the_binding(ocean_lib):
+    """The minimal ctypes binding a maintainer copies (ctypes_stub.py) has the
+    full binding's structures (same field names and types in the same order)
+    and loads the library's per-frame entry points."""
+    import ctypes_stub
     for n in ("ocean_params", "ocean_outputs"):
-        assert ns[n]._fields_ == getattr(ocean_lib, n)._fields_, n
+        assert getattr(ctypes_stub, n)._fields_ == getattr(ocean_lib, n)._fields_, n
+    lib = ctypes_stub.load(ocean_lib.LIB_PATH)
+    for name in ("ocean_create_seeded", "ocean_update", "ocean_destroy", "ocean_last_error"):
+        assert hasattr(lib, name)
 
 
 def _c_kind(t):

@@ -56,3 +56,53 @@ def test_noalloc_rejects_large_n(torch_cuda, ocean_lib):
     with pytest.raises(ocean_lib.OceanError) as e:
         ocean_lib.update_noalloc(lp, h0, 1.0, *_bufs(torch, N))
     assert e.value.code == ocean_lib.OCEAN_ERR_INVALID and "N <= 1024" in str(e.value)
+
+
+def test_noalloc_device_status_after_frames(torch_cuda, ocean_lib):
+    """ocean_noalloc_device_status reads (and clears) the status word of the
+    static path: OK after ordinary frames, and again on a second read."""
+    torch = torch_cuda
+    N = 256
+    d = P.c2(N)
+    lp = P.lib_params(d)
+    with ocean_lib.Ocean(lp, seed=d["seed"]) as oc:
+        h0 = torch.empty((N, N, 4), device=torch.device("cuda"))
+        oc.get_h0(h0)
+        for t in (0.5, 1.5):
+            ocean_lib.update_noalloc(lp, h0, t, *_bufs(torch, N))
+        ocean_lib.noalloc_device_status()
+        ocean_lib.noalloc_device_status()
+
+
+def test_noalloc_refuses_table_rebuild_inside_a_capture(torch_cuda, ocean_lib):
+    """The first call after a change of N rebuilds the static twiddle table;
+    inside a stream capture that would run only at graph launch, so the call
+    is refused (nothing is enqueued) and the same call outside the capture
+    then succeeds and matches ocean_update."""
+    torch = torch_cuda
+    dev = torch.device("cuda")
+    small, other = P.c2(32), P.c2(64)
+    lp32, lp64 = P.lib_params(small), P.lib_params(other)
+    h32 = torch.empty((32, 32, 4), device=dev)
+    h64 = torch.empty((64, 64, 4), device=dev)
+    with ocean_lib.Ocean(lp32, seed=1) as a, ocean_lib.Ocean(lp64, seed=1) as b:
+        a.get_h0(h32)
+        b.get_h0(h64)
+        ocean_lib.update_noalloc(lp32, h32, 1.0, *_bufs(torch, 32))   # the table now holds N = 32
+        torch.cuda.synchronize()
+        got, want = _bufs(torch, 64), _bufs(torch, 64)
+        s = torch.cuda.Stream()
+        g = torch.cuda.CUDAGraph()
+        x = torch.zeros(1, device=dev)
+        with torch.cuda.stream(s):
+            with torch.cuda.graph(g, stream=s, capture_error_mode="relaxed"):
+                x.add_(1.0)
+                with pytest.raises(ocean_lib.OceanError) as e:
+                    ocean_lib.update_noalloc(lp64, h64, 2.0, *got, stream=s)
+        assert e.value.code == ocean_lib.OCEAN_ERR_INVALID and "capture" in str(e.value)
+        ocean_lib.update_noalloc(lp64, h64, 2.0, *got)
+        b.update(2.0, *want)
+        torch.cuda.synchronize()
+        ocean_lib.noalloc_device_status()
+        for gg, w in zip(got, want):
+            assert rel_l2(gg.cpu().numpy(), w.cpu().numpy()) < TOL
