@@ -23,26 +23,48 @@ static cudaError_t smem_setup(PerDevice& cache, Kernel kernel, size_t smem)
     return (cudaError_t)rc;
 }
 
-// smem_setup, plus the persistent grid of `kernel` on the current device:
-// resident CTAs per SM (for `threads` threads and `smem` bytes) x SMs.
+// smem_setup, plus the occupancy of `kernel` on the current device: how many
+// of its CTAs (`threads` threads, `smem` bytes) fit on one SM.
 template <class Kernel>
-static cudaError_t persistent_setup(PerDevice& cache, Kernel kernel, int threads, size_t smem, int* grid)
+static cudaError_t persistent_setup(PerDevice& cache, Kernel kernel, int threads, size_t smem, int* per_sm)
 {
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
-    const int rc = cache.get(dev, grid, (int)cudaErrorInvalidDevice, [&](int* v) -> int {
+    const int rc = cache.get(dev, per_sm, (int)cudaErrorInvalidDevice, [&](int* v) -> int {
         cudaError_t e2 = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e2 != cudaSuccess) return (int)e2;
-        int per_sm = 0, sms = 0;
-        if ((e2 = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem)) != cudaSuccess)
+        int n = 0;
+        if ((e2 = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kernel, threads, smem)) != cudaSuccess)
             return (int)e2;
-        if ((e2 = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return (int)e2;
-        if (per_sm < 1) return (int)cudaErrorInvalidConfiguration;
-        *v = per_sm * sms;
+        if (n < 1) return (int)cudaErrorInvalidConfiguration;
+        *v = n;
         return 0;
     });
     return (cudaError_t)rc;
+}
+
+// The current device's SM count (once per device).
+static cudaError_t device_sms(int* sms)
+{
+    static PerDevice cache;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    const int rc = cache.get(dev, sms, (int)cudaErrorInvalidDevice, [&](int* v) -> int {
+        return (int)cudaDeviceGetAttribute(v, cudaDevAttrMultiProcessorCount, dev);
+    });
+    return (cudaError_t)rc;
+}
+
+// Persistent grid: CTAs per SM (the tuning's cap, 0 = as many as fit) x SMs.
+static cudaError_t persistent_grid(int per_sm, int cap, int* grid)
+{
+    int sms = 0;
+    cudaError_t e = device_sms(&sms);
+    if (e != cudaSuccess) return e;
+    *grid = (cap > 0 && cap < per_sm ? cap : per_sm) * sms;
+    return cudaSuccess;
 }
 
 }  // namespace ocean

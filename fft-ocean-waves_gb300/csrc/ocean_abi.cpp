@@ -162,7 +162,7 @@ struct ocean_s {
     float2*      adj    = nullptr;  // adjoint scratch: [frames][3][N/2+1][N]
     int          adj_frames = 0;
     double*      sums   = nullptr;  // adjoint parameter sums (4 doubles)
-    bool         pdl_next = false;  // set inside ocean_update: each stage directly follows the previous one
+    bool         spec_dirty = true; // the combined spectrum was rebuilt since the last row pass was launched
     double       K      = 0.0;      // sqrt(g/(2*pi*L))
     double       w_dc   = 0.0;      // sqrt(g*1e-5): the floored DC frequency
 
@@ -226,6 +226,7 @@ struct ocean_s {
     {
         cudaError_t e = ocean::launch_spec_combine(N, 1, h0, (p.flags & OCEAN_FLAG_LITERAL_CONJ) ? 1 : 0, spec, s);
         if (e != cudaSuccess) return cuda_fail(e, "spectrum combine launch");
+        spec_dirty = true;   // the next row pass must wait for it before reading
         return OCEAN_OK;
     }
 };
@@ -439,11 +440,16 @@ int ocean_update_rows(ocean_t* o, double t, void* stream)
     ra.fc0        = o->frame(t);
     ra.tiles      = 1;
     ra.S          = 1;
+    // the row pass overlaps the stream's previous kernel unless that may be
+    // the spectrum rebuild (ocean_set_h0 is stream-ordered) or the tuning
+    // says otherwise for this N
+    ra.wait_first = (o->spec_dirty || !ocean::tuning_for(o->N).row_overlap) ? 1 : 0;
     // NVTX ranges name the stages as the reference's GL debug groups do (main.cpp:623,644,665,689)
     nvtxRangePushA("ocean rows: evolution + horizontal FFT");
     cudaError_t e = ocean::launch_row_pass(o->N, ra, static_cast<cudaStream_t>(stream));
     nvtxRangePop();
     if (e != cudaSuccess) return cuda_fail(e, "row pass launch");
+    o->spec_dirty = false;
     return OCEAN_OK;
 }
 
@@ -480,7 +486,11 @@ int ocean_update_columns(ocean_t* o, void* stream)
     if (!o) return fail(OCEAN_ERR_INVALID, "ocean is NULL");
     const ocean_outputs none{};
     nvtxRangePushA("ocean columns: vertical FFT + inversion");
-    cudaError_t e = ocean::launch_col_fft(o->N, 1, col_args(o, none), static_cast<cudaStream_t>(stream), o->pdl_next);
+    // every stage is a programmatic dependent of the stream's previous kernel:
+    // its launch overlaps that kernel's tail, and it waits for that kernel
+    // (griddepcontrol.wait) before it reads or writes anything that kernel may
+    // touch
+    cudaError_t e = ocean::launch_col_fft(o->N, 1, col_args(o, none), static_cast<cudaStream_t>(stream), true);
     nvtxRangePop();
     if (e != cudaSuccess) return cuda_fail(e, "column transform launch");
     return OCEAN_OK;
@@ -493,7 +503,7 @@ int ocean_update_outputs(ocean_t* o, const ocean_outputs* out, void* stream)
     int rc = resolve_outputs(o, out, &res);
     if (rc) return rc;
     nvtxRangePushA("ocean outputs: normal map + Jacobian");
-    cudaError_t e = ocean::launch_col_out(o->N, 1, col_args(o, res), static_cast<cudaStream_t>(stream), o->pdl_next);
+    cudaError_t e = ocean::launch_col_out(o->N, 1, col_args(o, res), static_cast<cudaStream_t>(stream), true);
     nvtxRangePop();
     if (e != cudaSuccess) return cuda_fail(e, "output launch");
     return OCEAN_OK;
@@ -507,13 +517,8 @@ int ocean_update(ocean_t* o, double t, const ocean_outputs* out, void* stream)
     int rc = resolve_outputs(o, out, &res);
     if (rc) return rc;
     if ((rc = ocean_update_rows(o, t, stream)) != OCEAN_OK) return rc;
-    // each stage follows the previous one on the same stream: launched as
-    // programmatic dependents, their set-up overlaps the previous stage's tail
-    o->pdl_next = true;
-    rc = ocean_update_columns(o, stream);
-    if (rc == OCEAN_OK) rc = ocean_update_outputs(o, &res, stream);
-    o->pdl_next = false;
-    return rc;
+    if ((rc = ocean_update_columns(o, stream)) != OCEAN_OK) return rc;
+    return ocean_update_outputs(o, &res, stream);
 }
 
 int ocean_device_status(ocean_t* o, void* stream)

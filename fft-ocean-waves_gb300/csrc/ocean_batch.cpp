@@ -87,18 +87,17 @@ struct ocean_batch_s {
 
 namespace {
 
-// Scratch (intermediate + column-major maps) one wave of units may use: a
-// wave's three stages then run out of L2 (129 MB) instead of HBM.
-constexpr size_t kWaveBytes = 64ull << 20;
-
 size_t unit_scratch_bytes(int N) { return ocean::inter_len(N) * sizeof(float2) + ocean::tmap_len(N) * sizeof(float); }
 
 // Waves of a group: whole tiles (all samples) when a tile's samples fit the
-// budget, else runs of samples of one tile; units are tile-major, so a wave's
-// units are contiguous and share their tiles' spectra.
+// scratch budget of a wave (the tuning's wave_mib: small enough that a wave's
+// three stages run out of the 129 MB L2), else runs of samples of one tile;
+// units are tile-major, so a wave's units are contiguous and share their
+// tiles' spectra.
 void plan_waves(ocean_batch_s::Group& g, int S)
 {
-    const size_t U = std::max<size_t>(1, kWaveBytes / unit_scratch_bytes(g.N));
+    const size_t budget = (size_t)ocean::tuning_for(g.N).wave_mib << 20;
+    const size_t U = std::max<size_t>(1, budget / unit_scratch_bytes(g.N));
     const size_t T = g.tiles.size();
     if (U >= (size_t)S) {
         g.wave_tiles = (int)std::min(T, U / S);
@@ -113,7 +112,7 @@ void plan_waves(ocean_batch_s::Group& g, int S)
 }
 
 // One wave: `tiles` tiles from slot t0, samples s0 .. s0+smp-1 of each.
-cudaError_t launch_wave(ocean_batch_s* b, const ocean_batch_s::Group& g, int t0, int tiles, int s0, int smp)
+cudaError_t launch_wave(ocean_batch_s* b, const ocean_batch_s::Group& g, int t0, int tiles, int s0, int smp, bool first)
 {
     const size_t u0 = g.first_unit + (size_t)t0 * b->S + s0;   // first unit (batch order)
     ocean::RowArgs ra;
@@ -126,6 +125,10 @@ cudaError_t launch_wave(ocean_batch_s* b, const ocean_batch_s::Group& g, int t0,
     ra.fc0    = ocean::FrameConsts{};
     ra.tiles  = tiles;
     ra.S      = smp;
+    // the first wave follows the H2D copy of the constants it reads; later
+    // waves follow a k_col_out, whose intermediate they may overwrite once it
+    // has started (see k_row_ws)
+    ra.wait_first = (first || !ocean::tuning_for(g.N).row_overlap) ? 1 : 0;
     cudaError_t e = ocean::launch_row_pass(g.N, ra, b->cap);
     if (e != cudaSuccess) return e;
     ocean::ColArgs ca;
@@ -145,16 +148,17 @@ int capture(ocean_batch_s* b)
     if ((e = cudaStreamBeginCapture(b->cap, cudaStreamCaptureModeRelaxed)) != cudaSuccess)
         return cuda_fail(e, "batch graph capture");
     e = cudaMemcpyAsync(b->d_desc, b->h_desc, b->desc_bytes, cudaMemcpyHostToDevice, b->cap);
+    bool first = true;
     for (size_t gi = 0; gi < b->groups.size() && e == cudaSuccess; ++gi) {
         const ocean_batch_s::Group& g = b->groups[gi];
         const int T = (int)g.tiles.size();
         if (g.wave_smp == 0) {
-            for (int t0 = 0; t0 < T && e == cudaSuccess; t0 += g.wave_tiles)
-                e = launch_wave(b, g, t0, std::min(g.wave_tiles, T - t0), 0, b->S);
+            for (int t0 = 0; t0 < T && e == cudaSuccess; t0 += g.wave_tiles, first = false)
+                e = launch_wave(b, g, t0, std::min(g.wave_tiles, T - t0), 0, b->S, first);
         } else {
             for (int t = 0; t < T && e == cudaSuccess; ++t)
-                for (int s0 = 0; s0 < b->S && e == cudaSuccess; s0 += g.wave_smp)
-                    e = launch_wave(b, g, t, 1, s0, std::min(g.wave_smp, b->S - s0));
+                for (int s0 = 0; s0 < b->S && e == cudaSuccess; s0 += g.wave_smp, first = false)
+                    e = launch_wave(b, g, t, 1, s0, std::min(g.wave_smp, b->S - s0), first);
         }
     }
     cudaGraph_t graph = nullptr;

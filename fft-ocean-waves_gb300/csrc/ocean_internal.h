@@ -61,7 +61,8 @@ __host__ __device__ constexpr size_t spec_len(int N) { return (size_t)N * N + 2 
 // or, with spec NULL (single unit only), it is formed on the fly from h0
 // ([N][N] float4 (h0k, h0m)).  The intermediate of unit u starts at
 // inter + u*inter_len(N).  Per-unit constants come from `fcs` (device,
-// [tiles*S]) or, for a single unit, from `fc0`.
+// [tiles*S]) or, for a single unit, from `fc0`.  The row pass is launched as
+// a programmatic dependent of the stream's previous kernel (wait_first).
 struct RowArgs {
     const float2*      spec;
     const float4*      h0;
@@ -71,6 +72,10 @@ struct RowArgs {
     const FrameConsts* fcs;
     FrameConsts        fc0;
     int                tiles, S;
+    // 1: wait for the stream's previous kernel before reading anything (it
+    // may have written the spectrum, h0 or the twiddle plans); 0: the row pass
+    // may overlap that kernel and waits for it only at its end.
+    int                wait_first;
 };
 
 // Column side of a frame: k_col_fft (column transforms, intermediate ->
@@ -114,6 +119,16 @@ struct AdjRowArgs {
     float         wV;    // 2V/(g Lw^3); dV weight is wV/|k|^2
     FrameConsts   fc[kMaxChunkFrames];
 };
+
+// Launch configuration of size N (ocean_tuning of include/ocean.h): the
+// compiled-in table (tuning_table.inc, written by tune.py) unless
+// ocean_set_tuning replaced it.
+struct Tuning {
+    int row_overlap;       // the row pass overlaps the stream's previous kernel
+    int row_ctas_per_sm;   // persistent row-pass CTAs per SM, 0 = as many as fit
+    int wave_mib;          // batch wave scratch budget, MiB
+};
+Tuning tuning_for(int N);
 
 cudaError_t launch_adj_col(int N, int T, const AdjColArgs& a, cudaStream_t s);
 cudaError_t launch_adj_row(int N, const AdjRowArgs& a, cudaStream_t s);

@@ -275,7 +275,7 @@ __device__ __forceinline__ void row_position(const RowArgs& a, const float2* row
 // loop, which the compiler would otherwise hoist into registers.  FROM_H0: the
 // ring holds h0 rows and G, D are formed on the fly (ocean_update_noalloc).
 template <int N, bool MULTI, bool FROM_H0>
-__global__ void __launch_bounds__(RowCfg<N, FROM_H0>::THREADS, RowCfg<N, FROM_H0>::MINB) k_row_pass(RowArgs a)
+__device__ __forceinline__ void row_pass_body(const RowArgs& a)
 {
     using RC = RowCfg<N, FROM_H0>;
     using L  = typename RC::L;
@@ -289,10 +289,6 @@ __global__ void __launch_bounds__(RowCfg<N, FROM_H0>::THREADS, RowCfg<N, FROM_H0
 
     const int tid = threadIdx.x;
     const int n_items = a.tiles * RC::ITEMS;
-    // Launched as a programmatic dependent of the stream's previous kernel
-    // (its launch overlaps that kernel's tail): nothing is read or written
-    // before that kernel has finished.
-    pdl_wait_prior();
     // Thread 0 starts every copy at once: the twiddle table rides on the first
     // stage's barrier (the first item waits for it before its transform).
     if (tid == 0) {
@@ -372,6 +368,23 @@ __global__ void __launch_bounds__(RowCfg<N, FROM_H0>::THREADS, RowCfg<N, FROM_H0
     }
 }
 
+// The row pass is launched as a programmatic dependent of the stream's
+// previous kernel, so that it can run while that kernel (normally the previous
+// frame's output stage) is still writing.  It reads only the spectrum and the
+// twiddle plans and writes only the intermediate, none of which that kernel
+// touches once it has passed its own griddepcontrol.wait; so it waits for that
+// kernel only at its end -- the grid completes, and the kernels that depend on
+// it start, only after the previous kernel has completed, which keeps stream
+// order for everything downstream.  wait_first: wait before reading too (the
+// spectrum or h0 was just written by the previous kernel).
+template <int N, bool MULTI, bool FROM_H0>
+__global__ void __launch_bounds__(RowCfg<N, FROM_H0>::THREADS, RowCfg<N, FROM_H0>::MINB) k_row_pass(RowArgs a)
+{
+    if (a.wait_first) pdl_wait_prior();
+    row_pass_body<N, MULTI, FROM_H0>(a);
+    pdl_wait_prior();
+}
+
 // ---------------------------------------------------------------------------
 // Warp-specialised row pass (lines of whole warps, N >= 512).  The three
 // line FFTs of a job (row pair x time sample) run on 3*G "transform" threads
@@ -414,7 +427,7 @@ __device__ __forceinline__ void named_arrive(int id, int count)
 }
 
 template <int N, bool MULTI, bool FROM_H0>
-__global__ void __launch_bounds__(RowWsCfg<N, FROM_H0>::THREADS, RowWsCfg<N, FROM_H0>::MINB) k_row_ws(RowArgs a)
+__device__ __forceinline__ void row_ws_body(const RowArgs& a)
 {
     using WC = RowWsCfg<N, FROM_H0>;
     using L  = typename WC::L;
@@ -430,7 +443,6 @@ __global__ void __launch_bounds__(RowWsCfg<N, FROM_H0>::THREADS, RowWsCfg<N, FRO
     const int n_items = a.tiles * WC::ITEMS;
     const int nsmp    = MULTI ? a.S : 1;
     const int n_jobs  = (n_items - (int)blockIdx.x + (int)gridDim.x - 1) / (int)gridDim.x * nsmp;
-    pdl_wait_prior();   // as in k_row_pass: the previous kernel of the stream has finished
     if (tid == 0) {
         // issue order = need order: the first rows (prepass), the twiddles
         // (transforms), the next rows
@@ -557,6 +569,16 @@ __global__ void __launch_bounds__(RowWsCfg<N, FROM_H0>::THREADS, RowWsCfg<N, FRO
     }
 }
 
+// Launched as k_row_pass is (see there): waits for the stream's previous
+// kernel at its end, or first with wait_first.
+template <int N, bool MULTI, bool FROM_H0>
+__global__ void __launch_bounds__(RowWsCfg<N, FROM_H0>::THREADS, RowWsCfg<N, FROM_H0>::MINB) k_row_ws(RowArgs a)
+{
+    if (a.wait_first) pdl_wait_prior();
+    row_ws_body<N, MULTI, FROM_H0>(a);
+    pdl_wait_prior();
+}
+
 // ---------------------------------------------------------------------------
 // Column transforms.
 // ---------------------------------------------------------------------------
@@ -631,6 +653,15 @@ __global__ void __launch_bounds__(ColCfg<N>::THREADS) k_col_fft(const __grid_con
         __syncthreads();
         return;
     }
+    // The staged blocks are this CTA's alone and the next write of the
+    // intermediate is the next frame's row pass: drop their L2 lines instead
+    // of letting them be written back to HBM.
+    {
+        const float2* in = a.inter + (size_t)unit * inter_len(N);
+#pragma unroll
+        for (int f = 0; f < 3; ++f)
+            l2_discard(in + inter_index(N, f, 2 * pair0, 0), CF::FIELD_BYTES, tid, CF::THREADS);
+    }
 
     // Line li of pair pl holds field f = li % 3 (0: Dx, 1: Dy, 2: Dz) of both
     // columns, f(x0) + i*f(x0+1): the row-transformed spectra are Hermitian in
@@ -695,6 +726,10 @@ __global__ void __launch_bounds__(kOutTh, 5) k_col_out(const __grid_constant__ C
     const float*   tm = a.tmap + (size_t)unit * tmap_len(N);
     const int      tid = threadIdx.x;
     pdl_wait_prior();                                        // the column transforms have finished
+    // The next frame's row pass may start now: the intermediate it writes has
+    // been read (k_col_fft has completed), and it completes only after this
+    // grid has.
+    pdl_launch_dependents();
 
     // Stage the maps: each of the 3 x 34 columns (field f, x = x0-1 .. x0+32)
     // is rows y0 .. y0+31 (eight aligned 16-byte pieces) plus the halo rows
@@ -788,10 +823,12 @@ __global__ void __launch_bounds__(kOutTh, 5) k_col_out(const __grid_constant__ C
         // only rounding at the scale of 1 is the final add
         const float  dJ = (dxx * dzz - dxz * dzx) - dxx - dzz;
         const size_t o  = o0 + (size_t)k * N;
-        odx[o] = Xc[k + 1];
-        ody[o] = C1[k + 1];
-        odz[o] = Zc[k + 1];
-        onj[o] = make_float4(nx * rn, rn, nz * rn, 1.0f + dJ);
+        // streaming stores (evict first): the maps leave L2 before the
+        // frame's scratch does
+        __stcs(odx + o, Xc[k + 1]);
+        __stcs(ody + o, C1[k + 1]);
+        __stcs(odz + o, Zc[k + 1]);
+        __stcs(onj + o, make_float4(nx * rn, rn, nz * rn, 1.0f + dJ));
     }
 }
 
@@ -877,10 +914,11 @@ template <int N, bool MULTI, bool FROM_H0>
 static cudaError_t row_pass_nm(const RowArgs& a, cudaStream_t s)
 {
     using RC = RowCfg<N, FROM_H0>;
-    static PerDevice cache;   // persistent grid per device, found on its first launch
-    int grid = 0;
-    cudaError_t e = persistent_setup(cache, k_row_pass<N, MULTI, FROM_H0>, RC::THREADS, RC::SMEM, &grid);
-    if (e != cudaSuccess) return e;
+    static PerDevice cache;   // resident CTAs per SM on each device, found on its first launch
+    int per_sm = 0, grid = 0;
+    cudaError_t e = persistent_setup(cache, k_row_pass<N, MULTI, FROM_H0>, RC::THREADS, RC::SMEM, &per_sm);
+    if (e != cudaSuccess || (e = persistent_grid(per_sm, tuning_for(N).row_ctas_per_sm, &grid)) != cudaSuccess)
+        return e;
     const int items = a.tiles * RC::ITEMS;
     return launch_pdl(k_row_pass<N, MULTI, FROM_H0>, dim3(grid < items ? grid : items), dim3(RC::THREADS), RC::SMEM,
                       s, true, a);
@@ -890,10 +928,11 @@ template <int N, bool MULTI, bool FROM_H0>
 static cudaError_t row_ws_nm(const RowArgs& a, cudaStream_t s)
 {
     using WC = RowWsCfg<N, FROM_H0>;
-    static PerDevice cache;   // persistent grid per device, found on its first launch
-    int grid = 0;
-    cudaError_t e = persistent_setup(cache, k_row_ws<N, MULTI, FROM_H0>, WC::THREADS, WC::SMEM, &grid);
-    if (e != cudaSuccess) return e;
+    static PerDevice cache;   // resident CTAs per SM on each device, found on its first launch
+    int per_sm = 0, grid = 0;
+    cudaError_t e = persistent_setup(cache, k_row_ws<N, MULTI, FROM_H0>, WC::THREADS, WC::SMEM, &per_sm);
+    if (e != cudaSuccess || (e = persistent_grid(per_sm, tuning_for(N).row_ctas_per_sm, &grid)) != cudaSuccess)
+        return e;
     const int items = a.tiles * WC::ITEMS;
     return launch_pdl(k_row_ws<N, MULTI, FROM_H0>, dim3(grid < items ? grid : items), dim3(WC::THREADS), WC::SMEM, s,
                       true, a);

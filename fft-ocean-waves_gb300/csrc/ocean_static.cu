@@ -138,6 +138,7 @@ extern "C" int ocean_update_noalloc(const ocean_params* params, const float* h0_
     ra.fc0.literal_conj = (params->flags & OCEAN_FLAG_LITERAL_CONJ) ? 1 : 0;
     ra.tiles           = 1;
     ra.S               = 1;
+    ra.wait_first      = 1;                  // the caller's h0 (and a new twiddle table) come from earlier kernels
     if ((e = ocean::launch_row_pass(N, ra, s)) != cudaSuccess) return cuda_fail(e, "row pass launch");
     ocean::ColArgs ca;
     ca.inter     = d.inter;

@@ -1,0 +1,94 @@
+// ocean_tuning.cpp -- the per-N launch configuration (ocean_get_tuning /
+// ocean_set_tuning of include/ocean.h).  The defaults are the compiled-in
+// table tuning_table.inc, which tune.py writes from GB300 measurements; a
+// process may replace an entry at run time (the tuner does, to measure the
+// candidates).  No counterpart in the reference, which has one fixed dispatch
+// shape per shader.
+#include <atomic>
+#include <string>
+
+#include "ocean.h"
+#include "ocean_host.h"
+#include "ocean_internal.h"
+
+namespace {
+
+struct Entry {
+    int N, row_overlap, row_ctas_per_sm, wave_mib;
+};
+constexpr Entry kTable[] = {
+#include "tuning_table.inc"
+};
+constexpr int kSizes = (int)(sizeof(kTable) / sizeof(kTable[0]));
+static_assert(kSizes == 7, "one entry per supported N (32 .. 2048)");
+
+struct Live {
+    std::atomic<int> row_overlap, row_ctas_per_sm, wave_mib;
+};
+
+// The live table, filled from kTable on first use (thread-safe static
+// initialisation).
+Live* live()
+{
+    static Live* table = [] {
+        static Live l[kSizes];
+        for (int i = 0; i < kSizes; ++i) {
+            l[i].row_overlap.store(kTable[i].row_overlap);
+            l[i].row_ctas_per_sm.store(kTable[i].row_ctas_per_sm);
+            l[i].wave_mib.store(kTable[i].wave_mib);
+        }
+        return l;
+    }();
+    return table;
+}
+
+int slot(int N)
+{
+    for (int i = 0; i < kSizes; ++i)
+        if (kTable[i].N == N) return i;
+    return -1;
+}
+
+}  // namespace
+
+namespace ocean {
+
+Tuning tuning_for(int N)
+{
+    const int i = slot(N);
+    if (i < 0) return Tuning{0, 0, 64};
+    const Live& l = live()[i];
+    return Tuning{l.row_overlap.load(std::memory_order_relaxed), l.row_ctas_per_sm.load(std::memory_order_relaxed),
+                  l.wave_mib.load(std::memory_order_relaxed)};
+}
+
+}  // namespace ocean
+
+using namespace ocean::host;
+
+extern "C" int ocean_get_tuning(int32_t N, ocean_tuning* out)
+{
+    if (!out) return fail(OCEAN_ERR_INVALID, "out is NULL");
+    if (slot(N) < 0) return fail(OCEAN_ERR_INVALID, "no tuning entry for N = " + std::to_string(N));
+    const ocean::Tuning t = ocean::tuning_for(N);
+    out->row_overlap      = t.row_overlap;
+    out->row_ctas_per_sm  = t.row_ctas_per_sm;
+    out->wave_mib         = t.wave_mib;
+    out->reserved         = 0;
+    return OCEAN_OK;
+}
+
+extern "C" int ocean_set_tuning(int32_t N, const ocean_tuning* cfg)
+{
+    if (!cfg) return fail(OCEAN_ERR_INVALID, "cfg is NULL");
+    const int i = slot(N);
+    if (i < 0) return fail(OCEAN_ERR_INVALID, "no tuning entry for N = " + std::to_string(N));
+    if ((cfg->row_overlap != 0 && cfg->row_overlap != 1) || cfg->row_ctas_per_sm < 0 || cfg->row_ctas_per_sm > 32 ||
+        cfg->wave_mib < 1 || cfg->wave_mib > 4096 || cfg->reserved != 0)
+        return fail(OCEAN_ERR_INVALID, "tuning values out of range");
+    Live& l = live()[i];
+    l.row_overlap.store(cfg->row_overlap);
+    l.row_ctas_per_sm.store(cfg->row_ctas_per_sm);
+    l.wave_mib.store(cfg->wave_mib);
+    return OCEAN_OK;
+}

@@ -100,6 +100,19 @@ __device__ __forceinline__ bool block_wait(uint64_t* bar, uint32_t parity, int* 
     return *flag_smem != 0;
 }
 
+// Drop the L2 lines that lie wholly inside [p, p + bytes), spread over
+// `nthreads` threads (discard.global.L2: the lines' contents become undefined
+// and are never written back to HBM).  Only for scratch that the calling block
+// has consumed and that no other block reads before it is written again; the
+// partial lines at either end may hold another block's data and are kept.
+__device__ __forceinline__ void l2_discard(const void* p, size_t bytes, int tid, int nthreads)
+{
+    const uintptr_t b = reinterpret_cast<uintptr_t>(p);
+    const uintptr_t e = (b + bytes) & ~uintptr_t(127);
+    for (uintptr_t q = ((b + 127) & ~uintptr_t(127)) + (uintptr_t)tid * 128; q < e; q += (uintptr_t)nthreads * 128)
+        asm volatile("discard.global.L2 [%0], 128;" ::"l"(q) : "memory");
+}
+
 // Programmatic dependent launch: let the next kernel in the stream start its
 // prologue / wait for the previous kernel's results.
 __device__ __forceinline__ void pdl_launch_dependents()

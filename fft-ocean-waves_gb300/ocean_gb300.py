@@ -37,7 +37,7 @@ EXPORTS = [
     "ocean_version", "ocean_backward", "ocean_device_status", "ocean_batch_create", "ocean_batch_update",
     "ocean_batch_device_status", "ocean_batch_destroy", "ocean_update_noalloc", "ocean_displace_grid",
     "ocean_grid_tess_levels", "ocean_shade_grid", "ocean_sky_envmap", "ocean_render_skybox",
-    "ocean_debug_fail_allocations", "ocean_noalloc_device_status",
+    "ocean_debug_fail_allocations", "ocean_noalloc_device_status", "ocean_get_tuning", "ocean_set_tuning",
 ]
 OCEAN_GRAD_ACCUMULATE = 1
 
@@ -56,6 +56,11 @@ class ocean_params(C.Structure):
 
 class ocean_outputs(C.Structure):
     _fields_ = [("dx", C.c_void_p), ("dy", C.c_void_p), ("dz", C.c_void_p), ("normal_j", C.c_void_p)]
+
+
+class ocean_tuning(C.Structure):
+    _fields_ = [("row_overlap", C.c_int32), ("row_ctas_per_sm", C.c_int32), ("wave_mib", C.c_int32),
+                ("reserved", C.c_int32)]
 
 
 class ocean_grads(C.Structure):
@@ -128,6 +133,8 @@ def load() -> C.CDLL:
     L.ocean_batch_destroy.restype = None
     L.ocean_update_noalloc.argtypes = [P(ocean_params), vp, C.c_double, P(ocean_outputs), vp]
     L.ocean_noalloc_device_status.argtypes = [vp]
+    L.ocean_get_tuning.argtypes = [C.c_int32, P(ocean_tuning)]
+    L.ocean_set_tuning.argtypes = [C.c_int32, P(ocean_tuning)]
     L.ocean_displace_grid.argtypes = [P(ocean_outputs), C.c_int32, P(ocean_grid_params), vp, vp]
     L.ocean_grid_tess_levels.argtypes = [P(ocean_grid_params), vp, vp]
     L.ocean_shade_grid.argtypes = [vp, C.c_int64, P(ocean_shade_params), vp, vp, vp]
@@ -198,6 +205,26 @@ def update_noalloc(params: Params, h0_dev, t: float, dx, dy, dz, normal_j, strea
     cp = params.c()
     o = ocean_outputs(_addr(dx), _addr(dy), _addr(dz), _addr(normal_j))
     check(load().ocean_update_noalloc(C.byref(cp), _addr(h0_dev), float(t), C.byref(o), _stream(stream)))
+
+
+def get_tuning(N: int) -> dict:
+    """The launch configuration of size N (ocean_get_tuning)."""
+    t = ocean_tuning()
+    check(load().ocean_get_tuning(int(N), C.byref(t)))
+    return {"row_overlap": t.row_overlap, "row_ctas_per_sm": t.row_ctas_per_sm, "wave_mib": t.wave_mib}
+
+
+def set_tuning(N: int, row_overlap=None, row_ctas_per_sm=None, wave_mib=None) -> dict:
+    """Replace fields of size N's launch configuration for this process
+    (ocean_set_tuning); returns the previous configuration."""
+    old = get_tuning(N)
+    new = dict(old)
+    for k, v in (("row_overlap", row_overlap), ("row_ctas_per_sm", row_ctas_per_sm), ("wave_mib", wave_mib)):
+        if v is not None:
+            new[k] = int(v)
+    t = ocean_tuning(new["row_overlap"], new["row_ctas_per_sm"], new["wave_mib"], 0)
+    check(load().ocean_set_tuning(int(N), C.byref(t)))
+    return old
 
 
 def noalloc_device_status(stream=None) -> None:

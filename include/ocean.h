@@ -353,6 +353,25 @@ typedef struct ocean_grads {
 OCEAN_API int ocean_backward(ocean_t* ocean, const double* times, int32_t T, const float* g_dx, const float* g_dy,
                              const float* g_dz, uint32_t flags, ocean_grads* grads, void* stream);
 
+/* ---- Launch configuration per N ---------------------------------------- */
+
+/* How the kernels of size N are launched.  The defaults are a table compiled
+ * into the library (written by the project's tuner from GB300 measurements);
+ * ocean_set_tuning replaces the entry of one N for the rest of the process
+ * (all handles; a batch reads wave_mib when it is created).  No counterpart in
+ * the reference, which dispatches every shader in one fixed shape. */
+typedef struct ocean_tuning {
+    int32_t row_overlap;      /* 1: a frame's row pass starts while the stream's previous kernel (the previous
+                                 frame's output stage) still runs, and waits for it only at its end; 0: it waits
+                                 before starting.  Stream order is kept either way.                            */
+    int32_t row_ctas_per_sm;  /* persistent row-pass CTAs per SM, 0 = as many as fit                            */
+    int32_t wave_mib;         /* batches: scratch (intermediate + column maps) of one wave of units, MiB        */
+    int32_t reserved;         /* 0                                                                               */
+} ocean_tuning;
+
+OCEAN_API int ocean_get_tuning(int32_t N, ocean_tuning* out);
+OCEAN_API int ocean_set_tuning(int32_t N, const ocean_tuning* cfg);
+
 OCEAN_API const char* ocean_last_error(void);
 OCEAN_API int ocean_version(void);
 

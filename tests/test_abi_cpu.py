@@ -117,7 +117,7 @@ def test_header_is_c99_and_links(ocean_lib, tmp_path):
 
 
 STRUCTS = ["ocean_params", "ocean_outputs", "ocean_grads", "ocean_grid_params", "ocean_shade_params",
-           "ocean_sky_params"]
+           "ocean_sky_params", "ocean_tuning"]
 
 
 def _c_layout(tmp_path, structs):
@@ -246,3 +246,22 @@ def test_grid_parameter_validation_before_any_device_call(ocean_lib):
     rc = lib.ocean_grid_tess_levels(C.byref(ocean_lib.grid_params(2, 1.0e30)), None, None)
     assert rc == ocean_lib.OCEAN_ERR_INVALID
     assert "texcoord_scale" in lib.ocean_last_error().decode()
+
+
+def test_tuning_table_round_trip(ocean_lib):
+    """ocean_get_tuning / ocean_set_tuning: one entry per supported N, values
+    replaced for the process and restored, out-of-range values and sizes
+    refused.  Host-only (no device call)."""
+    for N in (32, 64, 128, 256, 512, 1024, 2048):
+        t = ocean_lib.get_tuning(N)
+        assert t["row_overlap"] in (0, 1) and t["row_ctas_per_sm"] >= 0 and t["wave_mib"] >= 1
+    old = ocean_lib.set_tuning(512, row_overlap=0, row_ctas_per_sm=1, wave_mib=32)
+    assert ocean_lib.get_tuning(512) == {"row_overlap": 0, "row_ctas_per_sm": 1, "wave_mib": 32}
+    ocean_lib.set_tuning(512, **old)
+    assert ocean_lib.get_tuning(512) == old
+    for bad in (dict(row_overlap=2), dict(row_ctas_per_sm=-1), dict(wave_mib=0)):
+        with pytest.raises(ocean_lib.OceanError):
+            ocean_lib.set_tuning(512, **bad)
+    assert ocean_lib.get_tuning(512) == old
+    with pytest.raises(ocean_lib.OceanError):
+        ocean_lib.get_tuning(48)

@@ -93,11 +93,12 @@ def test_per_device_cache(tmp_path):
 
 
 def test_launchers_use_the_per_device_cache():
-    """No launcher keeps a process-wide set-up flag: every cudaFuncSetAttribute
-    of a kernel goes through launch_setup.cuh's per-device helpers."""
+    """No launcher sets a kernel attribute or queries occupancy on its own:
+    both go through launch_setup.cuh's per-device helpers."""
     for name in os.listdir(CSRC):
         if not name.endswith((".cu", ".cpp")):
             continue
         src = open(os.path.join(CSRC, name)).read()
-        assert "std::atomic<bool>" not in src, name
         assert "cudaFuncSetAttribute" not in src, name
+        assert "cudaOccupancyMaxActiveBlocksPerMultiprocessor" not in src, name
+    assert "PerDevice" in open(os.path.join(CSRC, "launch_setup.cuh")).read()
