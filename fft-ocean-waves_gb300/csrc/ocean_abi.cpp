@@ -462,6 +462,7 @@ static ocean::ColArgs col_args(const ocean_s* o, const ocean_outputs& out)
     ca.tw     = o->tw;
     ca.units  = nullptr;
     ca.u0     = o->col_unit(out);
+    ca.trigger_next = ocean::tuning_for(o->N).row_overlap;
     return ca;
 }
 

@@ -138,6 +138,7 @@ cudaError_t launch_wave(ocean_batch_s* b, const ocean_batch_s::Group& g, int t0,
     ca.tw     = g.tw;
     ca.units  = b->d_units() + u0;
     ca.u0     = ocean::ColUnit{};
+    ca.trigger_next = ocean::tuning_for(g.N).row_overlap;
     if ((e = ocean::launch_col_fft(g.N, tiles * smp, ca, b->cap, true)) != cudaSuccess) return e;
     return ocean::launch_col_out(g.N, tiles * smp, ca, b->cap, true);
 }

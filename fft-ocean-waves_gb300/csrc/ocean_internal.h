@@ -89,6 +89,9 @@ struct ColArgs {
     const float2*  tw;
     const ColUnit* units;   // device [units], or NULL: u0 for the single unit
     ColUnit        u0;
+    // k_col_out lets the stream's next kernel (the next frame's row pass,
+    // when it overlaps) launch as soon as it has started
+    int            trigger_next;
 };
 
 // ---------------------------------------------------------------------------

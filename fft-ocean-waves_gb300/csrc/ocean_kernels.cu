@@ -728,8 +728,9 @@ __global__ void __launch_bounds__(kOutTh, 5) k_col_out(const __grid_constant__ C
     pdl_wait_prior();                                        // the column transforms have finished
     // The next frame's row pass may start now: the intermediate it writes has
     // been read (k_col_fft has completed), and it completes only after this
-    // grid has.
-    pdl_launch_dependents();
+    // grid has.  Only when that row pass overlaps (tuning): otherwise its CTAs
+    // would only wait on the SMs.
+    if (a.trigger_next) pdl_launch_dependents();
 
     // Stage the maps: each of the 3 x 34 columns (field f, x = x0-1 .. x0+32)
     // is rows y0 .. y0+31 (eight aligned 16-byte pieces) plus the halo rows
