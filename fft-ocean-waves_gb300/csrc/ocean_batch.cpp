@@ -39,6 +39,7 @@ struct ocean_batch_s {
         int              wave_tiles = 1; // tiles per wave (all S samples), or
         int              wave_smp   = 0; // if > 0: samples per wave of a single tile
         int              wave_units = 1; // units the scratch holds
+        bool             fused      = false;   // fused column kernel: no column maps
     };
     int                       n_tiles = 0, S = 0;
     std::vector<ocean_params> params;
@@ -87,7 +88,10 @@ struct ocean_batch_s {
 
 namespace {
 
-size_t unit_scratch_bytes(int N) { return ocean::inter_len(N) * sizeof(float2) + ocean::tmap_len(N) * sizeof(float); }
+size_t unit_scratch_bytes(int N, bool fused)
+{
+    return ocean::inter_len(N) * sizeof(float2) + (fused ? 0 : ocean::tmap_len(N) * sizeof(float));
+}
 
 // Waves of a group: whole tiles (all samples) when a tile's samples fit the
 // scratch budget of a wave (the tuning's wave_mib: small enough that a wave's
@@ -97,7 +101,7 @@ size_t unit_scratch_bytes(int N) { return ocean::inter_len(N) * sizeof(float2) +
 void plan_waves(ocean_batch_s::Group& g, int S)
 {
     const size_t budget = (size_t)ocean::tuning_for(g.N).wave_mib << 20;
-    const size_t U = std::max<size_t>(1, budget / unit_scratch_bytes(g.N));
+    const size_t U = std::max<size_t>(1, budget / unit_scratch_bytes(g.N, g.fused));
     const size_t T = g.tiles.size();
     if (U >= (size_t)S) {
         g.wave_tiles = (int)std::min(T, U / S);
@@ -139,6 +143,7 @@ cudaError_t launch_wave(ocean_batch_s* b, const ocean_batch_s::Group& g, int t0,
     ca.units  = b->d_units() + u0;
     ca.u0     = ocean::ColUnit{};
     ca.trigger_next = ocean::tuning_for(g.N).row_overlap;
+    if (g.fused) return ocean::launch_col_fused(g.N, tiles * smp, ca, b->cap, true);
     if ((e = ocean::launch_col_fft(g.N, tiles * smp, ca, b->cap, true)) != cudaSuccess) return e;
     return ocean::launch_col_out(g.N, tiles * smp, ca, b->cap, true);
 }
@@ -234,11 +239,12 @@ int ocean_batch_create(const ocean_params* params, const uint64_t* seeds, int32_
     }
     for (ocean_batch_s::Group& g : b->groups) {
         const size_t N = (size_t)g.N, NN = N * N, T = g.tiles.size();
+        g.fused = ocean::tuning_for(g.N).col_fused != 0;
         plan_waves(g, samples);
         const size_t W = (size_t)g.wave_units;
         if ((e = dev_alloc(&g.spec, T * ocean::spec_len(g.N) * sizeof(float2))) != cudaSuccess ||
             (e = dev_alloc(&g.inter, W * ocean::inter_len(g.N) * sizeof(float2))) != cudaSuccess ||
-            (e = dev_alloc(&g.tmap, W * ocean::tmap_len(g.N) * sizeof(float))) != cudaSuccess) {
+            (!g.fused && (e = dev_alloc(&g.tmap, W * ocean::tmap_len(g.N) * sizeof(float))) != cudaSuccess)) {
             cudaFree(d_noise);
             cudaFree(d_h0);
             delete b;

@@ -834,6 +834,163 @@ __global__ void __launch_bounds__(kOutTh, 5) k_col_out(const __grid_constant__ C
 }
 
 // ---------------------------------------------------------------------------
+// Fused column side (N = 512, 1024; the tuning's col_fused): the column
+// transforms with the inversion and lambda (k_col_fft) and the Sobel normal
+// and Jacobian (k_col_out) in one kernel, so that the column-major maps never
+// leave the SM (inversion_cs.glsl:25-43, normal_map_cs.glsl:24-54).
+//
+// A CTA owns P column pairs -- output columns x0 .. x0+2P-1 -- and also
+// transforms its two halo columns x0-1 and x0+2P, packed into one complex line
+// per field: any two real columns can share a transform, because the
+// row-transformed spectra are Hermitian in y.  One warp per line, lines read
+// straight from the L2-resident intermediate.  After the transforms the real
+// columns are staged in shared memory (the exchange buffers, reused) and the
+// CTA computes its 2P x N output texels from there, the lanes of a warp on 2P
+// adjacent columns of 32/(2P) rows.
+// ---------------------------------------------------------------------------
+template <int N, int P>
+struct FusedCfg {
+    using L = typename ColLineFor<N>::type;
+    static_assert(L::G == 32, "one warp per line");
+    static constexpr int LINES    = 3 * (P + 1);           // P pairs and one halo line per field
+    static constexpr int THREADS  = LINES * 32;
+    static constexpr int CTAS     = N / (2 * P);           // per unit
+    static constexpr int COLS     = 2 * P + 2;             // staged columns x0-1 .. x0+2P
+    // staged column pitch (floats): the 2P columns a warp reads are 32/(2P)
+    // banks apart, and its 32/(2P) rows fill the banks in between
+    static constexpr int CP       = N + 16 / P;
+    static constexpr int ETHREADS = 256;                   // epilogue threads
+    static constexpr int EROWS    = ETHREADS / (2 * P);    // rows per epilogue step
+    static constexpr size_t XBUF  = (size_t)LINES * L::NPAD;               // float2
+    static constexpr size_t EBUF  = ((size_t)3 * COLS * CP + 1) / 2;       // float2
+    static constexpr size_t WORK  = XBUF > EBUF ? XBUF : EBUF;
+    static constexpr int    TW    = TwPlan<L>::LEN;
+    static constexpr int    TW0   = TwPlan<typename LineFor<N>::type>::LEN;   // the row plan precedes it
+    static constexpr size_t SMEM  = sizeof(float2) * (TW + WORK) + 128;
+    static_assert(N % (2 * P) == 0 && N % EROWS == 0 && THREADS >= ETHREADS, "fused column layout");
+    static_assert((16 / P) * 2 * P == 32 && 32 % (2 * P) == 0, "conflict-free staging pitch");
+};
+
+template <int N, int P>
+__global__ void __launch_bounds__(FusedCfg<N, P>::THREADS, 2) k_col_fused(const __grid_constant__ ColArgs a)
+{
+    using FC = FusedCfg<N, P>;
+    using L  = typename FC::L;
+    extern __shared__ unsigned char smem_raw[];
+    float2* smem = align_smem(smem_raw);
+    float2* tw_s = smem;
+    float2* work = smem + FC::TW;                            // exchange buffers, then the staged columns
+    __shared__ __align__(8) uint64_t bar_tw;
+    __shared__ int wait_ok;
+    const int      tid  = threadIdx.x;
+    const int      unit = blockIdx.y;
+    const ColUnit* cu   = a.units ? a.units + unit : &a.u0;
+    if (tid == 0) {
+        mbar_init(&bar_tw, 1);
+        fence_mbar_init();
+        // the twiddle plan does not depend on the row pass: fetch it now
+        mbar_arrive_expect_tx(&bar_tw, FC::TW * sizeof(float2));
+        bulk_g2s(tw_s, a.tw + FC::TW0, FC::TW * sizeof(float2), &bar_tw);
+    }
+    pdl_wait_prior();                                        // the row pass has finished
+
+    // Line li: field f = li % 3 of columns ca (real part) and cb (imaginary
+    // part); kind < P: the pair x0 + 2 kind, x0 + 2 kind + 1; kind == P: the
+    // halo columns x0 - 1 and x0 + 2P (periodic).
+    const int li = tid >> 5, t = tid & 31;
+    const int f = li % 3, kind = li / 3;
+    const int x0 = 2 * P * (int)blockIdx.x;
+    const int ca = kind < P ? x0 + 2 * kind : (x0 - 1) & (N - 1);
+    const int cb = kind < P ? ca + 1 : (x0 + 2 * P) & (N - 1);
+    const float2* in = a.inter + (size_t)unit * inter_len(N);
+    constexpr int G = L::G;
+    float2 v[L::E];
+#pragma unroll
+    for (int r = 0; r < L::E; ++r) {
+        // register r holds row y = t + r*G: rows below N/2 directly, rows above
+        // as the conjugate of row N - y (as in k_col_fft)
+        const int  ys = r < L::R1 / 2 ? t + r * G : (r == L::R1 / 2 ? N / 2 - t : N - t - r * G);
+        const bool cj = r > L::R1 / 2 || (r == L::R1 / 2 && t != 0);
+        float2 p, q;
+        if (kind < P) {                                      // one 16-byte (ca, cb) pair of the row
+            const float4 z = __ldg(reinterpret_cast<const float4*>(in + inter_index(N, f, ca, ys)));
+            p = make_float2(z.x, z.y);
+            q = make_float2(z.z, z.w);
+        } else {
+            p = __ldg(in + inter_index(N, f, ca, ys));
+            q = __ldg(in + inter_index(N, f, cb, ys));
+        }
+        if (cj) { p.y = -p.y; q.y = -q.y; }
+        v[r] = make_float2(p.x - q.y, p.y + q.x);            // p + i*q
+    }
+    if (!block_wait(&bar_tw, 0, &wait_ok, a.status)) return;
+    line_fft<L, +1, true, false>(v, work + li * L::NPAD, tw_s, t, li);
+    __syncthreads();                                         // the exchange buffers are free
+    // Every warp of this CTA has used its loads of the intermediate (a CTA may
+    // count as triggered once any of its threads triggers, so not before this
+    // barrier): the next frame's row pass may start overwriting it; it
+    // completes only after this grid.
+    if (a.trigger_next) pdl_launch_dependents();
+
+    // Stage the real columns: (-1)^(x+y) * 1/(2N^2) (* lambda for Dx, Dz).
+    // y = pos(t, e) is t plus an even constant, so the sign is per thread.
+    float* const E = reinterpret_cast<float*>(work);
+    {
+        const float sc = f == 1 ? cu->scale : cu->scale * cu->lambda;
+        const float sA = ((ca + t) & 1) ? -sc : sc;
+        const float sB = ((cb + t) & 1) ? -sc : sc;
+        const int   cA = kind < P ? 1 + 2 * kind : 0;
+        const int   cB = kind < P ? 2 + 2 * kind : 2 * P + 1;
+        float* const ea = E + (size_t)(f * FC::COLS + cA) * FC::CP;
+        float* const eb = E + (size_t)(f * FC::COLS + cB) * FC::CP;
+        static_assert(L::G % 2 == 0 && LineOut<L>::NS % 2 == 0, "even output offsets");
+#pragma unroll
+        for (int e = 0; e < L::E; ++e) {
+            const int y = LineOut<L>::pos(t, e);
+            ea[y] = sA * v[e].x;
+            eb[y] = sB * v[e].y;
+        }
+    }
+    __syncthreads();
+    if (tid >= FC::ETHREADS) return;
+
+    // Epilogue: texel (x0 + c - 1, y), c = tid % 2P + 1, y = tid / 2P + EROWS * k.
+    const int    c     = tid % (2 * P) + 1;                  // staged column of the texel
+    const int    r0    = tid / (2 * P);
+    const float* EX    = E;                                  // Dx columns
+    const float* EY    = E + (size_t)FC::COLS * FC::CP;      // Dy
+    const float* EZ    = E + (size_t)2 * FC::COLS * FC::CP;  // Dz
+    const int    cm    = (c - 1) * FC::CP, c0 = c * FC::CP, cp = (c + 1) * FC::CP;
+    float* const  odx  = cu->dx;
+    float* const  ody  = cu->dy;
+    float* const  odz  = cu->dz;
+    float4* const onj  = cu->nj;
+    const float   inv2d = cu->inv2d;
+    const int     x    = x0 + c - 1;
+#pragma unroll 2
+    for (int y = r0; y < N; y += FC::EROWS) {
+        const int ym = (y - 1) & (N - 1), yq = (y + 1) & (N - 1);
+        // taps z0..z7 (normal_map_cs.glsl:37-44) around (x, y)
+        const float z0 = EY[cm + ym], z1 = EY[c0 + ym], z2 = EY[cp + ym];
+        const float z3 = EY[cm + y], z4 = EY[cp + y];
+        const float z5 = EY[cm + yq], z6 = EY[c0 + yq], z7 = EY[cp + yq];
+        const float nz = z0 + 2.0f * z1 + z2 - z5 - 2.0f * z6 - z7;
+        const float nx = z0 + 2.0f * z3 + z5 - z2 - 2.0f * z4 - z7;
+        const float rn = rsqrtf(nx * nx + 1.0f + nz * nz);
+        const float dxx = (EX[cp + y] - EX[cm + y]) * inv2d;
+        const float dxz = (EX[c0 + yq] - EX[c0 + ym]) * inv2d;
+        const float dzx = (EZ[cp + y] - EZ[cm + y]) * inv2d;
+        const float dzz = (EZ[c0 + yq] - EZ[c0 + ym]) * inv2d;
+        const float dJ  = (dxx * dzz - dxz * dzx) - dxx - dzz;
+        const size_t o  = (size_t)y * N + x;
+        __stcs(odx + o, EX[c0 + y]);
+        __stcs(ody + o, EY[c0 + y]);
+        __stcs(odz + o, EZ[c0 + y]);
+        __stcs(onj + o, make_float4(nx * rn, rn, nz * rn, 1.0f + dJ));
+    }
+}
+
+// ---------------------------------------------------------------------------
 // Twiddle plans: the row decomposition's, then the column decomposition's.
 // ---------------------------------------------------------------------------
 template <class C>
@@ -987,7 +1144,35 @@ static cudaError_t col_out_n(int units, const ColArgs& a, cudaStream_t s, bool p
     return cudaLaunchKernelEx(&cfg, k_col_out<N>, a);
 }
 
+// Column pairs per CTA of the fused column kernel.
+constexpr int kFusedPairs = 2;
+
+template <int N>
+static cudaError_t col_fused_n(int units, const ColArgs& a, cudaStream_t s, bool pdl)
+{
+    if constexpr (ColLineFor<N>::type::G == 32) {
+        using FC = FusedCfg<N, kFusedPairs>;
+        static PerDevice attr;
+        cudaError_t e = smem_setup(attr, k_col_fused<N, kFusedPairs>, FC::SMEM);
+        if (e != cudaSuccess) return e;
+        return launch_pdl(k_col_fused<N, kFusedPairs>, dim3(FC::CTAS, units), dim3(FC::THREADS), FC::SMEM, s, pdl, a);
+    } else {
+        return cudaErrorInvalidValue;                        // lines of more than one warp
+    }
+}
+
 #define OCEAN_FOR_EACH_N(M) M(32) M(64) M(128) M(256) M(512) M(1024) M(2048)
+
+bool col_fused_available(int N) { return N == 512 || N == 1024; }
+
+cudaError_t launch_col_fused(int N, int units, const ColArgs& a, cudaStream_t s, bool pdl)
+{
+    switch (N) {
+    case 512: return col_fused_n<512>(units, a, s, pdl);
+    case 1024: return col_fused_n<1024>(units, a, s, pdl);
+    default: return cudaErrorInvalidValue;
+    }
+}
 
 size_t twiddle_len(int N)
 {

@@ -11,6 +11,8 @@ candidate of
                               output stage, or waits for it first)
     row_ctas_per_sm  0 (as many as fit), 1, 2, 3, 4, 6, 8 (persistent row-pass
                               grid; caps above the occupancy limit give its grid)
+    col_fused        0 / 1   (N = 512, 1024: the column side as one fused
+                              kernel, or as column FFT + output kernels)
 and keeps the fastest (median of `reps` runs).  Then it times the 64-tile,
 8-sample batch (workloads.batched_tiles) for each wave budget and keeps the
 fastest.  It writes DIR/tuning_table.inc -- the table the library compiles
@@ -62,12 +64,15 @@ def tune_size(torch, og, workloads, N, reps, log):
         for i in range(2 * RING):                         # warm-up (first-launch set-up of every kernel)
             ring[i % RING].update(i / 60.0, *outs[i % RING], stream=stream)
         torch.cuda.synchronize()
-        for cap in (0, 1, 2, 3, 4, 6, 8):                 # 0: as many CTAs per SM as fit
-            for overlap in (0, 1):
-                og.set_tuning(N, row_overlap=overlap, row_ctas_per_sm=cap)
-                ms = time_frames(torch, og, ring, outs, stream, reps=reps)
-                results.append({"row_overlap": overlap, "row_ctas_per_sm": cap, "ms_per_frame": round(ms, 6)})
-                log(f"N={N} overlap={overlap} ctas/SM={cap}: {ms * 1e3:.2f} us")
+        fused_opts = (0, 1) if N in (512, 1024) else (0,)
+        for fused in fused_opts:                          # the fused column kernel exists for 512 and 1024
+            for cap in (0, 1, 2, 3, 4, 6, 8):             # 0: as many CTAs per SM as fit
+                for overlap in (0, 1):
+                    og.set_tuning(N, row_overlap=overlap, row_ctas_per_sm=cap, col_fused=fused)
+                    ms = time_frames(torch, og, ring, outs, stream, reps=reps)
+                    results.append({"row_overlap": overlap, "row_ctas_per_sm": cap, "col_fused": fused,
+                                    "ms_per_frame": round(ms, 6)})
+                    log(f"N={N} fused={fused} overlap={overlap} ctas/SM={cap}: {ms * 1e3:.2f} us")
     for oc in ring:
         oc.close()
     best = min(results, key=lambda r: r["ms_per_frame"])
@@ -133,6 +138,7 @@ def main():
         best, res = tune_size(torch, og, workloads, N, args.reps, log)
         table[N]["row_overlap"] = best["row_overlap"]
         table[N]["row_ctas_per_sm"] = best["row_ctas_per_sm"]
+        table[N]["col_fused"] = best.get("col_fused", 0)
         sweep["sizes"][N] = {"best": best, "all": res}
     for N in SIZES:                                       # the batch is timed with the winners
         og.set_tuning(N, **table[N])
@@ -142,12 +148,12 @@ def main():
             table[N]["wave_mib"] = best["wave_mib"]
         sweep["batch"] = {"best": best, "all": res}
     dev = torch.cuda.get_device_name()
-    lines = ["// Launch configuration per N: {N, row_overlap, row_ctas_per_sm, wave_mib}.",
+    lines = ["// Launch configuration per N: {N, row_overlap, row_ctas_per_sm, wave_mib, col_fused}.",
              "// Written by fft-ocean-waves_gb300/tune.py from measurements on a GB300",
              f"// ({dev}): steady back-to-back frames for the single-tile knobs (median of",
              f"// {args.reps} runs of 40 frames), the 64-tile batch for wave_mib."]
-    lines += [f"{{{N}, {table[N]['row_overlap']}, {table[N]['row_ctas_per_sm']}, {table[N]['wave_mib']}}},"
-              for N in SIZES]
+    lines += [f"{{{N}, {table[N]['row_overlap']}, {table[N]['row_ctas_per_sm']}, {table[N]['wave_mib']}, "
+              f"{table[N]['col_fused']}}}," for N in SIZES]
     with open(os.path.join(args.out, "tuning_table.inc"), "w") as fh:
         fh.write("\n".join(lines) + "\n")
     with open(os.path.join(args.out, "tuning_sweep.json"), "w") as fh:

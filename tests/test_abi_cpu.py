@@ -255,13 +255,18 @@ def test_tuning_table_round_trip(ocean_lib):
     for N in (32, 64, 128, 256, 512, 1024, 2048):
         t = ocean_lib.get_tuning(N)
         assert t["row_overlap"] in (0, 1) and t["row_ctas_per_sm"] >= 0 and t["wave_mib"] >= 1
-    old = ocean_lib.set_tuning(512, row_overlap=0, row_ctas_per_sm=1, wave_mib=32)
-    assert ocean_lib.get_tuning(512) == {"row_overlap": 0, "row_ctas_per_sm": 1, "wave_mib": 32}
+    old = ocean_lib.set_tuning(512, row_overlap=0, row_ctas_per_sm=1, wave_mib=32, col_fused=0)
+    assert ocean_lib.get_tuning(512) == {"row_overlap": 0, "row_ctas_per_sm": 1, "wave_mib": 32, "col_fused": 0}
     ocean_lib.set_tuning(512, **old)
     assert ocean_lib.get_tuning(512) == old
-    for bad in (dict(row_overlap=2), dict(row_ctas_per_sm=-1), dict(wave_mib=0)):
+    for bad in (dict(row_overlap=2), dict(row_ctas_per_sm=-1), dict(wave_mib=0), dict(col_fused=3)):
         with pytest.raises(ocean_lib.OceanError):
             ocean_lib.set_tuning(512, **bad)
     assert ocean_lib.get_tuning(512) == old
     with pytest.raises(ocean_lib.OceanError):
         ocean_lib.get_tuning(48)
+    # the fused column kernel exists for N = 512 and 1024 only: elsewhere the
+    # entry reads 0 whatever is set
+    old2 = ocean_lib.set_tuning(2048, col_fused=1)
+    assert ocean_lib.get_tuning(2048)["col_fused"] == 0
+    ocean_lib.set_tuning(2048, **old2)

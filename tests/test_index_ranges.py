@@ -185,3 +185,55 @@ def test_adjoint_row_pass_accumulators_and_dh0(N):
                 np.add.at(dh0, y * N + kx, 1)
         assert acc.max() <= 1
     assert np.all(dh0 == 1)
+
+
+@pytest.mark.parametrize("N", [512, 1024])
+def test_col_fused_loads_staging_and_stores(N):
+    """k_col_fused<N, 2>: every line load lies in the intermediate (16-byte
+    pair loads aligned), each CTA's staged columns (two halo, 2P own) are
+    written exactly once before the epilogue reads them, every staged read is
+    in range and every output texel is written exactly once over the grid."""
+    P = 2
+    G, E, R1, pos, t = line(N, COL_LINE_FOR[N])
+    assert G == 32
+    COLS, CP, EROWS = 2 * P + 2, N + 16 // P, 256 // (2 * P)
+    LINES = 3 * (P + 1)
+    NPAD = N + N // R1
+    assert 3 * COLS * CP <= 2 * LINES * NPAD                       # staging fits the exchange buffers
+    r = np.arange(E)[None, :]
+    ys = np.where(r < R1 // 2, t + r * G, np.where(r == R1 // 2, N // 2 - t, N - t - r * G))
+    out_hits = np.zeros(N * N, np.int64)
+    for b in range(N // (2 * P)):
+        x0 = 2 * P * b
+        stage = np.zeros(3 * COLS * CP, np.int64)
+        for li in range(LINES):
+            f, kind = li % 3, li // 3
+            ca = x0 + 2 * kind if kind < P else (x0 - 1) & (N - 1)
+            cb = ca + 1 if kind < P else (x0 + 2 * P) & (N - 1)
+            for c in (ca, cb):
+                idx = inter_index(N, f, c, ys)
+                assert idx.min() >= 0 and idx.max() < inter_len(N)
+            if kind < P:
+                assert np.all(inter_index(N, f, ca, ys) % 2 == 0)         # float4 (pair) loads
+            cA = 1 + 2 * kind if kind < P else 0
+            cB = 2 + 2 * kind if kind < P else 2 * P + 1
+            y = t + pos                                                   # LineOut positions
+            for cc, col in ((cA, ca), (cB, cb)):
+                assert col == (x0 - 1 + cc) & (N - 1)                     # staged column cc is x0 - 1 + cc
+                np.add.at(stage, ((f * COLS + cc) * CP + y).ravel(), 1)
+        used = np.zeros_like(stage, dtype=bool)
+        for f in range(3):
+            for cc in range(COLS):
+                used[(f * COLS + cc) * CP:(f * COLS + cc) * CP + N] = True
+        assert np.all(stage[used] == 1) and np.all(stage[~used] == 0)
+        # epilogue: threads 0..255, texel (x0 + c - 1, y), reads columns c-1..c+1, rows y-1..y+1
+        tid = np.arange(256)
+        c = tid % (2 * P) + 1
+        for y0 in range(0, N, EROWS):
+            y = tid // (2 * P) + y0
+            for dc in (-1, 0, 1):
+                for dy in (-1, 0, 1):
+                    rd = (c + dc) * CP + ((y + dy) & (N - 1))
+                    assert rd.min() >= 0 and rd.max() < COLS * CP and np.all(used[rd])
+            np.add.at(out_hits, y * N + x0 + c - 1, 1)
+    assert np.all(out_hits == 1)
