@@ -203,14 +203,17 @@ __device__ __forceinline__ void row_modes(const RowArgs& a, const float2* rA, co
         g[1] = rB[xm];
         g[2] = rA[xm];
         g[3] = rB[x];
+        // L2 loads (ld.global.cg), not the read-only path: the row pass runs
+        // as a programmatic dependent and may start before the kernel that
+        // last wrote the spectrum has finished
         const float2* sp = a.spec + (size_t)tile * spec_len(N);
         if (x == 0) {                                   // column 0: D(0, yp), D(0, yq)
-            d[0] = __ldg(sp + (size_t)N * N + yp);
-            d[1] = __ldg(sp + (size_t)N * N + yq);
+            d[0] = __ldcg(sp + (size_t)N * N + yp);
+            d[1] = __ldcg(sp + (size_t)N * N + yq);
         }
         if (yp == 0) {                                  // row 0: D(x, 0), D(xm, 0)
-            d[0] = __ldg(sp + (size_t)N * N + N + x);
-            d[1] = __ldg(sp + (size_t)N * N + N + xm);
+            d[0] = __ldcg(sp + (size_t)N * N + N + x);
+            d[1] = __ldcg(sp + (size_t)N * N + N + xm);
             d[2] = d[1];
             d[3] = d[0];
         }
@@ -911,14 +914,18 @@ __global__ void __launch_bounds__(FusedCfg<N, P>::THREADS, 2) k_col_fused(const 
         // as the conjugate of row N - y (as in k_col_fft)
         const int  ys = r < L::R1 / 2 ? t + r * G : (r == L::R1 / 2 ? N / 2 - t : N - t - r * G);
         const bool cj = r > L::R1 / 2 || (r == L::R1 / 2 && t != 0);
+        // L2 loads (ld.global.cg): the read-only (non-coherent) path may keep
+        // lines of the previous frame's intermediate, which the row pass
+        // rewrites while this grid is already resident (it is launched as a
+        // programmatic dependent)
         float2 p, q;
         if (kind < P) {                                      // one 16-byte (ca, cb) pair of the row
-            const float4 z = __ldg(reinterpret_cast<const float4*>(in + inter_index(N, f, ca, ys)));
+            const float4 z = __ldcg(reinterpret_cast<const float4*>(in + inter_index(N, f, ca, ys)));
             p = make_float2(z.x, z.y);
             q = make_float2(z.z, z.w);
         } else {
-            p = __ldg(in + inter_index(N, f, ca, ys));
-            q = __ldg(in + inter_index(N, f, cb, ys));
+            p = __ldcg(in + inter_index(N, f, ca, ys));
+            q = __ldcg(in + inter_index(N, f, cb, ys));
         }
         if (cj) { p.y = -p.y; q.y = -q.y; }
         v[r] = make_float2(p.x - q.y, p.y + q.x);            // p + i*q

@@ -331,3 +331,36 @@ def test_superposition_full_size(torch_cuda, ocean_lib):
         s = _frame(torch, oc, N, t)
     for k in range(3):
         assert _rel(torch, s[k], frames[0][k] + frames[1][k]) < 2 * TOL
+
+
+@pytest.mark.parametrize("N", [512, 1024])
+def test_fused_column_kernel_matches_two_kernels(torch_cuda, ocean_lib, N):
+    """The fused column kernel (the tuning's col_fused) against the column
+    FFT + output kernels on the same frames, launched back to back on one
+    handle: dx, dy, dz bit for bit (same arithmetic), normal_j within 1e-6
+    relative L2 (its halo columns come from a differently paired transform,
+    which rounds differently)."""
+    torch = torch_cuda
+    d = P.c2(N)
+    dev = torch.device("cuda")
+    times = [0.5 + 3.25 * k for k in range(6)]
+    outs = {}
+    saved = ocean_lib.get_tuning(N)
+    try:
+        for fused in (0, 1):
+            ocean_lib.set_tuning(N, col_fused=fused)
+            assert ocean_lib.get_tuning(N)["col_fused"] == fused
+            with ocean_lib.Ocean(P.lib_params(d), seed=d["seed"]) as oc:
+                sets = [[torch.empty((N, N), device=dev) for _ in range(3)] + [torch.empty((N, N, 4), device=dev)]
+                        for _ in times]
+                for t, o in zip(times, sets):
+                    oc.update(t, *o)
+                torch.cuda.synchronize()
+                oc.device_status()
+                outs[fused] = [[x.cpu().numpy() for x in o] for o in sets]
+    finally:
+        ocean_lib.set_tuning(N, **saved)
+    for a, b in zip(outs[0], outs[1]):
+        for k in range(3):
+            assert np.array_equal(a[k], b[k])
+        assert rel_l2(b[3], a[3]) < 1e-6
