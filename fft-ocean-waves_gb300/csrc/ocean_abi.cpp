@@ -518,10 +518,11 @@ int ocean_update(ocean_t* o, double t, const ocean_outputs* out, void* stream)
     int rc = resolve_outputs(o, out, &res);
     if (rc) return rc;
     if ((rc = ocean_update_rows(o, t, stream)) != OCEAN_OK) return rc;
-    if (ocean::tuning_for(o->N).col_fused) {
+    if (const int pairs = ocean::tuning_for(o->N).col_fused) {
         // both column stages in one kernel: the column maps stay on chip
         nvtxRangePushA("ocean columns + outputs: vertical FFT, inversion, normal map + Jacobian");
-        cudaError_t e = ocean::launch_col_fused(o->N, 1, col_args(o, res), static_cast<cudaStream_t>(stream), true);
+        cudaError_t e =
+            ocean::launch_col_fused(o->N, pairs, 1, col_args(o, res), static_cast<cudaStream_t>(stream), true);
         nvtxRangePop();
         if (e != cudaSuccess) return cuda_fail(e, "fused column launch");
         return OCEAN_OK;

@@ -39,7 +39,7 @@ struct ocean_batch_s {
         int              wave_tiles = 1; // tiles per wave (all S samples), or
         int              wave_smp   = 0; // if > 0: samples per wave of a single tile
         int              wave_units = 1; // units the scratch holds
-        bool             fused      = false;   // fused column kernel: no column maps
+        int              fused      = 0;   // fused column kernel's pairs per CTA (0: two kernels, column maps)
     };
     int                       n_tiles = 0, S = 0;
     std::vector<ocean_params> params;
@@ -88,7 +88,7 @@ struct ocean_batch_s {
 
 namespace {
 
-size_t unit_scratch_bytes(int N, bool fused)
+size_t unit_scratch_bytes(int N, int fused)
 {
     return ocean::inter_len(N) * sizeof(float2) + (fused ? 0 : ocean::tmap_len(N) * sizeof(float));
 }
@@ -143,7 +143,7 @@ cudaError_t launch_wave(ocean_batch_s* b, const ocean_batch_s::Group& g, int t0,
     ca.units  = b->d_units() + u0;
     ca.u0     = ocean::ColUnit{};
     ca.trigger_next = ocean::tuning_for(g.N).row_overlap;
-    if (g.fused) return ocean::launch_col_fused(g.N, tiles * smp, ca, b->cap, true);
+    if (g.fused) return ocean::launch_col_fused(g.N, g.fused, tiles * smp, ca, b->cap, true);
     if ((e = ocean::launch_col_fft(g.N, tiles * smp, ca, b->cap, true)) != cudaSuccess) return e;
     return ocean::launch_col_out(g.N, tiles * smp, ca, b->cap, true);
 }
@@ -239,7 +239,7 @@ int ocean_batch_create(const ocean_params* params, const uint64_t* seeds, int32_
     }
     for (ocean_batch_s::Group& g : b->groups) {
         const size_t N = (size_t)g.N, NN = N * N, T = g.tiles.size();
-        g.fused = ocean::tuning_for(g.N).col_fused != 0;
+        g.fused = ocean::tuning_for(g.N).col_fused;
         plan_waves(g, samples);
         const size_t W = (size_t)g.wave_units;
         if ((e = dev_alloc(&g.spec, T * ocean::spec_len(g.N) * sizeof(float2))) != cudaSuccess ||

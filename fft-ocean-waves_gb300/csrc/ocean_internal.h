@@ -130,7 +130,7 @@ struct Tuning {
     int row_overlap;       // the row pass overlaps the stream's previous kernel
     int row_ctas_per_sm;   // persistent row-pass CTAs per SM, 0 = as many as fit
     int wave_mib;          // batch wave scratch budget, MiB
-    int col_fused;         // frames use the fused column kernel (where available)
+    int col_fused;         // 0, or the fused column kernel's column pairs per CTA (2, 4)
 };
 Tuning tuning_for(int N);
 
@@ -149,9 +149,10 @@ cudaError_t launch_spec_combine(int N, int tiles, const float4* h0, int literal_
 // dependent of the preceding kernel in `s`.
 cudaError_t launch_col_fft(int N, int units, const ColArgs& a, cudaStream_t s, bool pdl);
 cudaError_t launch_col_out(int N, int units, const ColArgs& a, cudaStream_t s, bool pdl);
-// k_col_fused (both column stages in one kernel; no column maps): sizes whose
-// column lines are one warp (N = 512, 1024).
+// k_col_fused (both column stages in one kernel; no column maps) with `pairs`
+// (2 or 4) column pairs per CTA: sizes whose column lines are one warp
+// (N = 512, 1024).
 bool        col_fused_available(int N);
-cudaError_t launch_col_fused(int N, int units, const ColArgs& a, cudaStream_t s, bool pdl);
+cudaError_t launch_col_fused(int N, int pairs, int units, const ColArgs& a, cudaStream_t s, bool pdl);
 
 }  // namespace ocean

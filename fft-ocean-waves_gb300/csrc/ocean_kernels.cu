@@ -875,7 +875,7 @@ struct FusedCfg {
 };
 
 template <int N, int P>
-__global__ void __launch_bounds__(FusedCfg<N, P>::THREADS, 2) k_col_fused(const __grid_constant__ ColArgs a)
+__global__ void __launch_bounds__(FusedCfg<N, P>::THREADS, P == 2 ? 2 : 1) k_col_fused(const __grid_constant__ ColArgs a)
 {
     using FC = FusedCfg<N, P>;
     using L  = typename FC::L;
@@ -1151,32 +1151,36 @@ static cudaError_t col_out_n(int units, const ColArgs& a, cudaStream_t s, bool p
     return cudaLaunchKernelEx(&cfg, k_col_out<N>, a);
 }
 
-// Column pairs per CTA of the fused column kernel.
-constexpr int kFusedPairs = 2;
+// The fused column kernel with P column pairs per CTA.
+template <int N, int P>
+static cudaError_t col_fused_np(int units, const ColArgs& a, cudaStream_t s, bool pdl)
+{
+    using FC = FusedCfg<N, P>;
+    static PerDevice attr;
+    cudaError_t e = smem_setup(attr, k_col_fused<N, P>, FC::SMEM);
+    if (e != cudaSuccess) return e;
+    return launch_pdl(k_col_fused<N, P>, dim3(FC::CTAS, units), dim3(FC::THREADS), FC::SMEM, s, pdl, a);
+}
 
 template <int N>
-static cudaError_t col_fused_n(int units, const ColArgs& a, cudaStream_t s, bool pdl)
+static cudaError_t col_fused_n(int pairs, int units, const ColArgs& a, cudaStream_t s, bool pdl)
 {
     if constexpr (ColLineFor<N>::type::G == 32) {
-        using FC = FusedCfg<N, kFusedPairs>;
-        static PerDevice attr;
-        cudaError_t e = smem_setup(attr, k_col_fused<N, kFusedPairs>, FC::SMEM);
-        if (e != cudaSuccess) return e;
-        return launch_pdl(k_col_fused<N, kFusedPairs>, dim3(FC::CTAS, units), dim3(FC::THREADS), FC::SMEM, s, pdl, a);
-    } else {
-        return cudaErrorInvalidValue;                        // lines of more than one warp
+        if (pairs == 2) return col_fused_np<N, 2>(units, a, s, pdl);
+        if (pairs == 4) return col_fused_np<N, 4>(units, a, s, pdl);
     }
+    return cudaErrorInvalidValue;                            // lines of more than one warp, or no such shape
 }
 
 #define OCEAN_FOR_EACH_N(M) M(32) M(64) M(128) M(256) M(512) M(1024) M(2048)
 
 bool col_fused_available(int N) { return N == 512 || N == 1024; }
 
-cudaError_t launch_col_fused(int N, int units, const ColArgs& a, cudaStream_t s, bool pdl)
+cudaError_t launch_col_fused(int N, int pairs, int units, const ColArgs& a, cudaStream_t s, bool pdl)
 {
     switch (N) {
-    case 512: return col_fused_n<512>(units, a, s, pdl);
-    case 1024: return col_fused_n<1024>(units, a, s, pdl);
+    case 512: return col_fused_n<512>(pairs, units, a, s, pdl);
+    case 1024: return col_fused_n<1024>(pairs, units, a, s, pdl);
     default: return cudaErrorInvalidValue;
     }
 }

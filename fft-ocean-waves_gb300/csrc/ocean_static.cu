@@ -155,8 +155,9 @@ extern "C" int ocean_update_noalloc(const ocean_params* params, const float* h0_
     ca.u0.inv2d  = (float)((double)N / (2.0 * (double)params->L));
     ca.u0.pad_   = 0.0f;
     ca.trigger_next = 0;           // the next call's row pass waits for this frame first
-    if (ocean::tuning_for(N).col_fused) {
-        if ((e = ocean::launch_col_fused(N, 1, ca, s, true)) != cudaSuccess) return cuda_fail(e, "fused column launch");
+    if (const int pairs = ocean::tuning_for(N).col_fused) {
+        if ((e = ocean::launch_col_fused(N, pairs, 1, ca, s, true)) != cudaSuccess)
+            return cuda_fail(e, "fused column launch");
         return OCEAN_OK;
     }
     if ((e = ocean::launch_col_fft(N, 1, ca, s, true)) != cudaSuccess) return cuda_fail(e, "column transform launch");

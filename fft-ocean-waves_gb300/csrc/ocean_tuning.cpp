@@ -61,7 +61,7 @@ Tuning tuning_for(int N)
     const Live& l = live()[i];
     return Tuning{l.row_overlap.load(std::memory_order_relaxed), l.row_ctas_per_sm.load(std::memory_order_relaxed),
                   l.wave_mib.load(std::memory_order_relaxed),
-                  l.col_fused.load(std::memory_order_relaxed) && ocean::col_fused_available(N) ? 1 : 0};
+                  ocean::col_fused_available(N) ? l.col_fused.load(std::memory_order_relaxed) : 0};
 }
 
 }  // namespace ocean
@@ -86,7 +86,7 @@ extern "C" int ocean_set_tuning(int32_t N, const ocean_tuning* cfg)
     const int i = slot(N);
     if (i < 0) return fail(OCEAN_ERR_INVALID, "no tuning entry for N = " + std::to_string(N));
     if ((cfg->row_overlap != 0 && cfg->row_overlap != 1) || cfg->row_ctas_per_sm < 0 || cfg->row_ctas_per_sm > 32 ||
-        cfg->wave_mib < 1 || cfg->wave_mib > 4096 || (cfg->col_fused != 0 && cfg->col_fused != 1))
+        cfg->wave_mib < 1 || cfg->wave_mib > 4096 || (cfg->col_fused != 0 && cfg->col_fused != 2 && cfg->col_fused != 4))
         return fail(OCEAN_ERR_INVALID, "tuning values out of range");
     Live& l = live()[i];
     l.row_overlap.store(cfg->row_overlap);

@@ -11,8 +11,9 @@ candidate of
                               output stage, or waits for it first)
     row_ctas_per_sm  0 (as many as fit), 1, 2, 3, 4, 6, 8 (persistent row-pass
                               grid; caps above the occupancy limit give its grid)
-    col_fused        0 / 1   (N = 512, 1024: the column side as one fused
-                              kernel, or as column FFT + output kernels)
+    col_fused        0 / 2 / 4 (N = 512, 1024: the column side as column FFT +
+                              output kernels, or as one fused kernel with 2 or 4
+                              column pairs per CTA)
 and keeps the fastest (median of `reps` runs).  Then it times the 64-tile,
 8-sample batch (workloads.batched_tiles) for each wave budget and keeps the
 fastest.  It writes DIR/tuning_table.inc -- the table the library compiles
@@ -64,7 +65,7 @@ def tune_size(torch, og, workloads, N, reps, log):
         for i in range(2 * RING):                         # warm-up (first-launch set-up of every kernel)
             ring[i % RING].update(i / 60.0, *outs[i % RING], stream=stream)
         torch.cuda.synchronize()
-        fused_opts = (0, 1) if N in (512, 1024) else (0,)
+        fused_opts = (0, 2, 4) if N in (512, 1024) else (0,)
         for fused in fused_opts:                          # the fused column kernel exists for 512 and 1024
             for cap in (0, 1, 2, 3, 4, 6, 8):             # 0: as many CTAs per SM as fit
                 for overlap in (0, 1):

@@ -366,10 +366,10 @@ typedef struct ocean_tuning {
                                  before starting.  Stream order is kept either way.                            */
     int32_t row_ctas_per_sm;  /* persistent row-pass CTAs per SM, 0 = as many as fit                            */
     int32_t wave_mib;         /* batches: scratch (intermediate + column maps) of one wave of units, MiB        */
-    int32_t col_fused;        /* 1: ocean_update, batches and ocean_update_noalloc run the column transforms and
-                                 the normal/Jacobian stage as one kernel (N = 512 and 1024; ignored elsewhere);
-                                 0: as two kernels through column-major maps, as ocean_update_columns and
-                                 ocean_update_outputs do                                                         */
+    int32_t col_fused;        /* 2 or 4: ocean_update, batches and ocean_update_noalloc run the column
+                                 transforms and the normal/Jacobian stage as one kernel with that many column
+                                 pairs per CTA (N = 512 and 1024; reads 0 elsewhere); 0: as two kernels through
+                                 column-major maps, as ocean_update_columns and ocean_update_outputs do        */
 } ocean_tuning;
 
 OCEAN_API int ocean_get_tuning(int32_t N, ocean_tuning* out);

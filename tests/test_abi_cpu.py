@@ -259,7 +259,7 @@ def test_tuning_table_round_trip(ocean_lib):
     assert ocean_lib.get_tuning(512) == {"row_overlap": 0, "row_ctas_per_sm": 1, "wave_mib": 32, "col_fused": 0}
     ocean_lib.set_tuning(512, **old)
     assert ocean_lib.get_tuning(512) == old
-    for bad in (dict(row_overlap=2), dict(row_ctas_per_sm=-1), dict(wave_mib=0), dict(col_fused=3)):
+    for bad in (dict(row_overlap=2), dict(row_ctas_per_sm=-1), dict(wave_mib=0), dict(col_fused=1), dict(col_fused=3)):
         with pytest.raises(ocean_lib.OceanError):
             ocean_lib.set_tuning(512, **bad)
     assert ocean_lib.get_tuning(512) == old
@@ -267,6 +267,6 @@ def test_tuning_table_round_trip(ocean_lib):
         ocean_lib.get_tuning(48)
     # the fused column kernel exists for N = 512 and 1024 only: elsewhere the
     # entry reads 0 whatever is set
-    old2 = ocean_lib.set_tuning(2048, col_fused=1)
+    old2 = ocean_lib.set_tuning(2048, col_fused=2)
     assert ocean_lib.get_tuning(2048)["col_fused"] == 0
     ocean_lib.set_tuning(2048, **old2)

@@ -187,13 +187,12 @@ def test_adjoint_row_pass_accumulators_and_dh0(N):
     assert np.all(dh0 == 1)
 
 
-@pytest.mark.parametrize("N", [512, 1024])
-def test_col_fused_loads_staging_and_stores(N):
-    """k_col_fused<N, 2>: every line load lies in the intermediate (16-byte
+@pytest.mark.parametrize("N,P", [(512, 2), (1024, 2), (512, 4), (1024, 4)])
+def test_col_fused_loads_staging_and_stores(N, P):
+    """k_col_fused<N, P>: every line load lies in the intermediate (16-byte
     pair loads aligned), each CTA's staged columns (two halo, 2P own) are
     written exactly once before the epilogue reads them, every staged read is
     in range and every output texel is written exactly once over the grid."""
-    P = 2
     G, E, R1, pos, t = line(N, COL_LINE_FOR[N])
     assert G == 32
     COLS, CP, EROWS = 2 * P + 2, N + 16 // P, 256 // (2 * P)

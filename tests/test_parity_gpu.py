@@ -344,11 +344,11 @@ def test_superposition_full_size(torch_cuda, ocean_lib):
 
 @pytest.mark.parametrize("N", [512, 1024])
 def test_fused_column_kernel_matches_two_kernels(torch_cuda, ocean_lib, N):
-    """The fused column kernel (the tuning's col_fused) against the column
-    FFT + output kernels on the same frames, launched back to back on one
-    handle: dx, dy, dz bit for bit (same arithmetic), normal_j within 1e-6
-    relative L2 (its halo columns come from a differently paired transform,
-    which rounds differently)."""
+    """The fused column kernel (the tuning's col_fused: 2 or 4 column pairs
+    per CTA) against the column FFT + output kernels on the same frames,
+    launched back to back on one handle: dx, dy, dz bit for bit (same
+    arithmetic), normal_j within 1e-6 relative L2 (its halo columns come from
+    a differently paired transform, which rounds differently)."""
     torch = torch_cuda
     d = P.c2(N)
     dev = torch.device("cuda")
@@ -356,7 +356,7 @@ def test_fused_column_kernel_matches_two_kernels(torch_cuda, ocean_lib, N):
     outs = {}
     saved = ocean_lib.get_tuning(N)
     try:
-        for fused in (0, 1):
+        for fused in (0, 2, 4):
             ocean_lib.set_tuning(N, col_fused=fused)
             assert ocean_lib.get_tuning(N)["col_fused"] == fused
             with ocean_lib.Ocean(P.lib_params(d), seed=d["seed"]) as oc:
@@ -369,7 +369,8 @@ def test_fused_column_kernel_matches_two_kernels(torch_cuda, ocean_lib, N):
                 outs[fused] = [[x.cpu().numpy() for x in o] for o in sets]
     finally:
         ocean_lib.set_tuning(N, **saved)
-    for a, b in zip(outs[0], outs[1]):
-        for k in range(3):
-            assert np.array_equal(a[k], b[k])
-        assert rel_l2(b[3], a[3]) < 1e-6
+    for fused in (2, 4):
+        for a, b in zip(outs[0], outs[fused]):
+            for k in range(3):
+                assert np.array_equal(a[k], b[k]), fused
+            assert rel_l2(b[3], a[3]) < 1e-6, fused
