@@ -930,14 +930,22 @@ __global__ void __launch_bounds__(FusedCfg<N, P>::THREADS, P == 2 ? 2 : 1) k_col
         if (cj) { p.y = -p.y; q.y = -q.y; }
         v[r] = make_float2(p.x - q.y, p.y + q.x);            // p + i*q
     }
+    // The next frame's row pass may overwrite the intermediate once every
+    // thread's loads have returned (a CTA may count as triggered as soon as any
+    // of its threads triggers).  The barrier's predicate depends on every
+    // loaded value, so no thread passes it before all of the CTA's loads have
+    // completed; the row pass then runs on the SMs this grid leaves free and
+    // completes only after this grid.
+    {
+        unsigned dep = 0;
+#pragma unroll
+        for (int r = 0; r < L::E; ++r) dep |= __float_as_uint(v[r].x) ^ __float_as_uint(v[r].y);
+        (void)__syncthreads_or(dep == 0x7fc00001u);
+        if (a.trigger_next) pdl_launch_dependents();
+    }
     if (!block_wait(&bar_tw, 0, &wait_ok, a.status)) return;
     line_fft<L, +1, true, false>(v, work + li * L::NPAD, tw_s, t, li);
     __syncthreads();                                         // the exchange buffers are free
-    // Every warp of this CTA has used its loads of the intermediate (a CTA may
-    // count as triggered once any of its threads triggers, so not before this
-    // barrier): the next frame's row pass may start overwriting it; it
-    // completes only after this grid.
-    if (a.trigger_next) pdl_launch_dependents();
 
     // Stage the real columns: (-1)^(x+y) * 1/(2N^2) (* lambda for Dx, Dz).
     // y = pos(t, e) is t plus an even constant, so the sign is per thread.
