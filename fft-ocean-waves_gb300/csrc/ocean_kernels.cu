@@ -862,15 +862,15 @@ struct FusedCfg {
     // staged column pitch (floats): the 2P columns a warp reads are 32/(2P)
     // banks apart, and its 32/(2P) rows fill the banks in between
     static constexpr int CP       = N + 16 / P;
-    static constexpr int ETHREADS = 256;                   // epilogue threads
-    static constexpr int EROWS    = ETHREADS / (2 * P);    // rows per epilogue step
+    static constexpr int ETHREADS = THREADS;               // epilogue threads: all of them
+    static constexpr int EROWS    = ETHREADS / (2 * P);    // rows per epilogue step (need not divide N)
     static constexpr size_t XBUF  = (size_t)LINES * L::NPAD;               // float2
     static constexpr size_t EBUF  = ((size_t)3 * COLS * CP + 1) / 2;       // float2
     static constexpr size_t WORK  = XBUF > EBUF ? XBUF : EBUF;
     static constexpr int    TW    = TwPlan<L>::LEN;
     static constexpr int    TW0   = TwPlan<typename LineFor<N>::type>::LEN;   // the row plan precedes it
     static constexpr size_t SMEM  = sizeof(float2) * (TW + WORK) + 128;
-    static_assert(N % (2 * P) == 0 && N % EROWS == 0 && THREADS >= ETHREADS, "fused column layout");
+    static_assert(N % (2 * P) == 0 && THREADS % (2 * P) == 0, "fused column layout");
     static_assert((16 / P) * 2 * P == 32 && 32 % (2 * P) == 0, "conflict-free staging pitch");
 };
 
@@ -967,7 +967,6 @@ __global__ void __launch_bounds__(FusedCfg<N, P>::THREADS, P == 2 ? 2 : 1) k_col
         }
     }
     __syncthreads();
-    if (tid >= FC::ETHREADS) return;
 
     // Epilogue: texel (x0 + c - 1, y), c = tid % 2P + 1, y = tid / 2P + EROWS * k.
     const int    c     = tid % (2 * P) + 1;                  // staged column of the texel

@@ -195,8 +195,8 @@ def test_col_fused_loads_staging_and_stores(N, P):
     in range and every output texel is written exactly once over the grid."""
     G, E, R1, pos, t = line(N, COL_LINE_FOR[N])
     assert G == 32
-    COLS, CP, EROWS = 2 * P + 2, N + 16 // P, 256 // (2 * P)
     LINES = 3 * (P + 1)
+    COLS, CP, EROWS = 2 * P + 2, N + 16 // P, 32 * LINES // (2 * P)
     NPAD = N + N // R1
     assert 3 * COLS * CP <= 2 * LINES * NPAD                       # staging fits the exchange buffers
     r = np.arange(E)[None, :]
@@ -225,11 +225,13 @@ def test_col_fused_loads_staging_and_stores(N, P):
             for cc in range(COLS):
                 used[(f * COLS + cc) * CP:(f * COLS + cc) * CP + N] = True
         assert np.all(stage[used] == 1) and np.all(stage[~used] == 0)
-        # epilogue: threads 0..255, texel (x0 + c - 1, y), reads columns c-1..c+1, rows y-1..y+1
-        tid = np.arange(256)
+        # epilogue: every thread, texel (x0 + c - 1, y), reads columns c-1..c+1, rows y-1..y+1
+        tid = np.arange(32 * LINES)
         c = tid % (2 * P) + 1
         for y0 in range(0, N, EROWS):
             y = tid // (2 * P) + y0
+            keep = y < N
+            y, c = y[keep], (tid % (2 * P) + 1)[keep]
             for dc in (-1, 0, 1):
                 for dy in (-1, 0, 1):
                     rd = (c + dc) * CP + ((y + dy) & (N - 1))
