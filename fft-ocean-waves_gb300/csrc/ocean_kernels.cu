@@ -848,8 +848,8 @@ __global__ void __launch_bounds__(kOutTh, 5) k_col_out(const __grid_constant__ C
 // row-transformed spectra are Hermitian in y.  One warp per line, lines read
 // straight from the L2-resident intermediate.  After the transforms the real
 // columns are staged in shared memory (the exchange buffers, reused) and the
-// CTA computes its 2P x N output texels from there, four adjacent texels of a
-// row per thread (16-byte stores).
+// CTA computes its 2P x N output texels from there, the lanes of a warp on 2P
+// adjacent columns of 32/(2P) rows.
 // ---------------------------------------------------------------------------
 template <int N, int P>
 struct FusedCfg {
@@ -862,14 +862,15 @@ struct FusedCfg {
     // staged column pitch (floats): the 2P columns a warp reads are 32/(2P)
     // banks apart, and its 32/(2P) rows fill the banks in between
     static constexpr int CP       = N + 16 / P;
-    static constexpr int EROWS    = THREADS / (P / 2);     // rows per epilogue step (need not divide N)
+    static constexpr int ETHREADS = THREADS;               // epilogue threads: all of them
+    static constexpr int EROWS    = ETHREADS / (2 * P);    // rows per epilogue step (need not divide N)
     static constexpr size_t XBUF  = (size_t)LINES * L::NPAD;               // float2
     static constexpr size_t EBUF  = ((size_t)3 * COLS * CP + 1) / 2;       // float2
     static constexpr size_t WORK  = XBUF > EBUF ? XBUF : EBUF;
     static constexpr int    TW    = TwPlan<L>::LEN;
     static constexpr int    TW0   = TwPlan<typename LineFor<N>::type>::LEN;   // the row plan precedes it
     static constexpr size_t SMEM  = sizeof(float2) * (TW + WORK) + 128;
-    static_assert(N % (2 * P) == 0 && P % 2 == 0 && THREADS % (P / 2) == 0, "fused column layout");
+    static_assert(N % (2 * P) == 0 && THREADS % (2 * P) == 0, "fused column layout");
     static_assert((16 / P) * 2 * P == 32 && 32 % (2 * P) == 0, "conflict-free staging pitch");
 };
 
@@ -967,59 +968,39 @@ __global__ void __launch_bounds__(FusedCfg<N, P>::THREADS, P == 2 ? 2 : 1) k_col
     }
     __syncthreads();
 
-    // Epilogue: each thread computes four adjacent texels of one row -- output
-    // columns x0 + 4q .. x0 + 4q + 3 (staged columns 4q + 1 .. 4q + 4),
-    // q = tid % (P/2) -- at rows y = tid / (P/2) + EROWS k, reading the 6 x 3
-    // neighbourhood once for all four and writing 16-byte pieces.
-    constexpr int Q = P / 2;                                 // groups of four columns
-    const int    q     = tid % Q;
-    const int    s0    = 4 * q;                              // staged column of the first texel's x - 1
-    const float* EX    = E + (size_t)s0 * FC::CP;            // Dx, Dy, Dz from staged column s0 on
-    const float* EY    = EX + (size_t)FC::COLS * FC::CP;
-    const float* EZ    = EX + (size_t)2 * FC::COLS * FC::CP;
+    // Epilogue: texel (x0 + c - 1, y), c = tid % 2P + 1, y = tid / 2P + EROWS * k.
+    const int    c     = tid % (2 * P) + 1;                  // staged column of the texel
+    const int    r0    = tid / (2 * P);
+    const float* EX    = E;                                  // Dx columns
+    const float* EY    = E + (size_t)FC::COLS * FC::CP;      // Dy
+    const float* EZ    = E + (size_t)2 * FC::COLS * FC::CP;  // Dz
+    const int    cm    = (c - 1) * FC::CP, c0 = c * FC::CP, cp = (c + 1) * FC::CP;
     float* const  odx  = cu->dx;
     float* const  ody  = cu->dy;
     float* const  odz  = cu->dz;
     float4* const onj  = cu->nj;
     const float   inv2d = cu->inv2d;
-    const int     x    = x0 + 4 * q;
-    for (int y = tid / Q; y < N; y += FC::EROWS) {
+    const int     x    = x0 + c - 1;
+#pragma unroll 2
+    for (int y = r0; y < N; y += FC::EROWS) {
         const int ym = (y - 1) & (N - 1), yq = (y + 1) & (N - 1);
-        float Ym[6], Y0[6], Yq[6], X0[6], Z0[6], Xm[4], Xq[4], Zm[4], Zq[4];
-#pragma unroll
-        for (int j = 0; j < 6; ++j) {
-            Ym[j] = EY[j * FC::CP + ym];
-            Y0[j] = EY[j * FC::CP + y];
-            Yq[j] = EY[j * FC::CP + yq];
-            X0[j] = EX[j * FC::CP + y];
-            Z0[j] = EZ[j * FC::CP + y];
-        }
-#pragma unroll
-        for (int j = 0; j < 4; ++j) {
-            Xm[j] = EX[(j + 1) * FC::CP + ym];
-            Xq[j] = EX[(j + 1) * FC::CP + yq];
-            Zm[j] = EZ[(j + 1) * FC::CP + ym];
-            Zq[j] = EZ[(j + 1) * FC::CP + yq];
-        }
-        const size_t o = (size_t)y * N + x;
-#pragma unroll
-        for (int j = 0; j < 4; ++j) {
-            // taps z0..z7 (normal_map_cs.glsl:37-44) around (x + j, y)
-            const float z0 = Ym[j], z1 = Ym[j + 1], z2 = Ym[j + 2], z3 = Y0[j], z4 = Y0[j + 2];
-            const float z5 = Yq[j], z6 = Yq[j + 1], z7 = Yq[j + 2];
-            const float nz = z0 + 2.0f * z1 + z2 - z5 - 2.0f * z6 - z7;
-            const float nx = z0 + 2.0f * z3 + z5 - z2 - 2.0f * z4 - z7;
-            const float rn = rsqrtf(nx * nx + 1.0f + nz * nz);
-            const float dxx = (X0[j + 2] - X0[j]) * inv2d;
-            const float dxz = (Xq[j] - Xm[j]) * inv2d;
-            const float dzx = (Z0[j + 2] - Z0[j]) * inv2d;
-            const float dzz = (Zq[j] - Zm[j]) * inv2d;
-            const float dJ  = (dxx * dzz - dxz * dzx) - dxx - dzz;
-            __stcs(onj + o + j, make_float4(nx * rn, rn, nz * rn, 1.0f + dJ));
-        }
-        __stcs(reinterpret_cast<float4*>(odx + o), make_float4(X0[1], X0[2], X0[3], X0[4]));
-        __stcs(reinterpret_cast<float4*>(ody + o), make_float4(Y0[1], Y0[2], Y0[3], Y0[4]));
-        __stcs(reinterpret_cast<float4*>(odz + o), make_float4(Z0[1], Z0[2], Z0[3], Z0[4]));
+        // taps z0..z7 (normal_map_cs.glsl:37-44) around (x, y)
+        const float z0 = EY[cm + ym], z1 = EY[c0 + ym], z2 = EY[cp + ym];
+        const float z3 = EY[cm + y], z4 = EY[cp + y];
+        const float z5 = EY[cm + yq], z6 = EY[c0 + yq], z7 = EY[cp + yq];
+        const float nz = z0 + 2.0f * z1 + z2 - z5 - 2.0f * z6 - z7;
+        const float nx = z0 + 2.0f * z3 + z5 - z2 - 2.0f * z4 - z7;
+        const float rn = rsqrtf(nx * nx + 1.0f + nz * nz);
+        const float dxx = (EX[cp + y] - EX[cm + y]) * inv2d;
+        const float dxz = (EX[c0 + yq] - EX[c0 + ym]) * inv2d;
+        const float dzx = (EZ[cp + y] - EZ[cm + y]) * inv2d;
+        const float dzz = (EZ[c0 + yq] - EZ[c0 + ym]) * inv2d;
+        const float dJ  = (dxx * dzz - dxz * dzx) - dxx - dzz;
+        const size_t o  = (size_t)y * N + x;
+        __stcs(odx + o, EX[c0 + y]);
+        __stcs(ody + o, EY[c0 + y]);
+        __stcs(odz + o, EZ[c0 + y]);
+        __stcs(onj + o, make_float4(nx * rn, rn, nz * rn, 1.0f + dJ));
     }
 }
 

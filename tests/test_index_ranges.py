@@ -196,7 +196,7 @@ def test_col_fused_loads_staging_and_stores(N, P):
     G, E, R1, pos, t = line(N, COL_LINE_FOR[N])
     assert G == 32
     LINES = 3 * (P + 1)
-    COLS, CP = 2 * P + 2, N + 16 // P
+    COLS, CP, EROWS = 2 * P + 2, N + 16 // P, 32 * LINES // (2 * P)
     NPAD = N + N // R1
     assert 3 * COLS * CP <= 2 * LINES * NPAD                       # staging fits the exchange buffers
     r = np.arange(E)[None, :]
@@ -225,20 +225,16 @@ def test_col_fused_loads_staging_and_stores(N, P):
             for cc in range(COLS):
                 used[(f * COLS + cc) * CP:(f * COLS + cc) * CP + N] = True
         assert np.all(stage[used] == 1) and np.all(stage[~used] == 0)
-        # epilogue: every thread, texels (x0 + 4q + j, y), j < 4, reading
-        # staged columns 4q .. 4q + 5 at rows y - 1 .. y + 1
-        Q = P // 2
+        # epilogue: every thread, texel (x0 + c - 1, y), reads columns c-1..c+1, rows y-1..y+1
         tid = np.arange(32 * LINES)
-        q = tid % Q
-        for y0 in range(0, N, 32 * LINES // Q):
-            y = tid // Q + y0
+        c = tid % (2 * P) + 1
+        for y0 in range(0, N, EROWS):
+            y = tid // (2 * P) + y0
             keep = y < N
-            yy, qq = y[keep], q[keep]
-            for k in range(6):
+            y, c = y[keep], (tid % (2 * P) + 1)[keep]
+            for dc in (-1, 0, 1):
                 for dy in (-1, 0, 1):
-                    rd = (4 * qq + k) * CP + ((yy + dy) & (N - 1))
+                    rd = (c + dc) * CP + ((y + dy) & (N - 1))
                     assert rd.min() >= 0 and rd.max() < COLS * CP and np.all(used[rd])
-            for j in range(4):
-                np.add.at(out_hits, yy * N + x0 + 4 * qq + j, 1)
-            assert np.all((yy * N + x0 + 4 * qq) % 4 == 0)              # 16-byte output pieces
+            np.add.at(out_hits, y * N + x0 + c - 1, 1)
     assert np.all(out_hits == 1)
