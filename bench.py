@@ -55,10 +55,10 @@ sys.path.insert(0, ROOT)
 
 METRIC = "ocean frames/s (N=1024, 3 fields + normal/J)"
 BYTES_PER_TEXEL = 92            # algorithmic bytes per texel per frame
-# The frame's 92 B/texel split over the three kernels: rows read h0 (16) and
-# write the intermediate (24); columns read it (24); outputs write dx, dy, dz
-# and normal_j (28).
-KERNEL_BYTES = {"k_row_pass": 40, "k_row_ws": 40, "k_col_fft": 24, "k_col_out": 28}
+# The frame's 92 B/texel split over its kernels: rows read h0 (16) and write
+# the intermediate (24); columns read it (24); outputs write dx, dy, dz and
+# normal_j (28); the fused column kernel does both column stages (52).
+KERNEL_BYTES = {"k_row_pass": 40, "k_row_ws": 40, "k_col_fft": 24, "k_col_out": 28, "k_col_fused": 52}
 
 
 def row_kernel(N):
@@ -305,9 +305,14 @@ def run_gpu(args, world, rank, local):
             # work does not overlap and the average is one launch's duration.
             kernel_ms = {}
             saved = og.set_tuning(N, row_overlap=0)
-            for name, call in ((row_kernel(N), lambda j, t: ring[j].update_rows(t, stream=stream)),
-                               ("k_col_fft", lambda j, t: ring[j].update_columns(stream=stream)),
-                               ("k_col_out", lambda j, t: ring[j].update_outputs(*ring_out[j], stream=stream))):
+            if og.get_tuning(N)["col_fused"]:                # the frame's column side is one kernel
+                stages = ((row_kernel(N), lambda j, t: ring[j].update_rows(t, stream=stream)),
+                          ("k_col_fused", lambda j, t: ring[j].update_columns_outputs(*ring_out[j], stream=stream)))
+            else:
+                stages = ((row_kernel(N), lambda j, t: ring[j].update_rows(t, stream=stream)),
+                          ("k_col_fft", lambda j, t: ring[j].update_columns(stream=stream)),
+                          ("k_col_out", lambda j, t: ring[j].update_outputs(*ring_out[j], stream=stream)))
+            for name, call in stages:
                 a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
                 prime()
                 a.record(stream)
@@ -319,20 +324,24 @@ def run_gpu(args, world, rank, local):
             og.set_tuning(N, **saved)
             # the same stages with events between them inside flushed frames
             # (each then also pays its own launch)
-            kv = [[torch.cuda.Event(enable_timing=True) for _ in range(4)] for _ in range(K)]
+            kv = [[torch.cuda.Event(enable_timing=True) for _ in range(len(stages) + 1)] for _ in range(K)]
             for i in range(K):
                 flush()
                 t = (args.warmup + i) / 60.0
-                kv[i][0].record(stream)
-                oc.update_rows(t, stream=stream)
-                kv[i][1].record(stream)
-                oc.update_columns(stream=stream)
-                kv[i][2].record(stream)
-                oc.update_outputs(dx, dy, dz, nj, stream=stream)
-                kv[i][3].record(stream)
+                for j, (name, call) in enumerate(stages):
+                    kv[i][j].record(stream)
+                    if j == 0:
+                        oc.update_rows(t, stream=stream)
+                    elif name == "k_col_fused":
+                        oc.update_columns_outputs(dx, dy, dz, nj, stream=stream)
+                    elif name == "k_col_fft":
+                        oc.update_columns(stream=stream)
+                    else:
+                        oc.update_outputs(dx, dy, dz, nj, stream=stream)
+                kv[i][len(stages)].record(stream)
             torch.cuda.synchronize()
             kernel_iso_ms = {name: sum(kv[i][j].elapsed_time(kv[i][j + 1]) for i in range(K)) / K
-                             for j, name in enumerate((row_kernel(N), "k_col_fft", "k_col_out"))}
+                             for j, (name, _) in enumerate(stages)}
 
             # e2e: C-ABI call + all outputs copied to pinned host memory, every frame.
             hdx, hdy, hdz = (torch.empty((N, N), dtype=torch.float32, pin_memory=True) for _ in range(3))

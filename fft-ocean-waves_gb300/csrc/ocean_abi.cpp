@@ -510,14 +510,12 @@ int ocean_update_outputs(ocean_t* o, const ocean_outputs* out, void* stream)
     return OCEAN_OK;
 }
 
-int ocean_update(ocean_t* o, double t, const ocean_outputs* out, void* stream)
+int ocean_update_columns_outputs(ocean_t* o, const ocean_outputs* out, void* stream)
 {
     if (!o) return fail(OCEAN_ERR_INVALID, "ocean is NULL");
-    if (!std::isfinite(t)) return fail(OCEAN_ERR_INVALID, "time is not finite");
     ocean_outputs res;
     int rc = resolve_outputs(o, out, &res);
     if (rc) return rc;
-    if ((rc = ocean_update_rows(o, t, stream)) != OCEAN_OK) return rc;
     if (const int pairs = ocean::tuning_for(o->N).col_fused) {
         // both column stages in one kernel: the column maps stay on chip
         nvtxRangePushA("ocean columns + outputs: vertical FFT, inversion, normal map + Jacobian");
@@ -529,6 +527,17 @@ int ocean_update(ocean_t* o, double t, const ocean_outputs* out, void* stream)
     }
     if ((rc = ocean_update_columns(o, stream)) != OCEAN_OK) return rc;
     return ocean_update_outputs(o, &res, stream);
+}
+
+int ocean_update(ocean_t* o, double t, const ocean_outputs* out, void* stream)
+{
+    if (!o) return fail(OCEAN_ERR_INVALID, "ocean is NULL");
+    if (!std::isfinite(t)) return fail(OCEAN_ERR_INVALID, "time is not finite");
+    ocean_outputs res;
+    int rc = resolve_outputs(o, out, &res);
+    if (rc) return rc;
+    if ((rc = ocean_update_rows(o, t, stream)) != OCEAN_OK) return rc;
+    return ocean_update_columns_outputs(o, &res, stream);
 }
 
 int ocean_device_status(ocean_t* o, void* stream)

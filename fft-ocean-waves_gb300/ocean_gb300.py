@@ -31,7 +31,7 @@ OCEAN_FLAG_LITERAL_CONJ = 1
 # Every entry point include/ocean.h declares (checked by the CPU tests).
 EXPORTS = [
     "ocean_create", "ocean_create_seeded", "ocean_destroy", "ocean_update", "ocean_update_rows",
-    "ocean_update_columns", "ocean_update_outputs", "ocean_get_outputs",
+    "ocean_update_columns", "ocean_update_outputs", "ocean_update_columns_outputs", "ocean_get_outputs",
     "ocean_set_params", "ocean_get_params", "ocean_get_h0", "ocean_set_h0", "ocean_compute_h0",
     "ocean_fill_noise", "ocean_bit_reversed_indices", "ocean_butterfly_table", "ocean_last_error",
     "ocean_version", "ocean_backward", "ocean_device_status", "ocean_batch_create", "ocean_batch_update",
@@ -115,6 +115,7 @@ def load() -> C.CDLL:
     L.ocean_update_rows.argtypes = [vp, C.c_double, vp]
     L.ocean_update_columns.argtypes = [vp, vp]
     L.ocean_update_outputs.argtypes = [vp, P(ocean_outputs), vp]
+    L.ocean_update_columns_outputs.argtypes = [vp, P(ocean_outputs), vp]
     L.ocean_get_outputs.argtypes = [vp, P(ocean_outputs)]
     L.ocean_set_params.argtypes = [vp, P(ocean_params)]
     L.ocean_get_params.argtypes = [vp, P(ocean_params)]
@@ -467,6 +468,15 @@ class Ocean:
             return
         o = ocean_outputs(_addr(dx), _addr(dy), _addr(dz), _addr(normal_j))
         check(load().ocean_update_outputs(self._h, C.byref(o), _stream(stream)))
+
+    def update_columns_outputs(self, dx=None, dy=None, dz=None, normal_j=None, stream=None) -> None:
+        """Columns and outputs as one stage (one fused kernel where the tuning
+        says so)."""
+        if dx is None:
+            check(load().ocean_update_columns_outputs(self._h, None, _stream(stream)))
+            return
+        o = ocean_outputs(_addr(dx), _addr(dy), _addr(dz), _addr(normal_j))
+        check(load().ocean_update_columns_outputs(self._h, C.byref(o), _stream(stream)))
 
     def backward(self, times, g_dx=None, g_dy=None, g_dz=None, dh0=None, accumulate=False, stream=None) -> dict:
         """Gradients for upstream dL/d(dx, dy, dz) of shape (T, N, N) (device

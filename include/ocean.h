@@ -110,10 +110,18 @@ OCEAN_API int ocean_update(ocean_t* ocean, double t, const ocean_outputs* out, v
  *   outputs  the maps written to dx, dy, dz, plus the normal map and
  *            Jacobian (generate_normal_map(), main.cpp:244, :687-707); out ==
  *            NULL writes the handle-owned buffers.
- * ocean_update == rows, columns, outputs on one stream. */
+ * ocean_update == rows, columns, outputs on one stream (or rows and
+ * ocean_update_columns_outputs, below). */
 OCEAN_API int ocean_update_rows(ocean_t* ocean, double t, void* stream);
 OCEAN_API int ocean_update_columns(ocean_t* ocean, void* stream);
 OCEAN_API int ocean_update_outputs(ocean_t* ocean, const ocean_outputs* out, void* stream);
+
+/* columns + outputs as one stage (the vertical butterfly passes, inversion_cs.glsl
+ * and generate_normal_map(), main.cpp:647-707): one fused kernel where the
+ * launch configuration says so (ocean_tuning.col_fused; the column-major maps
+ * then stay on chip), else ocean_update_columns then ocean_update_outputs.
+ * ocean_update == ocean_update_rows, ocean_update_columns_outputs. */
+OCEAN_API int ocean_update_columns_outputs(ocean_t* ocean, const ocean_outputs* out, void* stream);
 
 /* Synchronise `stream` and report (and clear) the handle's device status:
  * OCEAN_ERR_TIMEOUT if a kernel gave up a bounded wait for its TMA copies
