@@ -848,9 +848,8 @@ __global__ void __launch_bounds__(kOutTh, 5) k_col_out(const __grid_constant__ C
 // row-transformed spectra are Hermitian in y.  One warp per line, lines read
 // straight from the L2-resident intermediate.  After the transforms the real
 // columns are staged in shared memory (the exchange buffers, reused) and the
-// CTA computes its 2P x N output texels from there: the normal map with the
-// lanes of a warp on 2P adjacent columns of 32/(2P) rows (full 128-byte
-// lines at P = 4), the three displacement maps copied out in 16-byte pieces.
+// CTA computes its 2P x N output texels from there, the lanes of a warp on 2P
+// adjacent columns of 32/(2P) rows.
 // ---------------------------------------------------------------------------
 template <int N, int P>
 struct FusedCfg {
@@ -871,7 +870,7 @@ struct FusedCfg {
     static constexpr int    TW    = TwPlan<L>::LEN;
     static constexpr int    TW0   = TwPlan<typename LineFor<N>::type>::LEN;   // the row plan precedes it
     static constexpr size_t SMEM  = sizeof(float2) * (TW + WORK) + 128;
-    static_assert(N % (2 * P) == 0 && THREADS % (2 * P) == 0 && P % 2 == 0, "fused column layout");
+    static_assert(N % (2 * P) == 0 && THREADS % (2 * P) == 0, "fused column layout");
     static_assert((16 / P) * 2 * P == 32 && 32 % (2 * P) == 0, "conflict-free staging pitch");
 };
 
@@ -997,23 +996,11 @@ __global__ void __launch_bounds__(FusedCfg<N, P>::THREADS, P == 2 ? 2 : 1) k_col
         const float dzx = (EZ[cp + y] - EZ[cm + y]) * inv2d;
         const float dzz = (EZ[c0 + yq] - EZ[c0 + ym]) * inv2d;
         const float dJ  = (dxx * dzz - dxz * dzx) - dxx - dzz;
-        __stcs(onj + (size_t)y * N + x, make_float4(nx * rn, rn, nz * rn, 1.0f + dJ));
-    }
-    // dx, dy, dz are the staged columns themselves: copied out with one 16-byte
-    // store per four texels of a row (thread: column group g of four, row y;
-    // the lanes of a warp cover 32/(P/2) rows, conflict-free in the staging)
-    constexpr int Q  = P / 2;
-    const int     g  = tid % Q;
-    const int     xg = x0 + 4 * g;
-    for (int y = tid / Q; y < N; y += FC::THREADS / Q) {
-        const size_t o = (size_t)y * N + xg;
-        const int    s = (4 * g + 1) * FC::CP + y;
-        __stcs(reinterpret_cast<float4*>(odx + o),
-               make_float4(EX[s], EX[s + FC::CP], EX[s + 2 * FC::CP], EX[s + 3 * FC::CP]));
-        __stcs(reinterpret_cast<float4*>(ody + o),
-               make_float4(EY[s], EY[s + FC::CP], EY[s + 2 * FC::CP], EY[s + 3 * FC::CP]));
-        __stcs(reinterpret_cast<float4*>(odz + o),
-               make_float4(EZ[s], EZ[s + FC::CP], EZ[s + 2 * FC::CP], EZ[s + 3 * FC::CP]));
+        const size_t o  = (size_t)y * N + x;
+        __stcs(odx + o, EX[c0 + y]);
+        __stcs(ody + o, EY[c0 + y]);
+        __stcs(odz + o, EZ[c0 + y]);
+        __stcs(onj + o, make_float4(nx * rn, rn, nz * rn, 1.0f + dJ));
     }
 }
 
