@@ -1120,6 +1120,8 @@ static cudaError_t row_pass_n(const RowArgs& a, cudaStream_t s)
             if constexpr (N <= 1024) return row_ws_nm<N, false, true>(a, s);
             else return cudaErrorInvalidValue;                // its staged h0 rows would not fit
         }
+        if (tuning_for(N).row_variant == 1)                   // every warp runs the prepass and its line
+            return single ? row_pass_nm<N, false, false>(a, s) : row_pass_nm<N, true, false>(a, s);
         return single ? row_ws_nm<N, false, false>(a, s) : row_ws_nm<N, true, false>(a, s);
     } else {
         if (!a.spec) return row_pass_nm<N, false, true>(a, s);

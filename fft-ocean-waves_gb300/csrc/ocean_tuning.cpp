@@ -14,7 +14,7 @@
 namespace {
 
 struct Entry {
-    int N, row_overlap, row_ctas_per_sm, wave_mib, col_fused;
+    int N, row_overlap, row_ctas_per_sm, wave_mib, col_fused, row_variant;
 };
 constexpr Entry kTable[] = {
 #include "tuning_table.inc"
@@ -23,7 +23,7 @@ constexpr int kSizes = (int)(sizeof(kTable) / sizeof(kTable[0]));
 static_assert(kSizes == 7, "one entry per supported N (32 .. 2048)");
 
 struct Live {
-    std::atomic<int> row_overlap, row_ctas_per_sm, wave_mib, col_fused;
+    std::atomic<int> row_overlap, row_ctas_per_sm, wave_mib, col_fused, row_variant;
 };
 
 // The live table, filled from kTable on first use (thread-safe static
@@ -37,6 +37,7 @@ Live* live()
             l[i].row_ctas_per_sm.store(kTable[i].row_ctas_per_sm);
             l[i].wave_mib.store(kTable[i].wave_mib);
             l[i].col_fused.store(kTable[i].col_fused);
+            l[i].row_variant.store(kTable[i].row_variant);
         }
         return l;
     }();
@@ -57,11 +58,12 @@ namespace ocean {
 Tuning tuning_for(int N)
 {
     const int i = slot(N);
-    if (i < 0) return Tuning{0, 0, 64, 0};
+    if (i < 0) return Tuning{0, 0, 64, 0, 1};
     const Live& l = live()[i];
     return Tuning{l.row_overlap.load(std::memory_order_relaxed), l.row_ctas_per_sm.load(std::memory_order_relaxed),
                   l.wave_mib.load(std::memory_order_relaxed),
-                  ocean::col_fused_available(N) ? l.col_fused.load(std::memory_order_relaxed) : 0};
+                  ocean::col_fused_available(N) ? l.col_fused.load(std::memory_order_relaxed) : 0,
+                  N >= 512 ? l.row_variant.load(std::memory_order_relaxed) : 1};
 }
 
 }  // namespace ocean
@@ -77,6 +79,7 @@ extern "C" int ocean_get_tuning(int32_t N, ocean_tuning* out)
     out->row_ctas_per_sm  = t.row_ctas_per_sm;
     out->wave_mib         = t.wave_mib;
     out->col_fused        = t.col_fused;
+    out->row_variant      = t.row_variant;
     return OCEAN_OK;
 }
 
@@ -86,12 +89,14 @@ extern "C" int ocean_set_tuning(int32_t N, const ocean_tuning* cfg)
     const int i = slot(N);
     if (i < 0) return fail(OCEAN_ERR_INVALID, "no tuning entry for N = " + std::to_string(N));
     if ((cfg->row_overlap != 0 && cfg->row_overlap != 1) || cfg->row_ctas_per_sm < 0 || cfg->row_ctas_per_sm > 32 ||
-        cfg->wave_mib < 1 || cfg->wave_mib > 4096 || (cfg->col_fused != 0 && cfg->col_fused != 2 && cfg->col_fused != 4))
+        cfg->wave_mib < 1 || cfg->wave_mib > 4096 || (cfg->col_fused != 0 && cfg->col_fused != 2 && cfg->col_fused != 4) ||
+        (cfg->row_variant != 0 && cfg->row_variant != 1))
         return fail(OCEAN_ERR_INVALID, "tuning values out of range");
     Live& l = live()[i];
     l.row_overlap.store(cfg->row_overlap);
     l.row_ctas_per_sm.store(cfg->row_ctas_per_sm);
     l.wave_mib.store(cfg->wave_mib);
     l.col_fused.store(cfg->col_fused);
+    l.row_variant.store(cfg->row_variant);
     return OCEAN_OK;
 }

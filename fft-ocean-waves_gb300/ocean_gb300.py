@@ -60,7 +60,7 @@ class ocean_outputs(C.Structure):
 
 class ocean_tuning(C.Structure):
     _fields_ = [("row_overlap", C.c_int32), ("row_ctas_per_sm", C.c_int32), ("wave_mib", C.c_int32),
-                ("col_fused", C.c_int32)]
+                ("col_fused", C.c_int32), ("row_variant", C.c_int32)]
 
 
 class ocean_grads(C.Structure):
@@ -213,19 +213,21 @@ def get_tuning(N: int) -> dict:
     t = ocean_tuning()
     check(load().ocean_get_tuning(int(N), C.byref(t)))
     return {"row_overlap": t.row_overlap, "row_ctas_per_sm": t.row_ctas_per_sm, "wave_mib": t.wave_mib,
-            "col_fused": t.col_fused}
+            "col_fused": t.col_fused, "row_variant": t.row_variant}
 
 
-def set_tuning(N: int, row_overlap=None, row_ctas_per_sm=None, wave_mib=None, col_fused=None) -> dict:
+def set_tuning(N: int, row_overlap=None, row_ctas_per_sm=None, wave_mib=None, col_fused=None,
+               row_variant=None) -> dict:
     """Replace fields of size N's launch configuration for this process
     (ocean_set_tuning); returns the previous configuration."""
     old = get_tuning(N)
     new = dict(old)
     for k, v in (("row_overlap", row_overlap), ("row_ctas_per_sm", row_ctas_per_sm), ("wave_mib", wave_mib),
-                 ("col_fused", col_fused)):
+                 ("col_fused", col_fused), ("row_variant", row_variant)):
         if v is not None:
             new[k] = int(v)
-    t = ocean_tuning(new["row_overlap"], new["row_ctas_per_sm"], new["wave_mib"], new["col_fused"])
+    t = ocean_tuning(new["row_overlap"], new["row_ctas_per_sm"], new["wave_mib"], new["col_fused"],
+                     new["row_variant"])
     check(load().ocean_set_tuning(int(N), C.byref(t)))
     return old
 

@@ -11,6 +11,8 @@ candidate of
                               output stage, or waits for it first)
     row_ctas_per_sm  0 (as many as fit), 1, 2, 3, 4, 6, 8 (persistent row-pass
                               grid; caps above the occupancy limit give its grid)
+    row_variant      0 / 1   (N >= 512: warp-specialised row pass, or every warp
+                              running the prepass and then its line FFT)
     col_fused        0 / 2 / 4 (N = 512, 1024: the column side as column FFT +
                               output kernels, or as one fused kernel with 2 or 4
                               column pairs per CTA)
@@ -66,14 +68,18 @@ def tune_size(torch, og, workloads, N, reps, log):
             ring[i % RING].update(i / 60.0, *outs[i % RING], stream=stream)
         torch.cuda.synchronize()
         fused_opts = (0, 2, 4) if N in (512, 1024) else (0,)
-        for fused in fused_opts:                          # the fused column kernel exists for 512 and 1024
-            for cap in (0, 1, 2, 3, 4, 6, 8):             # 0: as many CTAs per SM as fit
-                for overlap in (0, 1):
-                    og.set_tuning(N, row_overlap=overlap, row_ctas_per_sm=cap, col_fused=fused)
-                    ms = time_frames(torch, og, ring, outs, stream, reps=reps)
-                    results.append({"row_overlap": overlap, "row_ctas_per_sm": cap, "col_fused": fused,
-                                    "ms_per_frame": round(ms, 6)})
-                    log(f"N={N} fused={fused} overlap={overlap} ctas/SM={cap}: {ms * 1e3:.2f} us")
+        variants = (0, 1) if N >= 512 else (1,)
+        for variant in variants:                          # row pass: warp-specialised or every warp
+            for fused in fused_opts:                      # the fused column kernel exists for 512 and 1024
+                for cap in (0, 1, 2, 3, 4, 6, 8):         # 0: as many CTAs per SM as fit
+                    for overlap in (0, 1):
+                        og.set_tuning(N, row_overlap=overlap, row_ctas_per_sm=cap, col_fused=fused,
+                                      row_variant=variant)
+                        ms = time_frames(torch, og, ring, outs, stream, reps=reps)
+                        results.append({"row_overlap": overlap, "row_ctas_per_sm": cap, "col_fused": fused,
+                                        "row_variant": variant, "ms_per_frame": round(ms, 6)})
+                        log(f"N={N} variant={variant} fused={fused} overlap={overlap} ctas/SM={cap}: "
+                            f"{ms * 1e3:.2f} us")
     for oc in ring:
         oc.close()
     best = min(results, key=lambda r: r["ms_per_frame"])
@@ -140,6 +146,7 @@ def main():
         table[N]["row_overlap"] = best["row_overlap"]
         table[N]["row_ctas_per_sm"] = best["row_ctas_per_sm"]
         table[N]["col_fused"] = best.get("col_fused", 0)
+        table[N]["row_variant"] = best.get("row_variant", table[N]["row_variant"])
         sweep["sizes"][N] = {"best": best, "all": res}
     for N in SIZES:                                       # the batch is timed with the winners
         og.set_tuning(N, **table[N])
@@ -149,12 +156,12 @@ def main():
             table[N]["wave_mib"] = best["wave_mib"]
         sweep["batch"] = {"best": best, "all": res}
     dev = torch.cuda.get_device_name()
-    lines = ["// Launch configuration per N: {N, row_overlap, row_ctas_per_sm, wave_mib, col_fused}.",
+    lines = ["// Launch configuration per N: {N, row_overlap, row_ctas_per_sm, wave_mib, col_fused, row_variant}.",
              "// Written by fft-ocean-waves_gb300/tune.py from measurements on a GB300",
              f"// ({dev}): steady back-to-back frames for the single-tile knobs (median of",
              f"// {args.reps} runs of 40 frames), the 64-tile batch for wave_mib."]
     lines += [f"{{{N}, {table[N]['row_overlap']}, {table[N]['row_ctas_per_sm']}, {table[N]['wave_mib']}, "
-              f"{table[N]['col_fused']}}}," for N in SIZES]
+              f"{table[N]['col_fused']}, {table[N]['row_variant']}}}," for N in SIZES]
     with open(os.path.join(args.out, "tuning_table.inc"), "w") as fh:
         fh.write("\n".join(lines) + "\n")
     with open(os.path.join(args.out, "tuning_sweep.json"), "w") as fh:

@@ -378,6 +378,9 @@ typedef struct ocean_tuning {
                                  transforms and the normal/Jacobian stage as one kernel with that many column
                                  pairs per CTA (N = 512 and 1024; reads 0 elsewhere); 0: as two kernels through
                                  column-major maps, as ocean_update_columns and ocean_update_outputs do        */
+    int32_t row_variant;      /* N >= 512: 0 = warp-specialised row pass (prepass warps feed transform warps),
+                                 1 = every warp runs the prepass and then its line FFT (one row pair per CTA
+                                 at N = 1024); below 512 only the latter exists and this reads 1            */
 } ocean_tuning;
 
 OCEAN_API int ocean_get_tuning(int32_t N, ocean_tuning* out);

@@ -255,11 +255,13 @@ def test_tuning_table_round_trip(ocean_lib):
     for N in (32, 64, 128, 256, 512, 1024, 2048):
         t = ocean_lib.get_tuning(N)
         assert t["row_overlap"] in (0, 1) and t["row_ctas_per_sm"] >= 0 and t["wave_mib"] >= 1
-    old = ocean_lib.set_tuning(512, row_overlap=0, row_ctas_per_sm=1, wave_mib=32, col_fused=0)
-    assert ocean_lib.get_tuning(512) == {"row_overlap": 0, "row_ctas_per_sm": 1, "wave_mib": 32, "col_fused": 0}
+    old = ocean_lib.set_tuning(512, row_overlap=0, row_ctas_per_sm=1, wave_mib=32, col_fused=0, row_variant=1)
+    assert ocean_lib.get_tuning(512) == {"row_overlap": 0, "row_ctas_per_sm": 1, "wave_mib": 32, "col_fused": 0,
+                                         "row_variant": 1}
     ocean_lib.set_tuning(512, **old)
     assert ocean_lib.get_tuning(512) == old
-    for bad in (dict(row_overlap=2), dict(row_ctas_per_sm=-1), dict(wave_mib=0), dict(col_fused=1), dict(col_fused=3)):
+    for bad in (dict(row_overlap=2), dict(row_ctas_per_sm=-1), dict(wave_mib=0), dict(col_fused=1), dict(col_fused=3),
+                dict(row_variant=2)):
         with pytest.raises(ocean_lib.OceanError):
             ocean_lib.set_tuning(512, **bad)
     assert ocean_lib.get_tuning(512) == old
@@ -270,3 +272,7 @@ def test_tuning_table_round_trip(ocean_lib):
     old2 = ocean_lib.set_tuning(2048, col_fused=2)
     assert ocean_lib.get_tuning(2048)["col_fused"] == 0
     ocean_lib.set_tuning(2048, **old2)
+    # below N = 512 only the every-warp row pass exists
+    old3 = ocean_lib.set_tuning(256, row_variant=0)
+    assert ocean_lib.get_tuning(256)["row_variant"] == 1
+    ocean_lib.set_tuning(256, **old3)

@@ -374,3 +374,37 @@ def test_fused_column_kernel_matches_two_kernels(torch_cuda, ocean_lib, N):
             for k in range(3):
                 assert np.array_equal(a[k], b[k]), fused
             assert rel_l2(b[3], a[3]) < 1e-6, fused
+
+
+@pytest.mark.parametrize("N", [512, 1024, 2048])
+def test_row_pass_variants_agree(torch_cuda, ocean_lib, oracle_mod, N):
+    """The two row-pass kernels the tuning chooses between at N >= 512 (the
+    warp-specialised k_row_ws, and k_row_pass with every warp on the prepass
+    and then its line) give the same frames, back to back on one handle,
+    and the every-warp one matches the FP64 oracle."""
+    torch = torch_cuda
+    d = P.c2(N)
+    dev = torch.device("cuda")
+    times = [0.25, 9.5, 1.0e5]
+    outs = {}
+    saved = ocean_lib.get_tuning(N)
+    try:
+        for variant in (0, 1):
+            ocean_lib.set_tuning(N, row_variant=variant)
+            assert ocean_lib.get_tuning(N)["row_variant"] == variant
+            with ocean_lib.Ocean(P.lib_params(d), seed=d["seed"]) as oc:
+                sets = [[torch.empty((N, N), device=dev) for _ in range(3)] + [torch.empty((N, N, 4), device=dev)]
+                        for _ in times]
+                for t, o in zip(times, sets):
+                    oc.update(t, *o)
+                torch.cuda.synchronize()
+                oc.device_status()
+                outs[variant] = [[x.cpu().numpy() for x in o] for o in sets]
+    finally:
+        ocean_lib.set_tuning(N, **saved)
+    for a, b in zip(outs[0], outs[1]):
+        for k in range(4):
+            assert rel_l2(b[k], a[k]) < 1e-6, k
+    op = P.oracle_params(d)
+    ref = oracle_mod.update(op, oracle_mod.h0(op, oracle_mod.noise(d["seed"], N)), times[1])
+    _check({"dx": outs[1][1][0], "dy": outs[1][1][1], "dz": outs[1][1][2], "nj": outs[1][1][3]}, ref)
