@@ -2,8 +2,8 @@
 //
 // A "line" is one N-point transform (one row or one column of a spectrum).
 // It is computed by G = N/R1 cooperating threads, each holding R1 complex
-// values in registers, as a Stockham auto-sort FFT of 2 or 3 passes
-// (radices R1, R2[, R3]; every radix <= 32 and dividing R1):
+// values in registers, as a Stockham auto-sort FFT of 2 to 4 passes
+// (radices R1, R2[, R3[, R4]]; every radix <= 32 and dividing R1):
 //
 //   pass 1 (radix R1, Ns = 1):   thread t owns inputs x[t + r*N/R1], r < R1,
 //                                so a line is loaded with unit stride across
@@ -137,17 +137,20 @@ __device__ __forceinline__ void dft(float2* v)
     }
 }
 
-template <int N_, int R1_, int R2_, int R3_ = 1>
+template <int N_, int R1_, int R2_, int R3_ = 1, int R4_ = 1>
 struct LineCfg {
     static constexpr int N    = N_;
     static constexpr int R1   = R1_;
     static constexpr int R2   = R2_;
     static constexpr int R3   = R3_;
+    static constexpr int R4   = R4_;
     static constexpr int G    = N / R1;      // threads per line
     static constexpr int E    = R1;          // complex values per thread
     static constexpr int NPAD = N + N / R1;  // padded exchange-buffer length
-    static_assert(R1 * R2 * R3 == N, "radices must multiply to N");
-    static_assert(R1 <= 32 && R2 <= R1 && R3 <= R1 && R1 % R2 == 0 && R1 % R3 == 0, "bad radices");
+    static_assert(R1 * R2 * R3 * R4 == N, "radices must multiply to N");
+    static_assert(R1 <= 32 && R2 <= R1 && R3 <= R1 && R4 <= R1 && R1 % R2 == 0 && R1 % R3 == 0 && R1 % R4 == 0,
+                  "bad radices");
+    static_assert(R4 == 1 || R3 > 1, "a fourth pass needs a third");
     __device__ __forceinline__ static int pad(int i) { return i + i / R1; }
 };
 
@@ -164,16 +167,21 @@ template <> struct LineFor<1024> { using type = LineCfg<1024, 16, 16, 4>; };
 template <> struct LineFor<2048> { using type = LineCfg<2048, 16, 16, 8>; };
 
 // Inter-pass twiddles of a decomposition, laid out so that the threads of a
-// warp read consecutive entries (no bank conflicts, no index arithmetic):
-//   pass 2: T[r*R1 + k]          = W_N^(k*r*N/(R1*R2)),  k < R1,    r < R2;
-//   pass 3: T[P2 + r*R1*R2 + k]  = W_N^(k*r),            k < R1*R2, r < R3;
+// warp read consecutive entries (no bank conflicts, no index arithmetic).
+// Pass p (p = 2, 3, 4) has NS = R1 ... R(p-1) butterfly strides and radix R =
+// Rp; its segment holds T[off + r*NS + k] = W_N^(k*r*N/(NS*R)), k < NS,
+// r < R:
+//   pass 2: off 0,        NS = R1;
+//   pass 3: off P2,       NS = R1*R2;
+//   pass 4: off P2 + P3,  NS = R1*R2*R3.
 // W_N = exp(+2*pi*i/N), rounded from double (conjugated in the transform for
 // SIGN < 0).  Built once per size by launch_twiddles().
 template <class C>
 struct TwPlan {
     static constexpr int P2  = C::R1 * C::R2;
     static constexpr int P3  = C::R3 > 1 ? C::R1 * C::R2 * C::R3 : 0;
-    static constexpr int LEN = P2 + P3;
+    static constexpr int P4  = C::R4 > 1 ? C::R1 * C::R2 * C::R3 * C::R4 : 0;
+    static constexpr int LEN = P2 + P3 + P4;
 };
 
 // Barrier among the threads of one line.  With NAMED, lines of >= 32 threads
@@ -192,10 +200,11 @@ __device__ __forceinline__ void line_sync(int li)
 
 // One exchange + pass: the registers hold the outputs of a pass of radix RP
 // with stride NSP; they are written to `buf`, re-read as the inputs of a pass
-// of radix RN (stride NSP*RP), twiddled and transformed.  Contains two line
-// barriers (see line_sync); without TAIL_SYNC only the first, and a thread may
-// then leave while others of its line still read `buf`.
-template <class C, int RP, int NSP, int RN, int SIGN, bool NAMED, bool TAIL_SYNC = true>
+// of radix RN (stride NSP*RP), twiddled (plan segment at TWOFF) and
+// transformed.  Contains two line barriers (see line_sync); without TAIL_SYNC
+// only the first, and a thread may then leave while others of its line still
+// read `buf`.
+template <class C, int RP, int NSP, int RN, int TWOFF, int SIGN, bool NAMED, bool TAIL_SYNC = true>
 __device__ __forceinline__ void stockham_pass(float2* v, float2* buf, const float2* tw, int t, bool active, int li)
 {
     constexpr int N   = C::N;
@@ -221,8 +230,7 @@ __device__ __forceinline__ void stockham_pass(float2* v, float2* buf, const floa
     if constexpr (TAIL_SYNC) line_sync<C, NAMED>(li);
     if (!active) return;
     // twiddle plan of this pass: entry r*NSN + k
-    const float2* T = NSP == 1 ? tw : tw + TwPlan<C>::P2;
-    static_assert(NSP == 1 ? NSN == C::R1 : NSN == C::R1 * C::R2, "plan layout");
+    const float2* T = tw + TWOFF;
 #pragma unroll
     for (int b = 0; b < C::R1 / RN; ++b) {
         const int j = t + b * C::G;
@@ -250,14 +258,19 @@ __device__ __forceinline__ void stockham_pass(float2* v, float2* buf, const floa
 template <class C, int SIGN, bool NAMED = true, bool TAIL_SYNC = true>
 __device__ __forceinline__ void line_fft(float2* v, float2* buf, const float2* tw, int t, int li, bool active = true)
 {
+    using TP = TwPlan<C>;
     if (active) dft<C::R1, SIGN>(v);
-    stockham_pass<C, C::R1, 1, C::R2, SIGN, NAMED, (C::R3 > 1) || TAIL_SYNC>(v, buf, tw, t, active, li);
-    if constexpr (C::R3 > 1) stockham_pass<C, C::R2, C::R1, C::R3, SIGN, NAMED, TAIL_SYNC>(v, buf, tw, t, active, li);
+    stockham_pass<C, C::R1, 1, C::R2, 0, SIGN, NAMED, (C::R3 > 1) || TAIL_SYNC>(v, buf, tw, t, active, li);
+    if constexpr (C::R3 > 1)
+        stockham_pass<C, C::R2, C::R1, C::R3, TP::P2, SIGN, NAMED, (C::R4 > 1) || TAIL_SYNC>(v, buf, tw, t, active, li);
+    if constexpr (C::R4 > 1)
+        stockham_pass<C, C::R3, C::R1 * C::R2, C::R4, TP::P2 + TP::P3, SIGN, NAMED, TAIL_SYNC>(v, buf, tw, t, active,
+                                                                                             li);
 }
 
 template <class C>
 struct LineOut {
-    static constexpr int RL = C::R3 > 1 ? C::R3 : C::R2;
+    static constexpr int RL = C::R4 > 1 ? C::R4 : (C::R3 > 1 ? C::R3 : C::R2);
     static constexpr int B  = C::R1 / RL;          // butterflies per thread in the last pass
     static constexpr int NS = C::N / RL;           // output stride of the last pass
     // position of register e = b*RL + r after line_fft

@@ -402,13 +402,24 @@ __global__ void __launch_bounds__(RowCfg<N, FROM_H0>::THREADS, RowCfg<N, FROM_H0
 // barrier operations whatever happens, so a timed-out copy wait (flagged in
 // the status word) never leaves a warp waiting.
 // ---------------------------------------------------------------------------
-template <int N, bool FROM_H0>
+// Row-line decompositions of the warp-specialised row pass: V = 0 the
+// 16-point-first LineFor lines; V = 2 8-point-first lines (one more exchange,
+// half the values per thread, twice the threads per line), whose twiddle plan
+// follows the row and column plans in the table (k_twiddles).
+template <int N> struct ColLineFor;   // the column decompositions (below), whose plan precedes this one
+template <int N, int V> struct RowLine { using type = typename LineFor<N>::type; };
+template <> struct RowLine<512, 2> { using type = LineCfg<512, 8, 8, 8>; };
+template <> struct RowLine<1024, 2> { using type = LineCfg<1024, 8, 8, 4, 4>; };
+template <> struct RowLine<2048, 2> { using type = LineCfg<2048, 8, 8, 8, 4>; };
+
+template <int N, bool FROM_H0, int V = 0>
 struct RowWsCfg {
-    using L = typename LineFor<N>::type;
+    using L = typename RowLine<N, V>::type;
     static_assert(L::G >= 32 && L::G % 32 == 0, "lines of whole warps");
     static constexpr int FFT_THREADS = 3 * L::G;
     static constexpr int PRE_THREADS = N >= 2048 ? 256 : 128;
     static constexpr int THREADS     = FFT_THREADS + PRE_THREADS;
+    static_assert(THREADS <= 1024, "one CTA");
     static constexpr int ITEMS       = N / 2 + 1;   // row pairs per tile
     static constexpr int STAGES      = 2;
     static constexpr int EW          = FROM_H0 ? 2 : 1;
@@ -416,7 +427,15 @@ struct RowWsCfg {
     static constexpr size_t BUF      = (size_t)3 * L::NPAD;   // one job's three line buffers
     static constexpr int    TW       = TwPlan<L>::LEN;
     static constexpr size_t SMEM     = sizeof(float2) * (TW + RING + 2 * BUF) + 128;
-    static constexpr int MINB        = 65536 / (THREADS * 96) < 1 ? 1 : 65536 / (THREADS * 96);
+    // register budget per thread the residency is set for: 96 for the
+    // 16-point-first lines, 64 for the 8-point-first ones (8 values per thread)
+    static constexpr int REGS        = V == 2 ? 64 : 96;
+    static constexpr int MINB        = 65536 / (THREADS * REGS) < 1 ? 1 : 65536 / (THREADS * REGS);
+    // offset of this decomposition's twiddle plan in the table (float2 units)
+    static constexpr int TWOFF = V == 2 ? TwPlan<typename LineFor<N>::type>::LEN +
+                                              TwPlan<typename ColLineFor<N>::type>::LEN
+                                        : 0;
+    static_assert(TWOFF % 2 == 0 && TW % 2 == 0, "16-byte twiddle copies");
     static constexpr int BAR_FULL = 4, BAR_EMPTY = 6, BAR_PRE = 8, BAR_TW = 9;   // named barriers (lines use 1..3)
 };
 
@@ -429,10 +448,10 @@ __device__ __forceinline__ void named_arrive(int id, int count)
     asm volatile("bar.arrive %0, %1;" ::"r"(id), "r"(count) : "memory");
 }
 
-template <int N, bool MULTI, bool FROM_H0>
+template <int N, bool MULTI, bool FROM_H0, int V>
 __device__ __forceinline__ void row_ws_body(const RowArgs& a)
 {
-    using WC = RowWsCfg<N, FROM_H0>;
+    using WC = RowWsCfg<N, FROM_H0, V>;
     using L  = typename WC::L;
     extern __shared__ unsigned char smem_raw[];
     float2* smem = align_smem(smem_raw);
@@ -458,7 +477,7 @@ __device__ __forceinline__ void row_ws_body(const RowArgs& a)
             row_issue<N, FROM_H0>(a, ring + (size_t)s * 2 * N * WC::EW, &bars[s], item);
             if (s == 0) {
                 mbar_arrive_expect_tx(&bar_tw, WC::TW * sizeof(float2));
-                bulk_g2s(tw_s, a.tw, WC::TW * sizeof(float2), &bar_tw);
+                bulk_g2s(tw_s, a.tw + WC::TWOFF, WC::TW * sizeof(float2), &bar_tw);
             }
         }
         wait_ok = 1;
@@ -574,11 +593,11 @@ __device__ __forceinline__ void row_ws_body(const RowArgs& a)
 
 // Launched as k_row_pass is (see there): waits for the stream's previous
 // kernel at its end, or first with wait_first.
-template <int N, bool MULTI, bool FROM_H0>
-__global__ void __launch_bounds__(RowWsCfg<N, FROM_H0>::THREADS, RowWsCfg<N, FROM_H0>::MINB) k_row_ws(RowArgs a)
+template <int N, bool MULTI, bool FROM_H0, int V = 0>
+__global__ void __launch_bounds__(RowWsCfg<N, FROM_H0, V>::THREADS, RowWsCfg<N, FROM_H0, V>::MINB) k_row_ws(RowArgs a)
 {
     if (a.wait_first) pdl_wait_prior();
-    row_ws_body<N, MULTI, FROM_H0>(a);
+    row_ws_body<N, MULTI, FROM_H0, V>(a);
     pdl_wait_prior();
 }
 
@@ -1010,14 +1029,17 @@ __global__ void __launch_bounds__(FusedCfg<N, P>::THREADS, P == 2 ? 2 : 1) k_col
 template <class C>
 __device__ float2 plan_entry(int i)
 {
-    constexpr int P2 = TwPlan<C>::P2;
-    long e;                                                   // exponent of W_N
-    if (i < P2) {
-        e = (long)(i % C::R1) * (i / C::R1) * (C::N / (C::R1 * C::R2));
+    // segment of entry i (TwPlan): pass 2, 3 or 4 with butterfly stride NS and radix R
+    using TP = TwPlan<C>;
+    int ns, r;
+    if (i < TP::P2) {
+        ns = C::R1, r = C::R2;
+    } else if (i < TP::P2 + TP::P3) {
+        i -= TP::P2, ns = C::R1 * C::R2, r = C::R3;
     } else {
-        i -= P2;
-        e = (long)(i % P2) * (i / P2);
+        i -= TP::P2 + TP::P3, ns = C::R1 * C::R2 * C::R3, r = C::R4;
     }
+    const long e = (long)(i % ns) * (i / ns) * (C::N / (ns * r));   // exponent of W_N
     double sn, cs;
     sincospi(2.0 * (double)(e % C::N) / (double)C::N, &sn, &cs);
     return make_float2((float)cs, (float)sn);
@@ -1028,15 +1050,19 @@ __global__ void k_twiddles(float2* __restrict__ tw)
 {
     using LR = typename LineFor<N>::type;
     using LC = typename ColLineFor<N>::type;
+    using LV = typename RowLine<N, 2>::type;
+    constexpr int A = TwPlan<LR>::LEN, B = A + TwPlan<LC>::LEN, C = B + TwPlan<LV>::LEN;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i < TwPlan<LR>::LEN) tw[i] = plan_entry<LR>(i);
-    else if (i < TwPlan<LR>::LEN + TwPlan<LC>::LEN) tw[i] = plan_entry<LC>(i - TwPlan<LR>::LEN);
+    if (i < A) tw[i] = plan_entry<LR>(i);
+    else if (i < B) tw[i] = plan_entry<LC>(i - A);
+    else if (i < C) tw[i] = plan_entry<LV>(i - B);
 }
 
 template <int N>
 static size_t twiddle_len_n()
 {
-    return (size_t)TwPlan<typename LineFor<N>::type>::LEN + TwPlan<typename ColLineFor<N>::type>::LEN;
+    return (size_t)TwPlan<typename LineFor<N>::type>::LEN + TwPlan<typename ColLineFor<N>::type>::LEN +
+           TwPlan<typename RowLine<N, 2>::type>::LEN;
 }
 
 // ---------------------------------------------------------------------------
@@ -1096,18 +1122,18 @@ static cudaError_t row_pass_nm(const RowArgs& a, cudaStream_t s)
                       s, true, a);
 }
 
-template <int N, bool MULTI, bool FROM_H0>
+template <int N, bool MULTI, bool FROM_H0, int V = 0>
 static cudaError_t row_ws_nm(const RowArgs& a, cudaStream_t s)
 {
-    using WC = RowWsCfg<N, FROM_H0>;
+    using WC = RowWsCfg<N, FROM_H0, V>;
     static PerDevice cache;   // resident CTAs per SM on each device, found on its first launch
     int per_sm = 0, grid = 0;
-    cudaError_t e = persistent_setup(cache, k_row_ws<N, MULTI, FROM_H0>, WC::THREADS, WC::SMEM, &per_sm);
+    cudaError_t e = persistent_setup(cache, k_row_ws<N, MULTI, FROM_H0, V>, WC::THREADS, WC::SMEM, &per_sm);
     if (e != cudaSuccess || (e = persistent_grid(per_sm, tuning_for(N).row_ctas_per_sm, &grid)) != cudaSuccess)
         return e;
     const int items = a.tiles * WC::ITEMS;
-    return launch_pdl(k_row_ws<N, MULTI, FROM_H0>, dim3(grid < items ? grid : items), dim3(WC::THREADS), WC::SMEM, s,
-                      true, a);
+    return launch_pdl(k_row_ws<N, MULTI, FROM_H0, V>, dim3(grid < items ? grid : items), dim3(WC::THREADS), WC::SMEM,
+                      s, true, a);
 }
 
 template <int N>
@@ -1120,8 +1146,11 @@ static cudaError_t row_pass_n(const RowArgs& a, cudaStream_t s)
             if constexpr (N <= 1024) return row_ws_nm<N, false, true>(a, s);
             else return cudaErrorInvalidValue;                // its staged h0 rows would not fit
         }
-        if (tuning_for(N).row_variant == 1)                   // every warp runs the prepass and its line
+        const int variant = tuning_for(N).row_variant;
+        if (variant == 1)                                     // every warp runs the prepass and its line
             return single ? row_pass_nm<N, false, false>(a, s) : row_pass_nm<N, true, false>(a, s);
+        if (variant == 2)                                     // warp-specialised, 8-point-first lines
+            return single ? row_ws_nm<N, false, false, 2>(a, s) : row_ws_nm<N, true, false, 2>(a, s);
         return single ? row_ws_nm<N, false, false>(a, s) : row_ws_nm<N, true, false>(a, s);
     } else {
         if (!a.spec) return row_pass_nm<N, false, true>(a, s);

@@ -37,7 +37,7 @@ static_assert(kStaticInterLen * 8 + kStaticTmapLen * 4 == 25190400, "documented 
 // table, device status word.
 static __device__ __align__(256) float2   g_static_inter[kStaticInterLen];
 static __device__ __align__(256) float    g_static_tmap[kStaticTmapLen];
-constexpr size_t kStaticTwLen    = 2560;   // twiddle plans of N = 1024, the largest needed
+constexpr size_t kStaticTwLen    = 4096;   // twiddle plans of N = 1024 (3,648), the largest needed
 static __device__ __align__(256) float2   g_static_tw[kStaticTwLen];
 static __device__ __align__(256) unsigned g_static_status;
 

@@ -90,7 +90,7 @@ extern "C" int ocean_set_tuning(int32_t N, const ocean_tuning* cfg)
     if (i < 0) return fail(OCEAN_ERR_INVALID, "no tuning entry for N = " + std::to_string(N));
     if ((cfg->row_overlap != 0 && cfg->row_overlap != 1) || cfg->row_ctas_per_sm < 0 || cfg->row_ctas_per_sm > 32 ||
         cfg->wave_mib < 1 || cfg->wave_mib > 4096 || (cfg->col_fused != 0 && cfg->col_fused != 2 && cfg->col_fused != 4) ||
-        (cfg->row_variant != 0 && cfg->row_variant != 1))
+        cfg->row_variant < 0 || cfg->row_variant > 2)
         return fail(OCEAN_ERR_INVALID, "tuning values out of range");
     Live& l = live()[i];
     l.row_overlap.store(cfg->row_overlap);

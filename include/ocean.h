@@ -380,7 +380,9 @@ typedef struct ocean_tuning {
                                  column-major maps, as ocean_update_columns and ocean_update_outputs do        */
     int32_t row_variant;      /* N >= 512: 0 = warp-specialised row pass (prepass warps feed transform warps),
                                  1 = every warp runs the prepass and then its line FFT (one row pair per CTA
-                                 at N = 1024); below 512 only the latter exists and this reads 1            */
+                                 at N = 1024), 2 = warp-specialised with 8-point-first lines (half the
+                                 registers per thread, one more exchange); below 512 only 1 exists and this
+                                 reads 1                                                                     */
 } ocean_tuning;
 
 OCEAN_API int ocean_get_tuning(int32_t N, ocean_tuning* out);

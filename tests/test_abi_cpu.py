@@ -261,7 +261,7 @@ def test_tuning_table_round_trip(ocean_lib):
     ocean_lib.set_tuning(512, **old)
     assert ocean_lib.get_tuning(512) == old
     for bad in (dict(row_overlap=2), dict(row_ctas_per_sm=-1), dict(wave_mib=0), dict(col_fused=1), dict(col_fused=3),
-                dict(row_variant=2)):
+                dict(row_variant=3)):
         with pytest.raises(ocean_lib.OceanError):
             ocean_lib.set_tuning(512, **bad)
     assert ocean_lib.get_tuning(512) == old

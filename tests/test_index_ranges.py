@@ -17,9 +17,10 @@ SIZES = sorted(LINE_FOR)
 
 
 def line(N, R):
-    R1, R2, R3 = R
+    R1, R2, R3 = R[:3]
+    R4 = R[3] if len(R) > 3 else 1
     G, E = N // R1, R1
-    RL = R3 if R3 > 1 else R2
+    RL = R4 if R4 > 1 else (R3 if R3 > 1 else R2)
     NS = N // RL
     t = np.arange(G)[:, None]
     e = np.arange(E)[None, :]
@@ -38,9 +39,14 @@ def inter_index(N, f, x, y):
     return ((f * (N // 2) + (x >> 1)) * inter_rows(N) + y) * 2 + (x & 1)
 
 
-@pytest.mark.parametrize("N", SIZES)
-def test_row_pass_stores_cover_the_intermediate_once(N):
-    G, E, R1, pos, t = line(N, LINE_FOR[N])
+# the 8-point-first row lines of the warp-specialised row pass (RowLine<N, 2>)
+ROW_LINE_V2 = {512: (8, 8, 8), 1024: (8, 8, 4, 4), 2048: (8, 8, 8, 4)}
+ROW_CASES = [(N, LINE_FOR[N]) for N in SIZES] + sorted(ROW_LINE_V2.items())
+
+
+@pytest.mark.parametrize("N,R", ROW_CASES)
+def test_row_pass_stores_cover_the_intermediate_once(N, R):
+    G, E, R1, pos, t = line(N, R)
     H = inter_rows(N)
     x = t + pos                                                  # (G, E) output positions of a line
     assert np.array_equal(np.sort(x.ravel()), np.arange(N))

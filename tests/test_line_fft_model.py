@@ -15,19 +15,24 @@ its own, for both signs.
 import numpy as np
 import pytest
 
-# LineFor (rows, adjoint) and ColLineFor (k_col_fft): (N, R1, R2, R3)
-DECOMPS = sorted({(32, 8, 4, 1), (64, 8, 8, 1), (128, 16, 8, 1), (256, 16, 16, 1), (512, 16, 16, 2),
-                  (1024, 16, 16, 4), (2048, 16, 16, 8), (1024, 32, 32, 1), (2048, 32, 8, 8)})
+# LineFor (rows, adjoint), ColLineFor (k_col_fft) and the 8-point-first row
+# lines (RowLine<N, 2>): (N, R1, R2, R3, R4)
+DECOMPS = sorted({(32, 8, 4, 1, 1), (64, 8, 8, 1, 1), (128, 16, 8, 1, 1), (256, 16, 16, 1, 1),
+                  (512, 16, 16, 2, 1), (1024, 16, 16, 4, 1), (2048, 16, 16, 8, 1), (1024, 32, 32, 1, 1),
+                  (2048, 32, 8, 8, 1), (512, 8, 8, 8, 1), (1024, 8, 8, 4, 4), (2048, 8, 8, 8, 4)})
 
 
-def plan(N, R1, R2, R3):
-    """k_twiddles' plan: entry i < P2 is W_N^((i%R1)*(i/R1)*N/(R1*R2)); entry
-    P2 + i is W_N^((i%P2)*(i/P2)), W_N = exp(+2 pi i/N)."""
-    P2 = R1 * R2
-    P3 = R1 * R2 * R3 if R3 > 1 else 0
-    i = np.arange(P2 + P3)
-    e = np.where(i < P2, (i % R1) * (i // R1) * (N // (R1 * R2)), ((i - P2) % P2) * ((i - P2) // P2))
-    return np.exp(2j * np.pi * (e % N) / N)
+def plan(N, R1, R2, R3, R4=1):
+    """k_twiddles' plan (plan_entry): segment p (pass 2, 3, 4) with butterfly
+    stride NS and radix R holds W_N^(k*r*N/(NS*R)) at r*NS + k, W_N =
+    exp(+2 pi i/N)."""
+    segs = [(R1, R2)] + ([(R1 * R2, R3)] if R3 > 1 else []) + ([(R1 * R2 * R3, R4)] if R4 > 1 else [])
+    out = []
+    for ns, r in segs:
+        i = np.arange(ns * r)
+        e = (i % ns) * (i // ns) * (N // (ns * r))
+        out.append(np.exp(2j * np.pi * (e % N) / N))
+    return np.concatenate(out)
 
 
 def dft(v, sign):
@@ -61,16 +66,18 @@ def stockham_pass(v, N, R1, G, RP, NSP, RN, T, sign):
     return out
 
 
-def line_fft(x, N, R1, R2, R3, sign):
+def line_fft(x, N, R1, R2, R3, sign, R4=1):
     G = N // R1
-    tw = plan(N, R1, R2, R3)
+    tw = plan(N, R1, R2, R3, R4)
     t = np.arange(G)[:, None]
     v = x[t + np.arange(R1)[None, :] * G]                         # v[r] = x[t + r*G]
     v = dft(v, sign)
     v = stockham_pass(v, N, R1, G, R1, 1, R2, tw, sign)
     if R3 > 1:
         v = stockham_pass(v, N, R1, G, R2, R1, R3, tw[R1 * R2:], sign)
-    RL = R3 if R3 > 1 else R2
+    if R4 > 1:
+        v = stockham_pass(v, N, R1, G, R3, R1 * R2, R4, tw[R1 * R2 + R1 * R2 * R3:], sign)
+    RL = R4 if R4 > 1 else (R3 if R3 > 1 else R2)
     e = np.arange(R1)[None, :]
     pos = (t + (e // RL) * G) + (e % RL) * (N // RL)            # LineOut::pos(t, e)
     X = np.empty(N, complex)
@@ -79,12 +86,12 @@ def line_fft(x, N, R1, R2, R3, sign):
     return X
 
 
-@pytest.mark.parametrize("N,R1,R2,R3", DECOMPS)
+@pytest.mark.parametrize("N,R1,R2,R3,R4", DECOMPS)
 @pytest.mark.parametrize("sign", [+1, -1])
-def test_line_fft_matches_numpy(N, R1, R2, R3, sign):
+def test_line_fft_matches_numpy(N, R1, R2, R3, R4, sign):
     rng = np.random.default_rng(N + R1)
     x = rng.standard_normal(N) + 1j * rng.standard_normal(N)
-    got = line_fft(x, N, R1, R2, R3, sign)
+    got = line_fft(x, N, R1, R2, R3, sign, R4)
     ref = np.fft.ifft(x) * N if sign > 0 else np.fft.fft(x)
     assert np.abs(got - ref).max() < 1e-9 * np.abs(ref).max()
 
@@ -92,6 +99,7 @@ def test_line_fft_matches_numpy(N, R1, R2, R3, sign):
 def test_decompositions_are_valid():
     """The static_asserts of LineCfg: radices multiply to N, each <= 32 and
     dividing R1."""
-    for N, R1, R2, R3 in DECOMPS:
-        assert R1 * R2 * R3 == N
-        assert R1 <= 32 and R2 <= R1 and R3 <= R1 and R1 % R2 == 0 and R1 % R3 == 0
+    for N, R1, R2, R3, R4 in DECOMPS:
+        assert R1 * R2 * R3 * R4 == N
+        assert R1 <= 32 and max(R2, R3, R4) <= R1 and R1 % R2 == 0 and R1 % R3 == 0 and R1 % R4 == 0
+        assert R4 == 1 or R3 > 1

@@ -378,10 +378,10 @@ def test_fused_column_kernel_matches_two_kernels(torch_cuda, ocean_lib, N):
 
 @pytest.mark.parametrize("N", [512, 1024, 2048])
 def test_row_pass_variants_agree(torch_cuda, ocean_lib, oracle_mod, N):
-    """The two row-pass kernels the tuning chooses between at N >= 512 (the
-    warp-specialised k_row_ws, and k_row_pass with every warp on the prepass
-    and then its line) give the same frames, back to back on one handle,
-    and the every-warp one matches the FP64 oracle."""
+    """The row-pass kernels the tuning chooses between at N >= 512 (the
+    warp-specialised k_row_ws with 16- or 8-point-first lines, and k_row_pass
+    with every warp on the prepass and then its line) give the same frames,
+    back to back on one handle, and match the FP64 oracle."""
     torch = torch_cuda
     d = P.c2(N)
     dev = torch.device("cuda")
@@ -389,7 +389,7 @@ def test_row_pass_variants_agree(torch_cuda, ocean_lib, oracle_mod, N):
     outs = {}
     saved = ocean_lib.get_tuning(N)
     try:
-        for variant in (0, 1):
+        for variant in (0, 1, 2):
             ocean_lib.set_tuning(N, row_variant=variant)
             assert ocean_lib.get_tuning(N)["row_variant"] == variant
             with ocean_lib.Ocean(P.lib_params(d), seed=d["seed"]) as oc:
@@ -402,9 +402,12 @@ def test_row_pass_variants_agree(torch_cuda, ocean_lib, oracle_mod, N):
                 outs[variant] = [[x.cpu().numpy() for x in o] for o in sets]
     finally:
         ocean_lib.set_tuning(N, **saved)
-    for a, b in zip(outs[0], outs[1]):
-        for k in range(4):
-            assert rel_l2(b[k], a[k]) < 1e-6, k
+    for variant in (1, 2):
+        for a, b in zip(outs[0], outs[variant]):
+            for k in range(4):
+                assert rel_l2(b[k], a[k]) < 1e-6, (variant, k)
     op = P.oracle_params(d)
     ref = oracle_mod.update(op, oracle_mod.h0(op, oracle_mod.noise(d["seed"], N)), times[1])
-    _check({"dx": outs[1][1][0], "dy": outs[1][1][1], "dz": outs[1][1][2], "nj": outs[1][1][3]}, ref)
+    for variant in (1, 2):
+        _check({"dx": outs[variant][1][0], "dy": outs[variant][1][1], "dz": outs[variant][1][2],
+                "nj": outs[variant][1][3]}, ref)
