@@ -284,12 +284,13 @@ def run_gpu(args, world, rank, local):
             for i in range(LEAD_IN):
                 j = (RING - LEAD_IN + i) % RING
                 ring[j].update((args.warmup - LEAD_IN + i) / 60.0, *ring_out[j], stream=stream)
+            per_frame = 2 if og.get_tuning(N)["col_fused"] else 3   # kernels per frame
             e0.record(stream)
             for i in range(K):
                 j = i % RING
                 ring[j].update((args.warmup + i) / 60.0, *ring_out[j], stream=stream)
-                launches += 2 if og.get_tuning(N)["col_fused"] else 3
             e1.record(stream)
+            launches += per_frame * K
             torch.cuda.synchronize()
             wall = time.perf_counter() - wall0
             if world > 1:
