@@ -405,9 +405,12 @@ __global__ void __launch_bounds__(RowCfg<N, FROM_H0>::THREADS, RowCfg<N, FROM_H0
 // Row-line decompositions of the warp-specialised row pass: V = 0 the
 // 16-point-first LineFor lines; V = 2 8-point-first lines (one more exchange,
 // half the values per thread, twice the threads per line), whose twiddle plan
-// follows the row and column plans in the table (k_twiddles).
+// follows the row and column plans in the table (k_twiddles); V = 3 (N = 1024)
+// the column lines, 32 x 32 (one warp per line, one exchange), which use the
+// column plan.
 template <int N> struct ColLineFor;   // the column decompositions (below), whose plan precedes this one
 template <int N, int V> struct RowLine { using type = typename LineFor<N>::type; };
+template <> struct RowLine<1024, 3> { using type = LineCfg<1024, 32, 32>; };
 template <> struct RowLine<512, 2> { using type = LineCfg<512, 8, 8, 8>; };
 template <> struct RowLine<1024, 2> { using type = LineCfg<1024, 8, 8, 4, 4>; };
 template <> struct RowLine<2048, 2> { using type = LineCfg<2048, 8, 8, 8, 4>; };
@@ -429,12 +432,13 @@ struct RowWsCfg {
     static constexpr size_t SMEM     = sizeof(float2) * (TW + RING + 2 * BUF) + 128;
     // register budget per thread the residency is set for: 96 for the
     // 16-point-first lines, 64 for the 8-point-first ones (8 values per thread)
-    static constexpr int REGS        = V == 2 ? 64 : 96;
+    static constexpr int REGS        = V == 2 ? 64 : (V == 3 ? 128 : 96);
     static constexpr int MINB        = 65536 / (THREADS * REGS) < 1 ? 1 : 65536 / (THREADS * REGS);
     // offset of this decomposition's twiddle plan in the table (float2 units)
-    static constexpr int TWOFF = V == 2 ? TwPlan<typename LineFor<N>::type>::LEN +
-                                              TwPlan<typename ColLineFor<N>::type>::LEN
-                                        : 0;
+    static constexpr int TWOFF = V == 2   ? TwPlan<typename LineFor<N>::type>::LEN +
+                                                TwPlan<typename ColLineFor<N>::type>::LEN
+                                 : V == 3 ? TwPlan<typename LineFor<N>::type>::LEN   // the column plan
+                                          : 0;
     static_assert(TWOFF % 2 == 0 && TW % 2 == 0, "16-byte twiddle copies");
     static constexpr int BAR_FULL = 4, BAR_EMPTY = 6, BAR_PRE = 8, BAR_TW = 9;   // named barriers (lines use 1..3)
 };
@@ -1151,6 +1155,9 @@ static cudaError_t row_pass_n(const RowArgs& a, cudaStream_t s)
             return single ? row_pass_nm<N, false, false>(a, s) : row_pass_nm<N, true, false>(a, s);
         if (variant == 2)                                     // warp-specialised, 8-point-first lines
             return single ? row_ws_nm<N, false, false, 2>(a, s) : row_ws_nm<N, true, false, 2>(a, s);
+        if constexpr (N == 1024)
+            if (variant == 3)                                 // warp-specialised, 32 x 32 lines
+                return single ? row_ws_nm<N, false, false, 3>(a, s) : row_ws_nm<N, true, false, 3>(a, s);
         return single ? row_ws_nm<N, false, false>(a, s) : row_ws_nm<N, true, false>(a, s);
     } else {
         if (!a.spec) return row_pass_nm<N, false, true>(a, s);

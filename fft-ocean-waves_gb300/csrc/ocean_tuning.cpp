@@ -44,6 +44,15 @@ Live* live()
     return table;
 }
 
+// The row-pass variants that exist for size N: below 512 only the every-warp
+// pass (1); variant 3 (32 x 32 lines) at N = 1024 only, elsewhere it reads 0.
+int row_variant_for(int N, int v)
+{
+    if (N < 512) return 1;
+    if (v == 3 && N != 1024) return 0;
+    return v;
+}
+
 int slot(int N)
 {
     for (int i = 0; i < kSizes; ++i)
@@ -63,7 +72,7 @@ Tuning tuning_for(int N)
     return Tuning{l.row_overlap.load(std::memory_order_relaxed), l.row_ctas_per_sm.load(std::memory_order_relaxed),
                   l.wave_mib.load(std::memory_order_relaxed),
                   ocean::col_fused_available(N) ? l.col_fused.load(std::memory_order_relaxed) : 0,
-                  N >= 512 ? l.row_variant.load(std::memory_order_relaxed) : 1};
+                  row_variant_for(N, l.row_variant.load(std::memory_order_relaxed))};
 }
 
 }  // namespace ocean
@@ -90,7 +99,7 @@ extern "C" int ocean_set_tuning(int32_t N, const ocean_tuning* cfg)
     if (i < 0) return fail(OCEAN_ERR_INVALID, "no tuning entry for N = " + std::to_string(N));
     if ((cfg->row_overlap != 0 && cfg->row_overlap != 1) || cfg->row_ctas_per_sm < 0 || cfg->row_ctas_per_sm > 32 ||
         cfg->wave_mib < 1 || cfg->wave_mib > 4096 || (cfg->col_fused != 0 && cfg->col_fused != 2 && cfg->col_fused != 4) ||
-        cfg->row_variant < 0 || cfg->row_variant > 2)
+        cfg->row_variant < 0 || cfg->row_variant > 3)
         return fail(OCEAN_ERR_INVALID, "tuning values out of range");
     Live& l = live()[i];
     l.row_overlap.store(cfg->row_overlap);

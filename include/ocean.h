@@ -381,7 +381,8 @@ typedef struct ocean_tuning {
     int32_t row_variant;      /* N >= 512: 0 = warp-specialised row pass (prepass warps feed transform warps),
                                  1 = every warp runs the prepass and then its line FFT (one row pair per CTA
                                  at N = 1024), 2 = warp-specialised with 8-point-first lines (half the
-                                 registers per thread, one more exchange); below 512 only 1 exists and this
+                                 registers per thread, one more exchange), 3 = warp-specialised with 32 x 32
+                                 lines (N = 1024 only; reads 0 elsewhere); below 512 only 1 exists and this
                                  reads 1                                                                     */
 } ocean_tuning;
 

@@ -41,7 +41,7 @@ def inter_index(N, f, x, y):
 
 # the 8-point-first row lines of the warp-specialised row pass (RowLine<N, 2>)
 ROW_LINE_V2 = {512: (8, 8, 8), 1024: (8, 8, 4, 4), 2048: (8, 8, 8, 4)}
-ROW_CASES = [(N, LINE_FOR[N]) for N in SIZES] + sorted(ROW_LINE_V2.items())
+ROW_CASES = [(N, LINE_FOR[N]) for N in SIZES] + sorted(ROW_LINE_V2.items()) + [(1024, (32, 32, 1))]
 
 
 @pytest.mark.parametrize("N,R", ROW_CASES)
