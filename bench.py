@@ -64,8 +64,10 @@ KERNEL_BYTES = {"k_row_pass": 40, "k_row_ws": 40, "k_col_fft": 24, "k_col_out": 
 
 
 def row_kernel(N):
-    """The row stage's kernel: warp-specialised where a line is whole warps."""
-    return "k_row_ws" if N >= 512 else "k_row_pass"
+    """The row stage's kernel: warp-specialised where a line is whole warps
+    and the tuning keeps that variant, else the every-warp pass."""
+    import ocean_gb300 as og
+    return "k_row_ws" if N >= 512 and og.get_tuning(N)["row_variant"] != 1 else "k_row_pass"
 
 
 def c2_params(N):
