@@ -61,13 +61,16 @@ BYTES_PER_TEXEL = 92            # algorithmic bytes per texel per frame
 # the intermediate (24); columns read it (24); outputs write dx, dy, dz and
 # normal_j (28); the fused column kernel does both column stages (52).
 KERNEL_BYTES = {"k_row_pass": 40, "k_row_ws": 40, "k_col_fft": 24, "k_col_out": 28, "k_col_fused": 52}
+# The frame's compulsory I/O: h0 in (16) and the four maps out (28); the
+# intermediate round trip is left out (it can stay in L2).
+COMPULSORY_BYTES_PER_TEXEL = 44
 
 
 def row_kernel(N):
     """The row stage's kernel: warp-specialised where a line is whole warps
     and the tuning keeps that variant, else the every-warp pass."""
     import ocean_gb300 as og
-    return "k_row_ws" if N >= 512 and og.get_tuning(N)["row_variant"] != 1 else "k_row_pass"
+    return "k_row_ws" if N >= 512 and og.get_tuning(N)["row_variant"] not in (1, 4) else "k_row_pass"
 
 
 def c2_params(N):
@@ -456,6 +459,9 @@ def run_gpu(args, world, rank, local):
                      "algorithmic_bytes_per_launch": dom_bytes, "traffic": traffic},
         "roofline_frame": {"bytes_per_frame": BYTES_PER_TEXEL * N * N, "achieved": round(frame_gbs, 1),
                            "frac": round(frame_gbs / peak, 4)},
+        "roofline_compulsory": {"bytes_per_frame": COMPULSORY_BYTES_PER_TEXEL * N * N,
+                                "achieved": round(frame_gbs * COMPULSORY_BYTES_PER_TEXEL / BYTES_PER_TEXEL, 1),
+                                "frac": round(frame_gbs * COMPULSORY_BYTES_PER_TEXEL / BYTES_PER_TEXEL / peak, 4)},
         "isolated": {"value": round(world * K / iso_s, 1), "unit": "frames/s", "ms_per_frame": round(iso_ms, 5),
                      "frac": round(iso_gbs / peak, 4),
                      "how": "one frame at a time, L2 flushed before each, CUDA events around each frame"},

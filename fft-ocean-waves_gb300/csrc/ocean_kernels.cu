@@ -129,9 +129,22 @@ __device__ __forceinline__ float2 herm_diff(float2 d, float2 d2, float c, float 
 // -i * f * z
 __device__ __forceinline__ float2 mul_mi(float f, float2 z) { return make_float2(f * z.y, -f * z.x); }
 
-template <int N, bool FROM_H0>
+// Row-line decompositions of the row passes: V = 0 the
+// 16-point-first LineFor lines; V = 2 8-point-first lines (one more exchange,
+// half the values per thread, twice the threads per line), whose twiddle plan
+// follows the row and column plans in the table (k_twiddles); V = 3 (N = 1024)
+// the column lines, 32 x 32 (one warp per line, one exchange), which use the
+// column plan.  The every-warp row pass uses V = 0 or 3.
+template <int N> struct ColLineFor;   // the column decompositions (below), whose plan precedes this one
+template <int N, int V> struct RowLine { using type = typename LineFor<N>::type; };
+template <> struct RowLine<1024, 3> { using type = LineCfg<1024, 32, 32>; };
+template <> struct RowLine<512, 2> { using type = LineCfg<512, 8, 8, 8>; };
+template <> struct RowLine<1024, 2> { using type = LineCfg<1024, 8, 8, 4, 4>; };
+template <> struct RowLine<2048, 2> { using type = LineCfg<2048, 8, 8, 8, 4>; };
+
+template <int N, bool FROM_H0, int V = 0>
 struct RowCfg {
-    using L = typename LineFor<N>::type;
+    using L = typename RowLine<N, V>::type;
     static constexpr int PAIRS   = L::G >= 32 ? 1 : 32 / L::G;  // row pairs per work item
     static constexpr int LINES   = 3 * PAIRS;
     static constexpr int THREADS = LINES * L::G;
@@ -140,8 +153,10 @@ struct RowCfg {
     // spread over (almost) every CTA slot at once, and the other resident
     // CTAs hide a CTA's wait for its rows.
     static constexpr int STAGES  = 1;
-    // resident CTAs per SM the register budget is set for (<= 80 registers)
-    static constexpr int MINB    = 65536 / (THREADS * 80) < 1 ? 1 : (65536 / (THREADS * 80) > 8 ? 8 : 65536 / (THREADS * 80));
+    // resident CTAs per SM the register budget is set for: <= 80 registers,
+    // 128 for the 32 x 32 lines (32 values per thread)
+    static constexpr int REGS    = V == 3 ? 128 : 80;
+    static constexpr int MINB    = 65536 / (THREADS * REGS) < 1 ? 1 : (65536 / (THREADS * REGS) > 8 ? 8 : 65536 / (THREADS * REGS));
     static constexpr int EW      = FROM_H0 ? 2 : 1;   // float2 per staged mode (h0: float4, G: float2)
     // shared memory (float2 units): tw[N] | ring [STAGES][PAIRS][2 rows][N modes] |
     // line buffers [LINES][NPAD] (line inputs in natural order, then the FFT's exchanges)
@@ -150,6 +165,10 @@ struct RowCfg {
     static constexpr int    TW    = TwPlan<L>::LEN;
     static constexpr size_t SMEM  = sizeof(float2) * (TW + RING + WORK) + 128;   // + base alignment slack
     static constexpr uint32_t ROW_BYTES = (uint32_t)(N * EW * sizeof(float2));
+    // offset of the line decomposition's twiddle plan in the table (float2
+    // units): the 32 x 32 lines use the column plan, which follows the row plan
+    static constexpr int TWOFF = V == 3 ? TwPlan<typename LineFor<N>::type>::LEN : 0;
+    static_assert(TWOFF % 2 == 0 && TW % 2 == 0, "16-byte twiddle copies");
 };
 
 // Fetch the spectrum rows of work item `item` (tile item/ITEMS, row pairs
@@ -277,11 +296,12 @@ __device__ __forceinline__ void row_position(const RowArgs& a, const float2* row
 // unit instantiation keeps the per-element constants out of a runtime sample
 // loop, which the compiler would otherwise hoist into registers.  FROM_H0: the
 // ring holds h0 rows and G, D are formed on the fly (ocean_update_noalloc).
-template <int N, bool MULTI, bool FROM_H0>
+template <int N, bool MULTI, bool FROM_H0, int V>
 __device__ __forceinline__ void row_pass_body(const RowArgs& a)
 {
-    using RC = RowCfg<N, FROM_H0>;
+    using RC = RowCfg<N, FROM_H0, V>;
     using L  = typename RC::L;
+    static_assert(RC::PAIRS == RowCfg<N, FROM_H0>::PAIRS, "row_issue's item layout");
     extern __shared__ unsigned char smem_raw[];
     float2* smem = align_smem(smem_raw);
     float2* tw_s = smem;
@@ -302,7 +322,7 @@ __device__ __forceinline__ void row_pass_body(const RowArgs& a)
             if (item >= n_items) break;
             const uint32_t twb = s == 0 ? (uint32_t)(RC::TW * sizeof(float2)) : 0u;
             row_issue<N, FROM_H0>(a, ring + (size_t)s * RC::PAIRS * 2 * N * RC::EW, &bars[s], item, twb);
-            if (twb) bulk_g2s(tw_s, a.tw, twb, &bars[0]);
+            if (twb) bulk_g2s(tw_s, a.tw + RC::TWOFF, twb, &bars[0]);
         }
     }
     __syncthreads();
@@ -314,6 +334,23 @@ __device__ __forceinline__ void row_pass_body(const RowArgs& a)
     const int f  = li % 3;                                           // 0: Dx, 1: Dy, 2: Dz
     const int pl_line = li / 3;
     uint32_t phase_bits = 0;
+
+    // 32 x 32 lines (one row pair per item, 128 registers): the first item's
+    // phases, which do not depend on its rows, are computed while its rows
+    // arrive.  (Under the 80-register budget of the other lines they would
+    // spill.)
+    constexpr bool PRE = V == 3 && RC::PAIRS == 1;
+    constexpr int  PP  = PRE ? (N / 2 + RC::THREADS) / RC::THREADS : 1;   // positions per thread
+    float pc[PP], ps[PP], pr[PP];
+    if (PRE) {
+        const int item = blockIdx.x, tile = item / RC::ITEMS, yp = item % RC::ITEMS;
+        const FrameConsts fc = MULTI ? a.fcs[tile * a.S] : a.fc0;
+#pragma unroll
+        for (int k = 0; k < PP; ++k) {
+            const int x = tid + k * RC::THREADS;
+            if (x <= N / 2) row_phase<N>(x, yp, fc, pc[k], ps[k], pr[k]);
+        }
+    }
 
     for (int k = 0, item = blockIdx.x; item < n_items; ++k, item += gridDim.x) {
         const int s = k % RC::STAGES;
@@ -331,12 +368,21 @@ __device__ __forceinline__ void row_pass_body(const RowArgs& a)
             // pairs (x, N-x): the modes (x, yp), (N-x, yp), (N-x, N-yp), (x, N-yp)
             // share |k| (ix^2 and iz^2 are even) and so the phase.
             constexpr int HX = N / 2 + 1;
-            for (int i = tid; i < RC::PAIRS * HX; i += RC::THREADS) {
-                const int pl = RC::PAIRS == 1 ? 0 : i / HX, x = i - pl * HX;
-                const int yp = pi * RC::PAIRS + pl;
-                if (RC::PAIRS > 1 && yp > N / 2) continue;
-                row_position<N, FROM_H0, L::NPAD>(a, stage + (pl * 2) * N * RC::EW, work + (pl * 3) * L::NPAD, tile,
-                                                  x, yp, fc);
+            if (PRE && k == 0 && smp == 0) {
+#pragma unroll
+                for (int kk = 0; kk < PP; ++kk) {
+                    const int x = tid + kk * RC::THREADS;
+                    if (x <= N / 2)
+                        row_position<N, FROM_H0, L::NPAD>(a, stage, work, tile, x, pi, fc, pc[kk], ps[kk], pr[kk]);
+                }
+            } else {
+                for (int i = tid; i < RC::PAIRS * HX; i += RC::THREADS) {
+                    const int pl = RC::PAIRS == 1 ? 0 : i / HX, x = i - pl * HX;
+                    const int yp = pi * RC::PAIRS + pl;
+                    if (RC::PAIRS > 1 && yp > N / 2) continue;
+                    row_position<N, FROM_H0, L::NPAD>(a, stage + (pl * 2) * N * RC::EW, work + (pl * 3) * L::NPAD,
+                                                      tile, x, yp, fc);
+                }
             }
             __syncthreads();                               // line inputs complete
             if (smp == nsmp - 1 && tid == 0) {             // ring stage consumed: refill it
@@ -380,11 +426,11 @@ __device__ __forceinline__ void row_pass_body(const RowArgs& a)
 // it start, only after the previous kernel has completed, which keeps stream
 // order for everything downstream.  wait_first: wait before reading too (the
 // spectrum or h0 was just written by the previous kernel).
-template <int N, bool MULTI, bool FROM_H0>
-__global__ void __launch_bounds__(RowCfg<N, FROM_H0>::THREADS, RowCfg<N, FROM_H0>::MINB) k_row_pass(RowArgs a)
+template <int N, bool MULTI, bool FROM_H0, int V = 0>
+__global__ void __launch_bounds__(RowCfg<N, FROM_H0, V>::THREADS, RowCfg<N, FROM_H0, V>::MINB) k_row_pass(RowArgs a)
 {
     if (a.wait_first) pdl_wait_prior();
-    row_pass_body<N, MULTI, FROM_H0>(a);
+    row_pass_body<N, MULTI, FROM_H0, V>(a);
     pdl_wait_prior();
 }
 
@@ -402,18 +448,6 @@ __global__ void __launch_bounds__(RowCfg<N, FROM_H0>::THREADS, RowCfg<N, FROM_H0
 // barrier operations whatever happens, so a timed-out copy wait (flagged in
 // the status word) never leaves a warp waiting.
 // ---------------------------------------------------------------------------
-// Row-line decompositions of the warp-specialised row pass: V = 0 the
-// 16-point-first LineFor lines; V = 2 8-point-first lines (one more exchange,
-// half the values per thread, twice the threads per line), whose twiddle plan
-// follows the row and column plans in the table (k_twiddles); V = 3 (N = 1024)
-// the column lines, 32 x 32 (one warp per line, one exchange), which use the
-// column plan.
-template <int N> struct ColLineFor;   // the column decompositions (below), whose plan precedes this one
-template <int N, int V> struct RowLine { using type = typename LineFor<N>::type; };
-template <> struct RowLine<1024, 3> { using type = LineCfg<1024, 32, 32>; };
-template <> struct RowLine<512, 2> { using type = LineCfg<512, 8, 8, 8>; };
-template <> struct RowLine<1024, 2> { using type = LineCfg<1024, 8, 8, 4, 4>; };
-template <> struct RowLine<2048, 2> { using type = LineCfg<2048, 8, 8, 8, 4>; };
 
 template <int N, bool FROM_H0, int V = 0>
 struct RowWsCfg {
@@ -1112,18 +1146,18 @@ static cudaError_t launch_pdl(void (*kernel)(Args), dim3 grid, dim3 block, size_
     return cudaLaunchKernelEx(&cfg, kernel, a);
 }
 
-template <int N, bool MULTI, bool FROM_H0>
+template <int N, bool MULTI, bool FROM_H0, int V = 0>
 static cudaError_t row_pass_nm(const RowArgs& a, cudaStream_t s)
 {
-    using RC = RowCfg<N, FROM_H0>;
+    using RC = RowCfg<N, FROM_H0, V>;
     static PerDevice cache;   // resident CTAs per SM on each device, found on its first launch
     int per_sm = 0, grid = 0;
-    cudaError_t e = persistent_setup(cache, k_row_pass<N, MULTI, FROM_H0>, RC::THREADS, RC::SMEM, &per_sm);
+    cudaError_t e = persistent_setup(cache, k_row_pass<N, MULTI, FROM_H0, V>, RC::THREADS, RC::SMEM, &per_sm);
     if (e != cudaSuccess || (e = persistent_grid(per_sm, tuning_for(N).row_ctas_per_sm, &grid)) != cudaSuccess)
         return e;
     const int items = a.tiles * RC::ITEMS;
-    return launch_pdl(k_row_pass<N, MULTI, FROM_H0>, dim3(grid < items ? grid : items), dim3(RC::THREADS), RC::SMEM,
-                      s, true, a);
+    return launch_pdl(k_row_pass<N, MULTI, FROM_H0, V>, dim3(grid < items ? grid : items), dim3(RC::THREADS),
+                      RC::SMEM, s, true, a);
 }
 
 template <int N, bool MULTI, bool FROM_H0, int V = 0>
@@ -1155,9 +1189,12 @@ static cudaError_t row_pass_n(const RowArgs& a, cudaStream_t s)
             return single ? row_pass_nm<N, false, false>(a, s) : row_pass_nm<N, true, false>(a, s);
         if (variant == 2)                                     // warp-specialised, 8-point-first lines
             return single ? row_ws_nm<N, false, false, 2>(a, s) : row_ws_nm<N, true, false, 2>(a, s);
-        if constexpr (N == 1024)
+        if constexpr (N == 1024) {
             if (variant == 3)                                 // warp-specialised, 32 x 32 lines
                 return single ? row_ws_nm<N, false, false, 3>(a, s) : row_ws_nm<N, true, false, 3>(a, s);
+            if (variant == 4)                                 // every warp, 32 x 32 lines
+                return single ? row_pass_nm<N, false, false, 3>(a, s) : row_pass_nm<N, true, false, 3>(a, s);
+        }
         return single ? row_ws_nm<N, false, false>(a, s) : row_ws_nm<N, true, false>(a, s);
     } else {
         if (!a.spec) return row_pass_nm<N, false, true>(a, s);

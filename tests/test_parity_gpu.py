@@ -379,15 +379,16 @@ def test_fused_column_kernel_matches_two_kernels(torch_cuda, ocean_lib, N):
 @pytest.mark.parametrize("N", [512, 1024, 2048])
 def test_row_pass_variants_agree(torch_cuda, ocean_lib, oracle_mod, N):
     """The row-pass kernels the tuning chooses between at N >= 512 (the
-    warp-specialised k_row_ws with 16- or 8-point-first lines, and k_row_pass
-    with every warp on the prepass and then its line) give the same frames,
-    back to back on one handle, and match the FP64 oracle."""
+    warp-specialised k_row_ws with 16- or 8-point-first lines or, at N = 1024,
+    32 x 32 lines, and k_row_pass with every warp on the prepass and then its
+    line, with the default or 32 x 32 lines) give the same frames, back to back
+    on one handle, and match the FP64 oracle."""
     torch = torch_cuda
     d = P.c2(N)
     dev = torch.device("cuda")
     times = [0.25, 9.5, 1.0e5]
     outs = {}
-    variants = (0, 1, 2, 3) if N == 1024 else (0, 1, 2)
+    variants = (0, 1, 2, 3, 4) if N == 1024 else (0, 1, 2)
     saved = ocean_lib.get_tuning(N)
     try:
         for variant in variants:
