@@ -963,29 +963,44 @@ __global__ void __launch_bounds__(FusedCfg<N, P>::THREADS, P == 2 ? 2 : 1) k_col
     const int ca = kind < P ? x0 + 2 * kind : (x0 - 1) & (N - 1);
     const int cb = kind < P ? ca + 1 : (x0 + 2 * P) & (N - 1);
     const float2* in = a.inter + (size_t)unit * inter_len(N);
-    constexpr int G = L::G;
-    float2 v[L::E];
+    constexpr int G = L::G, R1 = L::R1, HR = L::R1 / 2;
+    static_assert(G == 32 && L::E == R1, "one warp per line, one value per first-pass input");
+    // Register r holds row y = t + r*G.  Rows up to N/2 are loaded: registers
+    // r < R1/2 (rows t + r*G) and register R1/2 (row N/2 - t, the conjugate of
+    // row N/2 + t for t > 0).  A row y > N/2 is the conjugate of row N - y
+    // (the row-transformed spectra are Hermitian in y), which another lane has
+    // loaded: N - t - r*G = (32 - t) + (R1 - 1 - r)*G, register R1 - 1 - r of
+    // lane 32 - t (lane 0: its own register R1 - r).  L2 loads
+    // (ld.global.cg): the read-only (non-coherent) path may keep lines of the
+    // previous frame's intermediate, which the row pass rewrites while this
+    // grid is already resident (it is launched as a programmatic dependent).
+    float4 z[HR + 1];                                        // (column ca, column cb) of the row
 #pragma unroll
-    for (int r = 0; r < L::E; ++r) {
-        // register r holds row y = t + r*G: rows below N/2 directly, rows above
-        // as the conjugate of row N - y (as in k_col_fft)
-        const int  ys = r < L::R1 / 2 ? t + r * G : (r == L::R1 / 2 ? N / 2 - t : N - t - r * G);
-        const bool cj = r > L::R1 / 2 || (r == L::R1 / 2 && t != 0);
-        // L2 loads (ld.global.cg): the read-only (non-coherent) path may keep
-        // lines of the previous frame's intermediate, which the row pass
-        // rewrites while this grid is already resident (it is launched as a
-        // programmatic dependent)
-        float2 p, q;
+    for (int r = 0; r <= HR; ++r) {
+        const int ys = r < HR ? t + r * G : N / 2 - t;
         if (kind < P) {                                      // one 16-byte (ca, cb) pair of the row
-            const float4 z = __ldcg(reinterpret_cast<const float4*>(in + inter_index(N, f, ca, ys)));
-            p = make_float2(z.x, z.y);
-            q = make_float2(z.z, z.w);
+            z[r] = __ldcg(reinterpret_cast<const float4*>(in + inter_index(N, f, ca, ys)));
         } else {
-            p = __ldcg(in + inter_index(N, f, ca, ys));
-            q = __ldcg(in + inter_index(N, f, cb, ys));
+            const float2 p = __ldcg(in + inter_index(N, f, ca, ys));
+            const float2 q = __ldcg(in + inter_index(N, f, cb, ys));
+            z[r] = make_float4(p.x, p.y, q.x, q.y);
         }
-        if (cj) { p.y = -p.y; q.y = -q.y; }
-        v[r] = make_float2(p.x - q.y, p.y + q.x);            // p + i*q
+    }
+    float2 v[L::E];
+    const int src = (32 - t) & 31;
+#pragma unroll
+    for (int r = HR + 1; r < R1; ++r) {
+        const float4 w = z[R1 - 1 - r];
+        float4 m = make_float4(__shfl_sync(0xffffffffu, w.x, src), __shfl_sync(0xffffffffu, w.y, src),
+                               __shfl_sync(0xffffffffu, w.z, src), __shfl_sync(0xffffffffu, w.w, src));
+        if (t == 0) m = z[R1 - r];
+        v[r] = make_float2(m.x + m.w, m.z - m.y);            // conj(p) + i*conj(q)
+    }
+#pragma unroll
+    for (int r = 0; r <= HR; ++r) {
+        float4 m = z[r];
+        if (r == HR && t != 0) { m.y = -m.y; m.w = -m.w; }
+        v[r] = make_float2(m.x - m.w, m.y + m.z);            // p + i*q
     }
     // The next frame's row pass may overwrite the intermediate once every
     // thread's loads have returned (a CTA may count as triggered as soon as any

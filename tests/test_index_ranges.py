@@ -193,6 +193,29 @@ def test_adjoint_row_pass_accumulators_and_dh0(N):
     assert np.all(dh0 == 1)
 
 
+@pytest.mark.parametrize("N", [512, 1024])
+def test_col_fused_mirror_shuffles(N):
+    """k_col_fused loads rows 0..N/2 only; register r > R1/2 of lane t (row
+    N - t - r*G, the conjugate of a loaded row) comes from register R1-1-r of
+    lane (32 - t) & 31, lane 0 from its own register R1 - r.  Both source
+    registers are loaded ones, and they hold exactly the mirrored row."""
+    G, E, R1, pos, t = line(N, COL_LINE_FOR[N])
+    assert G == 32 and E == R1
+    HR = R1 // 2
+    lane = np.arange(32)
+    loaded = {r: np.where(np.full(32, r < HR), lane + r * G, N // 2 - lane) for r in range(HR + 1)}
+    for r in range(HR + 1):
+        assert loaded[r].min() >= 0 and loaded[r].max() <= N // 2
+    for r in range(HR + 1, R1):
+        want = N - lane - r * G                                  # the row register r stands for, mirrored
+        assert want.min() >= 1 and want.max() < N // 2
+        src = (32 - lane) & 31
+        got = loaded[R1 - 1 - r][src]
+        got[0] = loaded[R1 - r][0]
+        assert R1 - 1 - r < HR and R1 - r < HR
+        assert np.array_equal(got, want)
+
+
 @pytest.mark.parametrize("N,P", [(512, 2), (1024, 2), (512, 4), (1024, 4)])
 def test_col_fused_loads_staging_and_stores(N, P):
     """k_col_fused<N, P>: every line load lies in the intermediate (16-byte
