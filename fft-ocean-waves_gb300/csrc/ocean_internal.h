@@ -76,6 +76,9 @@ struct RowArgs {
     // may have written the spectrum, h0 or the twiddle plans); 0: the row pass
     // may overlap that kernel and waits for it only at its end.
     int                wait_first;
+    // single unit, warp-specialised pass: CTAs 0..prefetch_ctas-1 prefetch the
+    // other CTAs' spectrum rows into L2 (0: none); set by the launcher
+    int                prefetch_ctas;
 };
 
 // Column side of a frame: k_col_fft (column transforms, intermediate ->

@@ -522,6 +522,18 @@ __device__ __forceinline__ void row_ws_body(const RowArgs& a)
     }
     __syncthreads();
     pdl_launch_dependents();
+    // The first prefetch_ctas CTAs start on the SMs that the previous frame's
+    // column stage leaves free, the others only when it ends: the early ones
+    // ask L2 for the late ones' spectrum rows (item i >= E by CTA (i - E) % E,
+    // one row per thread), so that those find their rows there instead of in
+    // HBM.  A hint only; nothing waits for it.
+    if (!MULTI && !FROM_H0 && (int)blockIdx.x < a.prefetch_ctas) {
+        const int E = a.prefetch_ctas, i = E + (int)blockIdx.x + E * (tid >> 1);
+        if (i < n_items) {
+            const int yp = i, row = (tid & 1) ? (N - yp) & (N - 1) : yp;
+            l2_prefetch(a.spec + (size_t)row * N, N * sizeof(float2), 0, 1);
+        }
+    }
 
     // The first job's line inputs are computed by every warp: until they
     // exist the transform warps have nothing to do.  (Every CTA has a job:
@@ -1185,8 +1197,19 @@ static cudaError_t row_ws_nm(const RowArgs& a, cudaStream_t s)
     if (e != cudaSuccess || (e = persistent_grid(per_sm, tuning_for(N).row_ctas_per_sm, &grid)) != cudaSuccess)
         return e;
     const int items = a.tiles * WC::ITEMS;
-    return launch_pdl(k_row_ws<N, MULTI, FROM_H0, V>, dim3(grid < items ? grid : items), dim3(WC::THREADS), WC::SMEM,
-                      s, true, a);
+    if (grid > items) grid = items;
+    // Overlapping a fused column stage of the same N (the previous frame's),
+    // the CTAs on the SMs that stage leaves free start first and prefetch the
+    // others' rows.
+    RowArgs b = a;
+    b.prefetch_ctas = 0;
+    const Tuning tu = tuning_for(N);
+    int sms = 0;
+    if (!MULTI && !FROM_H0 && tu.row_overlap && tu.col_fused && device_sms(&sms) == cudaSuccess) {
+        const int free_sms = sms - N / (2 * tu.col_fused);
+        if (free_sms > 0) b.prefetch_ctas = free_sms * per_sm < grid ? free_sms * per_sm : grid;
+    }
+    return launch_pdl(k_row_ws<N, MULTI, FROM_H0, V>, dim3(grid), dim3(WC::THREADS), WC::SMEM, s, true, b);
 }
 
 template <int N>

@@ -100,6 +100,18 @@ __device__ __forceinline__ bool block_wait(uint64_t* bar, uint32_t parity, int* 
     return *flag_smem != 0;
 }
 
+// Ask L2 for [p, p + bytes) (cp.async.bulk.prefetch.L2: a hint, nothing
+// waits for it), in 4 KB pieces spread over `nthreads` threads.  p 16-byte
+// aligned, bytes a multiple of 16.
+__device__ __forceinline__ void l2_prefetch(const void* p, size_t bytes, int tid, int nthreads)
+{
+    const char* b = static_cast<const char*>(p);
+    for (size_t o = (size_t)tid * 4096; o < bytes; o += (size_t)nthreads * 4096) {
+        const uint32_t n = (uint32_t)(bytes - o < 4096 ? bytes - o : 4096);
+        asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(b + o), "r"(n) : "memory");
+    }
+}
+
 // Drop the L2 lines that lie wholly inside [p, p + bytes), spread over
 // `nthreads` threads (discard.global.L2: the lines' contents become undefined
 // and are never written back to HBM).  Only for scratch that the calling block

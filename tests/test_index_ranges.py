@@ -267,3 +267,25 @@ def test_col_fused_loads_staging_and_stores(N, P):
                     assert rd.min() >= 0 and rd.max() < COLS * CP and np.all(used[rd])
             np.add.at(out_hits, y * N + x0 + c - 1, 1)
     assert np.all(out_hits == 1)
+
+
+@pytest.mark.parametrize("N,P,per_sm,threads", [(1024, 4, 2, 224), (1024, 2, 2, 224), (512, 2, 2, 224)])
+def test_row_ws_spectrum_prefetch(N, P, per_sm, threads):
+    """k_row_ws, single unit overlapping a fused column stage: CTAs
+    0..E-1 (E = SMs the column stage leaves free x row CTAs per SM) prefetch
+    the spectrum rows of items E..N/2, each row pair exactly once, every
+    prefetch a whole in-range row of the spectrum."""
+    sms, items = 152, N // 2 + 1
+    grid = min(sms * per_sm, items)
+    E = min(max(0, sms - N // (2 * P)) * per_sm, grid)
+    seen = {}
+    for b in range(E):
+        for tid in range(threads):
+            i = E + b + E * (tid >> 1)
+            if i >= items:
+                continue
+            row = (N - i) & (N - 1) if tid & 1 else i
+            assert 0 <= row < N                                   # a.spec + row*N, N float2
+            seen[(i, tid & 1)] = seen.get((i, tid & 1), 0) + 1
+    assert all(v == 1 for v in seen.values())
+    assert len(seen) == 2 * max(0, items - E)
