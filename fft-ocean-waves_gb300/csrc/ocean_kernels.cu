@@ -329,6 +329,15 @@ __device__ __forceinline__ void row_pass_body(const RowArgs& a)
     // The column pass may start its set-up now; it waits for this grid to finish
     // before it reads the intermediate.
     pdl_launch_dependents();
+    // the early CTAs ask L2 for the late CTAs' spectrum rows (as k_row_ws;
+    // prefetch_ctas is 0 unless the launcher set it)
+    if (!MULTI && !FROM_H0 && RC::PAIRS == 1 && (int)blockIdx.x < a.prefetch_ctas) {
+        const int E = a.prefetch_ctas;
+        for (int i = E + (int)blockIdx.x + E * (tid >> 1); i < n_items; i += E * (RC::THREADS >> 1)) {
+            const int row = (tid & 1) ? (N - i) & (N - 1) : i;
+            l2_prefetch(a.spec + (size_t)row * N, N * sizeof(float2), 0, 1);
+        }
+    }
 
     const int li = tid / L::G, t = tid % L::G;
     const int f  = li % 3;                                           // 0: Dx, 1: Dy, 2: Dz
@@ -1183,8 +1192,18 @@ static cudaError_t row_pass_nm(const RowArgs& a, cudaStream_t s)
     if (e != cudaSuccess || (e = persistent_grid(per_sm, tuning_for(N).row_ctas_per_sm, &grid)) != cudaSuccess)
         return e;
     const int items = a.tiles * RC::ITEMS;
-    return launch_pdl(k_row_pass<N, MULTI, FROM_H0, V>, dim3(grid < items ? grid : items), dim3(RC::THREADS),
-                      RC::SMEM, s, true, a);
+    if (grid > items) grid = items;
+    // one row pair per item, overlapping a fused column stage of the same N:
+    // the CTAs on the SMs that stage leaves free prefetch the others' rows
+    RowArgs b = a;
+    b.prefetch_ctas = 0;
+    const Tuning tu = tuning_for(N);
+    int sms = 0;
+    if (!MULTI && !FROM_H0 && RC::PAIRS == 1 && tu.row_overlap && tu.col_fused && device_sms(&sms) == cudaSuccess) {
+        const int free_sms = sms - N / (2 * tu.col_fused);
+        if (free_sms > 0) b.prefetch_ctas = free_sms * per_sm < grid ? free_sms * per_sm : grid;
+    }
+    return launch_pdl(k_row_pass<N, MULTI, FROM_H0, V>, dim3(grid), dim3(RC::THREADS), RC::SMEM, s, true, b);
 }
 
 template <int N, bool MULTI, bool FROM_H0, int V = 0>

@@ -269,12 +269,15 @@ def test_col_fused_loads_staging_and_stores(N, P):
     assert np.all(out_hits == 1)
 
 
-@pytest.mark.parametrize("N,P,per_sm,threads", [(1024, 4, 2, 224), (1024, 2, 2, 224), (512, 2, 2, 224)])
-def test_row_ws_spectrum_prefetch(N, P, per_sm, threads):
-    """k_row_ws, single unit overlapping a fused column stage: CTAs
-    0..E-1 (E = SMs the column stage leaves free x row CTAs per SM) prefetch
-    the spectrum rows of items E..N/2, each row pair exactly once, every
-    prefetch a whole in-range row of the spectrum."""
+@pytest.mark.parametrize("N,P,per_sm,threads,loop", [(1024, 4, 2, 224, False), (1024, 2, 2, 224, False),
+                                                    (512, 2, 2, 224, False), (1024, 4, 4, 96, True),
+                                                    (512, 2, 8, 96, True)])
+def test_row_spectrum_prefetch(N, P, per_sm, threads, loop):
+    """Single unit overlapping a fused column stage: CTAs 0..E-1 (E = SMs the
+    column stage leaves free x row CTAs per SM) prefetch the spectrum rows of
+    items E..N/2, each row pair exactly once, every prefetch a whole in-range
+    row of the spectrum.  k_row_ws: one item per thread pair; k_row_pass
+    (loop): thread pairs step on by E * threads/2 items."""
     sms, items = 152, N // 2 + 1
     grid = min(sms * per_sm, items)
     E = min(max(0, sms - N // (2 * P)) * per_sm, grid)
@@ -282,10 +285,12 @@ def test_row_ws_spectrum_prefetch(N, P, per_sm, threads):
     for b in range(E):
         for tid in range(threads):
             i = E + b + E * (tid >> 1)
-            if i >= items:
-                continue
-            row = (N - i) & (N - 1) if tid & 1 else i
-            assert 0 <= row < N                                   # a.spec + row*N, N float2
-            seen[(i, tid & 1)] = seen.get((i, tid & 1), 0) + 1
+            while i < items:
+                row = (N - i) & (N - 1) if tid & 1 else i
+                assert 0 <= row < N                               # a.spec + row*N, N float2
+                seen[(i, tid & 1)] = seen.get((i, tid & 1), 0) + 1
+                if not loop:
+                    break
+                i += E * (threads >> 1)
     assert all(v == 1 for v in seen.values())
     assert len(seen) == (2 * (items - E) if E > 0 else 0)       # no free SMs: no prefetch
