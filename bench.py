@@ -538,7 +538,7 @@ def bench_adjoint_large(torch, og, dev, stream, n_sets=16, chunk=16):
     fwd_ms = bwd_ms = 0.0
     fwd_mem = bwd_mem = 0
     losses = []
-    ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]   # forward start/end, backward start/end
     with torch.cuda.stream(stream):
         for s, (p, seed) in enumerate(W.adjoint_sets(n_sets)):
             torch.cuda.synchronize()
@@ -570,7 +570,7 @@ def bench_adjoint_large(torch, og, dev, stream, n_sets=16, chunk=16):
             dh0 = torch.zeros((N, N, 4), device=dev)
             model.backward(times[:1], G[0, :1], G[1, :1], G[2, :1], dh0=dh0, stream=stream)   # adjoint scratch
             torch.cuda.synchronize()
-            ev[1].record(stream)
+            ev[2].record(stream)
             for c0 in range(0, T, chunk):
                 n = min(chunk, T - c0)
                 for j in range(n):
@@ -580,11 +580,11 @@ def bench_adjoint_large(torch, og, dev, stream, n_sets=16, chunk=16):
                         G[f, j].sub_(Tg[f]).mul_(2.0 / M)
                 model.backward(times[c0:c0 + n], G[0, :n], G[1, :n], G[2, :n], dh0=dh0, accumulate=c0 > 0,
                                stream=stream)
-            ev[2].record(stream)
+            ev[3].record(stream)
             torch.cuda.synchronize()
             bwd_mem = max(bwd_mem, free0 - torch.cuda.mem_get_info()[0])
             fwd_ms += ev[0].elapsed_time(ev[1])
-            bwd_ms += ev[1].elapsed_time(ev[2])
+            bwd_ms += ev[2].elapsed_time(ev[3])
             model.device_status()
             model.close()
             target.close()
