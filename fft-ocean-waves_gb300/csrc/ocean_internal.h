@@ -136,7 +136,8 @@ struct Tuning {
     int col_fused;         // 0, or the fused column kernel's column pairs per CTA (2, 4)
     int row_variant;       // N >= 512: 0 k_row_ws, 1 every warp (k_row_pass), 2 k_row_ws with 8-point-first
                            // lines, 3 (N = 1024) k_row_ws with 32 x 32 lines, 4 (N = 1024) k_row_pass
-                           // with 32 x 32 lines
+                           // with 32 x 32 lines, 5 (N = 1024) k_row_ws with 32 x 32 lines, one stage
+                           // and one buffer set, three CTAs per SM
 };
 Tuning tuning_for(int N);
 

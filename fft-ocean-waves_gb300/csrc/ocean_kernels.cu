@@ -138,6 +138,7 @@ __device__ __forceinline__ float2 mul_mi(float f, float2 z) { return make_float2
 template <int N> struct ColLineFor;   // the column decompositions (below), whose plan precedes this one
 template <int N, int V> struct RowLine { using type = typename LineFor<N>::type; };
 template <> struct RowLine<1024, 3> { using type = LineCfg<1024, 32, 32>; };
+template <> struct RowLine<1024, 5> { using type = LineCfg<1024, 32, 32>; };
 template <> struct RowLine<512, 2> { using type = LineCfg<512, 8, 8, 8>; };
 template <> struct RowLine<1024, 2> { using type = LineCfg<1024, 8, 8, 4, 4>; };
 template <> struct RowLine<2048, 2> { using type = LineCfg<2048, 8, 8, 8, 4>; };
@@ -467,20 +468,25 @@ struct RowWsCfg {
     static constexpr int THREADS     = FFT_THREADS + PRE_THREADS;
     static_assert(THREADS <= 1024, "one CTA");
     static constexpr int ITEMS       = N / 2 + 1;   // row pairs per tile
-    static constexpr int STAGES      = 2;
+    // V = 5 (32 x 32 lines, three CTAs per SM): one ring stage and one
+    // line-buffer set, so that three CTAs fit in shared memory; the prepass
+    // of job j + 1 then waits for job j's transforms
+    static constexpr int STAGES      = V == 5 ? 1 : 2;
+    static constexpr int SETS        = V == 5 ? 1 : 2;
     static constexpr int EW          = FROM_H0 ? 2 : 1;
     static constexpr size_t RING     = (size_t)STAGES * 2 * N * EW;
     static constexpr size_t BUF      = (size_t)3 * L::NPAD;   // one job's three line buffers
     static constexpr int    TW       = TwPlan<L>::LEN;
-    static constexpr size_t SMEM     = sizeof(float2) * (TW + RING + 2 * BUF) + 128;
+    static constexpr size_t SMEM     = sizeof(float2) * (TW + RING + SETS * BUF) + 128;
     // register budget per thread the residency is set for: 96 for the
-    // 16-point-first lines, 64 for the 8-point-first ones (8 values per thread)
+    // 16-point-first lines, 64 for the 8-point-first ones (8 values per
+    // thread), 128 for the 32 x 32 lines (96 with three CTAs per SM)
     static constexpr int REGS        = V == 2 ? 64 : (V == 3 ? 128 : 96);
     static constexpr int MINB        = 65536 / (THREADS * REGS) < 1 ? 1 : 65536 / (THREADS * REGS);
     // offset of this decomposition's twiddle plan in the table (float2 units)
     static constexpr int TWOFF = V == 2   ? TwPlan<typename LineFor<N>::type>::LEN +
                                                 TwPlan<typename ColLineFor<N>::type>::LEN
-                                 : V == 3 ? TwPlan<typename LineFor<N>::type>::LEN   // the column plan
+                                 : (V == 3 || V == 5) ? TwPlan<typename LineFor<N>::type>::LEN   // the column plan
                                           : 0;
     static_assert(TWOFF % 2 == 0 && TW % 2 == 0, "16-byte twiddle copies");
     static constexpr int BAR_FULL = 4, BAR_EMPTY = 6, BAR_PRE = 8, BAR_TW = 9;   // named barriers (lines use 1..3)
@@ -504,7 +510,7 @@ __device__ __forceinline__ void row_ws_body(const RowArgs& a)
     float2* smem = align_smem(smem_raw);
     float2* tw_s = smem;
     float2* ring = smem + WC::TW;                            // [STAGES][2 rows][N*EW]
-    float2* bufs = ring + WC::RING;                          // [2][3 lines][NPAD]
+    float2* bufs = ring + WC::RING;                          // [SETS][3 lines][NPAD]
     __shared__ __align__(8) uint64_t bars[WC::STAGES], bar_tw;
     __shared__ int wait_ok;
 
@@ -587,7 +593,7 @@ __device__ __forceinline__ void row_ws_body(const RowArgs& a)
         }
         named_sync(WC::BAR_TW, WC::FFT_THREADS);             // the twiddle plan is in
         for (int j = 0; j < n_jobs; ++j) {
-            const int b = j & 1, ki = j / nsmp, smp = j - ki * nsmp;
+            const int b = j % WC::SETS, ki = j / nsmp, smp = j - ki * nsmp;
             const int item = blockIdx.x + ki * gridDim.x, tile = item / WC::ITEMS, yp = item % WC::ITEMS;
             const int unit = MULTI ? tile * a.S + smp : 0;
             if (j > 0) named_sync(WC::BAR_FULL + b, WC::THREADS);   // the job's line inputs are complete
@@ -610,7 +616,7 @@ __device__ __forceinline__ void row_ws_body(const RowArgs& a)
         uint32_t  phase_bits = 1u;                            // stage 0's first phase went to job 0
         bool      gave_up    = wait_ok == 0;                  // a copy wait timed out: issue no more copies
         for (int j = 1; j < n_jobs; ++j) {
-            const int b = j & 1, ki = j / nsmp, smp = j - ki * nsmp;
+            const int b = j % WC::SETS, ki = j / nsmp, smp = j - ki * nsmp;
             const int item = blockIdx.x + ki * gridDim.x, tile = item / WC::ITEMS, yp = item % WC::ITEMS;
             const int st = ki % WC::STAGES;
             float2* stage = ring + (size_t)st * 2 * N * WC::EW;
@@ -628,7 +634,7 @@ __device__ __forceinline__ void row_ws_body(const RowArgs& a)
                 named_sync(WC::BAR_PRE, WC::PRE_THREADS);
                 gave_up = wait_ok == 0;
             }
-            if (j >= 2) named_sync(WC::BAR_EMPTY + b, WC::THREADS);   // set b's previous job is transformed
+            if (j >= WC::SETS) named_sync(WC::BAR_EMPTY + b, WC::THREADS);   // set b's previous job is transformed
             const FrameConsts fc = MULTI ? a.fcs[tile * a.S + smp] : a.fc0;
 #pragma unroll 4
             for (int x = pt; x <= N / 2; x += WC::PRE_THREADS)
@@ -646,7 +652,8 @@ __device__ __forceinline__ void row_ws_body(const RowArgs& a)
             }
         }
         // the transform side's last arrivals on EMPTY
-        for (int j = n_jobs - 2 > 0 ? n_jobs - 2 : 0; j < n_jobs; ++j) named_sync(WC::BAR_EMPTY + (j & 1), WC::THREADS);
+        for (int j = n_jobs - WC::SETS > 0 ? n_jobs - WC::SETS : 0; j < n_jobs; ++j)
+            named_sync(WC::BAR_EMPTY + j % WC::SETS, WC::THREADS);
     }
 }
 
@@ -1249,6 +1256,8 @@ static cudaError_t row_pass_n(const RowArgs& a, cudaStream_t s)
         if constexpr (N == 1024) {
             if (variant == 3)                                 // warp-specialised, 32 x 32 lines
                 return single ? row_ws_nm<N, false, false, 3>(a, s) : row_ws_nm<N, true, false, 3>(a, s);
+            if (variant == 5)                                 // the same, three CTAs per SM
+                return single ? row_ws_nm<N, false, false, 5>(a, s) : row_ws_nm<N, true, false, 5>(a, s);
             if (variant == 4)                                 // every warp, 32 x 32 lines
                 return single ? row_pass_nm<N, false, false, 3>(a, s) : row_pass_nm<N, true, false, 3>(a, s);
         }

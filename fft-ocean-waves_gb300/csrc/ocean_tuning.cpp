@@ -45,12 +45,12 @@ Live* live()
 }
 
 // The row-pass variants that exist for size N: below 512 only the every-warp
-// pass (1); variants 3 and 4 (32 x 32 lines) at N = 1024 only, elsewhere they
-// read as the same pass with the default lines (0 and 1).
+// pass (1); variants 3, 4 and 5 (32 x 32 lines) at N = 1024 only, elsewhere
+// they read as the same pass with the default lines (0, 1 and 0).
 int row_variant_for(int N, int v)
 {
     if (N < 512) return 1;
-    if (v == 3 && N != 1024) return 0;
+    if ((v == 3 || v == 5) && N != 1024) return 0;
     if (v == 4 && N != 1024) return 1;
     return v;
 }
@@ -101,7 +101,7 @@ extern "C" int ocean_set_tuning(int32_t N, const ocean_tuning* cfg)
     if (i < 0) return fail(OCEAN_ERR_INVALID, "no tuning entry for N = " + std::to_string(N));
     if ((cfg->row_overlap != 0 && cfg->row_overlap != 1) || cfg->row_ctas_per_sm < 0 || cfg->row_ctas_per_sm > 32 ||
         cfg->wave_mib < 1 || cfg->wave_mib > 4096 || (cfg->col_fused != 0 && cfg->col_fused != 2 && cfg->col_fused != 4) ||
-        cfg->row_variant < 0 || cfg->row_variant > 4)
+        cfg->row_variant < 0 || cfg->row_variant > 5)
         return fail(OCEAN_ERR_INVALID, "tuning values out of range");
     Live& l = live()[i];
     l.row_overlap.store(cfg->row_overlap);

@@ -11,11 +11,12 @@ candidate of
                               output stage, or waits for it first)
     row_ctas_per_sm  0 (as many as fit), 1, 2, 3, 4, 6, 8 (persistent row-pass
                               grid; caps above the occupancy limit give its grid)
-    row_variant      0 / 1 / 2 / 3 / 4 (N >= 512: warp-specialised row pass,
-                              every warp running the prepass and then its line
-                              FFT, warp-specialised with 8-point-first lines,
-                              or (N = 1024) warp-specialised or every warp with
-                              32 x 32 lines)
+    row_variant      0 .. 5 (N >= 512: warp-specialised row pass, every warp
+                              running the prepass and then its line FFT,
+                              warp-specialised with 8-point-first lines, or
+                              (N = 1024) warp-specialised or every warp with
+                              32 x 32 lines, or warp-specialised with 32 x 32
+                              lines at three CTAs per SM)
     col_fused        0 / 2 / 4 (N = 512, 1024: the column side as column FFT +
                               output kernels, or as one fused kernel with 2 or 4
                               column pairs per CTA)
@@ -74,7 +75,7 @@ def tune_size(torch, og, workloads, N, reps, log):
             ring[i % RING].update(i / 60.0, *outs[i % RING], stream=stream)
         torch.cuda.synchronize()
         fused_opts = (0, 2, 4) if N in (512, 1024) else (0,)
-        variants = ((0, 1, 2, 3, 4) if N == 1024 else (0, 1, 2)) if N >= 512 else (1,)
+        variants = ((0, 1, 2, 3, 4, 5) if N == 1024 else (0, 1, 2)) if N >= 512 else (1,)
         for variant in variants:                          # row pass: warp-specialised or every warp
             for fused in fused_opts:                      # the fused column kernel exists for 512 and 1024
                 for cap in (0, 1, 2, 3, 4, 6, 8):         # 0: as many CTAs per SM as fit

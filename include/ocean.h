@@ -383,7 +383,9 @@ typedef struct ocean_tuning {
                                  at N = 1024), 2 = warp-specialised with 8-point-first lines (half the
                                  registers per thread, one more exchange), 3 = warp-specialised with 32 x 32
                                  lines (N = 1024 only; reads 0 elsewhere), 4 = every warp with 32 x 32 lines
-                                 (N = 1024 only; reads 1 elsewhere); below 512 only 1 exists and this reads 1 */
+                                 (N = 1024 only; reads 1 elsewhere), 5 = as 3 with one ring stage and one
+                                 line-buffer set, three CTAs per SM (N = 1024 only; reads 0 elsewhere);
+                                 below 512 only 1 exists and this reads 1                                    */
 } ocean_tuning;
 
 OCEAN_API int ocean_get_tuning(int32_t N, ocean_tuning* out);

@@ -261,7 +261,7 @@ def test_tuning_table_round_trip(ocean_lib):
     ocean_lib.set_tuning(512, **old)
     assert ocean_lib.get_tuning(512) == old
     for bad in (dict(row_overlap=2), dict(row_ctas_per_sm=-1), dict(wave_mib=0), dict(col_fused=1), dict(col_fused=3),
-                dict(row_variant=5), dict(row_variant=-1)):
+                dict(row_variant=6), dict(row_variant=-1)):
         with pytest.raises(ocean_lib.OceanError):
             ocean_lib.set_tuning(512, **bad)
     assert ocean_lib.get_tuning(512) == old
@@ -277,6 +277,8 @@ def test_tuning_table_round_trip(ocean_lib):
     assert ocean_lib.get_tuning(2048)["row_variant"] == 0
     ocean_lib.set_tuning(2048, row_variant=4)
     assert ocean_lib.get_tuning(2048)["row_variant"] == 1
+    ocean_lib.set_tuning(2048, row_variant=5)
+    assert ocean_lib.get_tuning(2048)["row_variant"] == 0
     ocean_lib.set_tuning(2048, **old4)
     # below N = 512 only the every-warp row pass exists
     old3 = ocean_lib.set_tuning(256, row_variant=0)

@@ -22,11 +22,13 @@ LINE_FOR = {512: (16, 16, 2), 1024: (16, 16, 4), 2048: (16, 16, 8)}   # LineFor<
 BAR_SYNC0, BAR_FULL, BAR_EMPTY, BAR_PRE, BAR_TW = 0, 4, 6, 8, 9       # RowWsCfg; lines use 1..3
 
 
-def row_ws_warps(N, n_jobs, nsmp, tail_sync=False):
+def row_ws_warps(N, n_jobs, nsmp, tail_sync=False, sets=2, radices=None):
     """Per-warp barrier sequences of one k_row_ws CTA with n_jobs jobs (items x
     samples, nsmp samples per item).  tail_sync: line_fft ends on a line
-    barrier (the other callers of line_fft) or not (k_row_ws)."""
-    R1, R2, R3 = LINE_FOR[N]
+    barrier (the other callers of line_fft) or not (k_row_ws).  sets: line
+    buffer sets (RowWsCfg::SETS; 1 for the 32 x 32 lines at three CTAs per
+    SM).  radices: the line decomposition (default LineFor<N>)."""
+    R1, R2, R3 = radices or LINE_FOR[N]
     G = N // R1
     fft_threads = 3 * G
     pre_threads = 256 if N >= 2048 else 128
@@ -49,7 +51,7 @@ def row_ws_warps(N, n_jobs, nsmp, tail_sync=False):
         li = (w * 32) // G
         ops = list(prologue) + [("sync", BAR_TW, fft_threads)]
         for j in range(n_jobs):
-            b = j & 1
+            b = j % sets
             if j > 0:
                 ops.append(("sync", BAR_FULL + b, threads))
             ops += line_ops(li)
@@ -58,16 +60,16 @@ def row_ws_warps(N, n_jobs, nsmp, tail_sync=False):
     for w in range(pre_threads // 32):
         ops = list(prologue)
         for j in range(1, n_jobs):
-            b, smp = j & 1, j % nsmp
+            b, smp = j % sets, j % nsmp
             if smp == 0:
                 ops.append(("sync", BAR_PRE, pre_threads))       # the item's rows are in
-            if j >= 2:
+            if j >= sets:
                 ops.append(("sync", BAR_EMPTY + b, threads))     # set b's previous job is transformed
             ops.append(("arrive", BAR_FULL + b, threads))
             if smp == nsmp - 1:
                 ops.append(("sync", BAR_PRE, pre_threads))       # done with the stage: refill it
-        for j in range(max(n_jobs - 2, 0), n_jobs):              # the transform side's last arrivals
-            ops.append(("sync", BAR_EMPTY + (j & 1), threads))
+        for j in range(max(n_jobs - sets, 0), n_jobs):           # the transform side's last arrivals
+            ops.append(("sync", BAR_EMPTY + j % sets, threads))
         warps.append(ops)
     return warps
 
@@ -116,6 +118,14 @@ def run(warps, seed):
 @pytest.mark.parametrize("n_items,nsmp", [(1, 1), (2, 1), (3, 1), (7, 1), (1, 8), (2, 8), (3, 3)])
 def test_row_ws_protocol_terminates(N, n_items, nsmp):
     warps = row_ws_warps(N, n_items * nsmp, nsmp)
+    for seed in range(40):
+        run(warps, seed)
+
+
+@pytest.mark.parametrize("n_items,nsmp", [(1, 1), (2, 1), (3, 1), (7, 1), (2, 8), (3, 3)])
+def test_one_set_32x32_protocol_terminates(n_items, nsmp):
+    """row_variant 5: 32 x 32 lines (one warp each), one line-buffer set."""
+    warps = row_ws_warps(1024, n_items * nsmp, nsmp, sets=1, radices=(32, 32, 1))
     for seed in range(40):
         run(warps, seed)
 
