@@ -969,17 +969,19 @@ __global__ void __launch_bounds__(FusedCfg<N, P>::THREADS, P == 2 ? 2 : 1) k_col
     float2* tw_s = smem;
     float2* work = smem + FC::TW;                            // exchange buffers, then the staged columns
     __shared__ __align__(8) uint64_t bar_tw;
-    __shared__ int wait_ok;
+    __shared__ unsigned loaded_warps;
     const int      tid  = threadIdx.x;
     const int      unit = blockIdx.y;
     const ColUnit* cu   = a.units ? a.units + unit : &a.u0;
     if (tid == 0) {
         mbar_init(&bar_tw, 1);
         fence_mbar_init();
+        loaded_warps = 0;
         // the twiddle plan does not depend on the row pass: fetch it now
         mbar_arrive_expect_tx(&bar_tw, FC::TW * sizeof(float2));
         bulk_g2s(tw_s, a.tw + FC::TW0, FC::TW * sizeof(float2), &bar_tw);
     }
+    __syncthreads();                                         // the barrier and the counter are set up
     pdl_wait_prior();                                        // the row pass has finished
 
     // Line li: field f = li % 3 of columns ca (real part) and cb (imaginary
@@ -1032,18 +1034,28 @@ __global__ void __launch_bounds__(FusedCfg<N, P>::THREADS, P == 2 ? 2 : 1) k_col
     }
     // The next frame's row pass may overwrite the intermediate once every
     // thread's loads have returned (a CTA may count as triggered as soon as any
-    // of its threads triggers).  The barrier's predicate depends on every
-    // loaded value, so no thread passes it before all of the CTA's loads have
-    // completed; the row pass then runs on the SMs this grid leaves free and
-    // completes only after this grid.
+    // of its threads triggers).  Each warp reduces a word that depends on all
+    // of its lanes' loaded values, so its lane 0 passes the reduction only
+    // after the warp's loads have returned; it then counts the warp in, and
+    // the lane that counts the last warp triggers.  The row pass then runs on
+    // the SMs this grid leaves free and completes only after this grid.  No
+    // block barrier: a warp goes on to its transform as soon as its own line
+    // is loaded.
     {
         unsigned dep = 0;
 #pragma unroll
         for (int r = 0; r < L::E; ++r) dep |= __float_as_uint(v[r].x) ^ __float_as_uint(v[r].y);
-        (void)__syncthreads_or(dep == 0x7fc00001u);
-        if (a.trigger_next) pdl_launch_dependents();
+        dep = __reduce_or_sync(0xffffffffu, dep);
+        asm volatile("" ::"r"(dep) : "memory");             // the reduction stays, before the count
+        if (t == 0 && atomicAdd(&loaded_warps, 1u) == FC::LINES - 1 && a.trigger_next) pdl_launch_dependents();
     }
-    if (!block_wait(&bar_tw, 0, &wait_ok, a.status)) return;
+    // the twiddle plan, waited for per warp (bounded; a time-out is flagged,
+    // and the warp goes on so that every block barrier below is reached)
+    if (t == 0 && !mbar_wait_bounded(&bar_tw, 0)) {
+        atomicOr(a.status, kDeviceTimeout);
+        (void)mbar_wait_bounded(&bar_tw, 0);
+    }
+    __syncwarp();
     line_fft<L, +1, true, false>(v, work + li * L::NPAD, tw_s, t, li);
     __syncthreads();                                         // the exchange buffers are free
 
