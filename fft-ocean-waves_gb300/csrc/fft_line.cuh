@@ -31,6 +31,29 @@ namespace ocean {
 
 __device__ __forceinline__ float2 operator+(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
 __device__ __forceinline__ float2 operator-(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+// Complex add and subtract as one paired FP32 instruction each (add.rn.f32x2 /
+// sub.rn.f32x2, sm_100 and later): the two lanes round exactly as two scalar
+// adds.  With them the butterflies of an in-register DFT issue half the adds;
+// whether that shortens a kernel depends on the kernel (the line transforms
+// take them through their PAIRED parameter).
+__device__ __forceinline__ float2 add2(float2 a, float2 b)
+{
+    float2 r;
+    asm("{.reg .b64 a, b, r;\n\tmov.b64 a, {%2, %3};\n\tmov.b64 b, {%4, %5};\n\tadd.rn.f32x2 r, a, b;\n\t"
+        "mov.b64 {%0, %1}, r;}"
+        : "=f"(r.x), "=f"(r.y)
+        : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+    return r;
+}
+__device__ __forceinline__ float2 sub2(float2 a, float2 b)
+{
+    float2 r;
+    asm("{.reg .b64 a, b, r;\n\tmov.b64 a, {%2, %3};\n\tmov.b64 b, {%4, %5};\n\tsub.rn.f32x2 r, a, b;\n\t"
+        "mov.b64 {%0, %1}, r;}"
+        : "=f"(r.x), "=f"(r.y)
+        : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+    return r;
+}
 __device__ __forceinline__ float2 cmul(float2 a, float2 b)
 {
     return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
@@ -106,7 +129,7 @@ __host__ __device__ constexpr int bitrev_bits(int i, int bits)
 // Radix-2 decimation in time on bit-reversed input.  Every loop has a linear
 // induction variable so that it unrolls completely and all register indices
 // are compile-time constants.
-template <int R, int SIGN>
+template <int R, int SIGN, bool PAIRED = false>
 __device__ __forceinline__ void dft(float2* v)
 {
     constexpr int LG = ilog2c(R);
@@ -130,8 +153,8 @@ __device__ __forceinline__ void dft(float2* v)
                 const int i = k + g * 2 * h;
                 float2 b = mul_w32<SIGN>(v[i + h], idx);
                 float2 a = v[i];
-                v[i]     = a + b;
-                v[i + h] = a - b;
+                v[i]     = PAIRED ? add2(a, b) : a + b;
+                v[i + h] = PAIRED ? sub2(a, b) : a - b;
             }
         }
     }
@@ -204,7 +227,7 @@ __device__ __forceinline__ void line_sync(int li)
 // transformed.  Contains two line barriers (see line_sync); without TAIL_SYNC
 // only the first, and a thread may then leave while others of its line still
 // read `buf`.
-template <class C, int RP, int NSP, int RN, int TWOFF, int SIGN, bool NAMED, bool TAIL_SYNC = true>
+template <class C, int RP, int NSP, int RN, int TWOFF, int SIGN, bool NAMED, bool TAIL_SYNC = true, bool PAIRED = false>
 __device__ __forceinline__ void stockham_pass(float2* v, float2* buf, const float2* tw, int t, bool active, int li)
 {
     constexpr int N   = C::N;
@@ -241,7 +264,7 @@ __device__ __forceinline__ void stockham_pass(float2* v, float2* buf, const floa
             if (SIGN < 0) w.y = -w.y;
             v[b * RN + r] = cmul(v[b * RN + r], w);
         }
-        dft<RN, SIGN>(v + b * RN);
+        dft<RN, SIGN, PAIRED>(v + b * RN);
     }
 }
 
@@ -254,18 +277,20 @@ __device__ __forceinline__ void stockham_pass(float2* v, float2* buf, const floa
 // write `buf` again, or that order the reuse by a barrier of their own.
 // Threads with active == false do no work; for lines of >= 32 threads
 // they may skip the call entirely, for smaller lines they must call it (the
-// barrier is then the block's).
-template <class C, int SIGN, bool NAMED = true, bool TAIL_SYNC = true>
+// barrier is then the block's).  PAIRED: the DFT butterflies add and subtract
+// with paired FP32 instructions (same results, bit for bit).
+template <class C, int SIGN, bool NAMED = true, bool TAIL_SYNC = true, bool PAIRED = false>
 __device__ __forceinline__ void line_fft(float2* v, float2* buf, const float2* tw, int t, int li, bool active = true)
 {
     using TP = TwPlan<C>;
-    if (active) dft<C::R1, SIGN>(v);
-    stockham_pass<C, C::R1, 1, C::R2, 0, SIGN, NAMED, (C::R3 > 1) || TAIL_SYNC>(v, buf, tw, t, active, li);
+    if (active) dft<C::R1, SIGN, PAIRED>(v);
+    stockham_pass<C, C::R1, 1, C::R2, 0, SIGN, NAMED, (C::R3 > 1) || TAIL_SYNC, PAIRED>(v, buf, tw, t, active, li);
     if constexpr (C::R3 > 1)
-        stockham_pass<C, C::R2, C::R1, C::R3, TP::P2, SIGN, NAMED, (C::R4 > 1) || TAIL_SYNC>(v, buf, tw, t, active, li);
+        stockham_pass<C, C::R2, C::R1, C::R3, TP::P2, SIGN, NAMED, (C::R4 > 1) || TAIL_SYNC, PAIRED>(v, buf, tw, t,
+                                                                                                    active, li);
     if constexpr (C::R4 > 1)
-        stockham_pass<C, C::R3, C::R1 * C::R2, C::R4, TP::P2 + TP::P3, SIGN, NAMED, TAIL_SYNC>(v, buf, tw, t, active,
-                                                                                             li);
+        stockham_pass<C, C::R3, C::R1 * C::R2, C::R4, TP::P2 + TP::P3, SIGN, NAMED, TAIL_SYNC, PAIRED>(v, buf, tw, t,
+                                                                                                     active, li);
 }
 
 template <class C>

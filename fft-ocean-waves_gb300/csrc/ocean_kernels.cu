@@ -410,7 +410,7 @@ __device__ __forceinline__ void row_pass_body(const RowArgs& a)
 #pragma unroll
             for (int r = 0; r < L::E; ++r) v[r] = buf[t + r * L::G];
             line_sync<L, true>(li);                        // the line's inputs are in registers
-            line_fft<L, +1>(v, buf, tw_s, t, li);
+            line_fft<L, +1, true, true, true>(v, buf, tw_s, t, li);   // paired butterfly adds: faster here
             if (active) {
                 // column-pair blocked: x and x+1 of a row are adjacent.  pos(t, e)
                 // is t plus an even constant, so the parity is t's.
@@ -777,7 +777,8 @@ __global__ void __launch_bounds__(ColCfg<N>::THREADS) k_col_fft(const __grid_con
     }
     if (!block_wait(&bar_tw, 0, &wait_ok, a.status)) return;   // also: the tile is consumed
     pdl_launch_dependents();                                 // k_col_out may start its set-up
-    line_fft<L, +1, true, false>(v, work + li * L::NPAD, tw_s, t, li);   // no final barrier: work is not reused
+    // no final barrier (work is not reused); paired butterfly adds: faster here
+    line_fft<L, +1, true, false, true>(v, work + li * L::NPAD, tw_s, t, li);
 
     // output y = pos(t, e) is t plus an even constant: the (-1)^(x+y) sign is
     // the thread's, and the two columns' signs are opposite.  Dy is scaled by
