@@ -133,7 +133,7 @@ def tune_batch(torch, og, workloads, reps, log, budgets=(32, 48, 64, 96)):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--out", default=os.path.join(os.path.dirname(HERE), "gpurun_out"))
+    ap.add_argument("--out", default="tuning_out")
     ap.add_argument("--sizes", default=",".join(str(n) for n in SIZES))
     ap.add_argument("--reps", type=int, default=5)
     ap.add_argument("--no-batch", action="store_true")
