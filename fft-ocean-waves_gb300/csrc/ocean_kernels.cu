@@ -1081,12 +1081,10 @@ __global__ void __launch_bounds__(FusedCfg<N, P>::THREADS, P == 2 ? 2 : 1) k_col
     }
     __syncthreads();
 
-    // Epilogue: texel (x0 + c - 1, y), c = tid % 2P + 1, y = tid / 2P + EROWS * k.
-    const int    c     = tid % (2 * P) + 1;                  // staged column of the texel
-    const int    r0    = tid / (2 * P);
     const float* EX    = E;                                  // Dx columns
     const float* EY    = E + (size_t)FC::COLS * FC::CP;      // Dy
     const float* EZ    = E + (size_t)2 * FC::COLS * FC::CP;  // Dz
+    const int    c     = tid % (2 * P) + 1;                  // staged column of the texel
     const int    cm    = (c - 1) * FC::CP, c0 = c * FC::CP, cp = (c + 1) * FC::CP;
     float* const  odx  = cu->dx;
     float* const  ody  = cu->dy;
@@ -1094,26 +1092,69 @@ __global__ void __launch_bounds__(FusedCfg<N, P>::THREADS, P == 2 ? 2 : 1) k_col
     float4* const onj  = cu->nj;
     const float   inv2d = cu->inv2d;
     const int     x    = x0 + c - 1;
+    if constexpr (P == 4) {
+        // Epilogue, 4 pairs: thread (c, q), q = tid / 2P, walks its block of
+        // rows [q*N/EBLK, (q+1)*N/EBLK) top to bottom with the 3 x 3
+        // neighbourhood in registers: each row loads 9 staged values (row y+1
+        // of Dy's three columns, of Dx's and Dz's own column, row y of their
+        // side columns) instead of 19.  A warp covers 2P columns of 32/(2P)
+        // row blocks, so its stores are 32/(2P) row pieces, as below.  (With
+        // 2 pairs the independent rows below measured faster.)
+        constexpr int EBLK = FC::THREADS / (2 * P);
+        const int q  = tid / (2 * P);
+        const int ya = q * N / EBLK, yb = (q + 1) * N / EBLK;
+        // rows y-1 and y of the window (taps z0..z7, normal_map_cs.glsl:37-44)
+        const int ym = (ya - 1) & (N - 1);
+        float a0 = EY[cm + ym], a1 = EY[c0 + ym], a2 = EY[cp + ym];   // Dy, row y-1
+        float b0 = EY[cm + ya], b1 = EY[c0 + ya], b2 = EY[cp + ya];   // Dy, row y
+        float xu = EX[c0 + ym], xc = EX[c0 + ya];                      // Dx column, rows y-1, y
+        float zu = EZ[c0 + ym], zc = EZ[c0 + ya];                      // Dz column, rows y-1, y
+        for (int y = ya; y < yb; ++y) {
+            const int   yq = (y + 1) & (N - 1);
+            const float d0 = EY[cm + yq], d1 = EY[c0 + yq], d2 = EY[cp + yq];   // Dy, row y+1
+            const float xd = EX[c0 + yq], zd = EZ[c0 + yq];
+            const float nz = a0 + 2.0f * a1 + a2 - d0 - 2.0f * d1 - d2;
+            const float nx = a0 + 2.0f * b0 + d0 - a2 - 2.0f * b2 - d2;
+            const float rn = rsqrtf(nx * nx + 1.0f + nz * nz);
+            const float dxx = (EX[cp + y] - EX[cm + y]) * inv2d;
+            const float dxz = (xd - xu) * inv2d;
+            const float dzx = (EZ[cp + y] - EZ[cm + y]) * inv2d;
+            const float dzz = (zd - zu) * inv2d;
+            const float dJ  = (dxx * dzz - dxz * dzx) - dxx - dzz;
+            const size_t o  = (size_t)y * N + x;
+            __stcs(odx + o, xc);
+            __stcs(ody + o, b1);
+            __stcs(odz + o, zc);
+            __stcs(onj + o, make_float4(nx * rn, rn, nz * rn, 1.0f + dJ));
+            a0 = b0; a1 = b1; a2 = b2;
+            b0 = d0; b1 = d1; b2 = d2;
+            xu = xc; xc = xd;
+            zu = zc; zc = zd;
+        }
+    } else {
+        // Epilogue: texel (x0 + c - 1, y), y = tid / 2P + EROWS * k.
+        const int r0 = tid / (2 * P);
 #pragma unroll 2
-    for (int y = r0; y < N; y += FC::EROWS) {
-        const int ym = (y - 1) & (N - 1), yq = (y + 1) & (N - 1);
-        // taps z0..z7 (normal_map_cs.glsl:37-44) around (x, y)
-        const float z0 = EY[cm + ym], z1 = EY[c0 + ym], z2 = EY[cp + ym];
-        const float z3 = EY[cm + y], z4 = EY[cp + y];
-        const float z5 = EY[cm + yq], z6 = EY[c0 + yq], z7 = EY[cp + yq];
-        const float nz = z0 + 2.0f * z1 + z2 - z5 - 2.0f * z6 - z7;
-        const float nx = z0 + 2.0f * z3 + z5 - z2 - 2.0f * z4 - z7;
-        const float rn = rsqrtf(nx * nx + 1.0f + nz * nz);
-        const float dxx = (EX[cp + y] - EX[cm + y]) * inv2d;
-        const float dxz = (EX[c0 + yq] - EX[c0 + ym]) * inv2d;
-        const float dzx = (EZ[cp + y] - EZ[cm + y]) * inv2d;
-        const float dzz = (EZ[c0 + yq] - EZ[c0 + ym]) * inv2d;
-        const float dJ  = (dxx * dzz - dxz * dzx) - dxx - dzz;
-        const size_t o  = (size_t)y * N + x;
-        __stcs(odx + o, EX[c0 + y]);
-        __stcs(ody + o, EY[c0 + y]);
-        __stcs(odz + o, EZ[c0 + y]);
-        __stcs(onj + o, make_float4(nx * rn, rn, nz * rn, 1.0f + dJ));
+        for (int y = r0; y < N; y += FC::EROWS) {
+            const int ym = (y - 1) & (N - 1), yq = (y + 1) & (N - 1);
+            // taps z0..z7 (normal_map_cs.glsl:37-44) around (x, y)
+            const float z0 = EY[cm + ym], z1 = EY[c0 + ym], z2 = EY[cp + ym];
+            const float z3 = EY[cm + y], z4 = EY[cp + y];
+            const float z5 = EY[cm + yq], z6 = EY[c0 + yq], z7 = EY[cp + yq];
+            const float nz = z0 + 2.0f * z1 + z2 - z5 - 2.0f * z6 - z7;
+            const float nx = z0 + 2.0f * z3 + z5 - z2 - 2.0f * z4 - z7;
+            const float rn = rsqrtf(nx * nx + 1.0f + nz * nz);
+            const float dxx = (EX[cp + y] - EX[cm + y]) * inv2d;
+            const float dxz = (EX[c0 + yq] - EX[c0 + ym]) * inv2d;
+            const float dzx = (EZ[cp + y] - EZ[cm + y]) * inv2d;
+            const float dzz = (EZ[c0 + yq] - EZ[c0 + ym]) * inv2d;
+            const float dJ  = (dxx * dzz - dxz * dzx) - dxx - dzz;
+            const size_t o  = (size_t)y * N + x;
+            __stcs(odx + o, EX[c0 + y]);
+            __stcs(ody + o, EY[c0 + y]);
+            __stcs(odz + o, EZ[c0 + y]);
+            __stcs(onj + o, make_float4(nx * rn, rn, nz * rn, 1.0f + dJ));
+        }
     }
 }
 

@@ -254,18 +254,26 @@ def test_col_fused_loads_staging_and_stores(N, P):
             for cc in range(COLS):
                 used[(f * COLS + cc) * CP:(f * COLS + cc) * CP + N] = True
         assert np.all(stage[used] == 1) and np.all(stage[~used] == 0)
-        # epilogue: every thread, texel (x0 + c - 1, y), reads columns c-1..c+1, rows y-1..y+1
+        # epilogue, texel (x0 + c - 1, y) reading columns c-1..c+1, rows y-1..y+1.  4 pairs: thread
+        # (c, q) walks rows [q*N/EBLK, (q+1)*N/EBLK) of staged column c; 2 pairs: thread tid
+        # takes rows tid/2P + EROWS*k
         tid = np.arange(32 * LINES)
         c = tid % (2 * P) + 1
-        for y0 in range(0, N, EROWS):
-            y = tid // (2 * P) + y0
-            keep = y < N
-            y, c = y[keep], (tid % (2 * P) + 1)[keep]
+        if P == 4:
+            EBLK = 32 * LINES // (2 * P)
+            q = tid // (2 * P)
+            ya, yb = q * N // EBLK, (q + 1) * N // EBLK
+            assert ya.min() == 0 and yb.max() == N and np.all(yb > ya)
+            steps = [(ya + k, ya + k < yb) for k in range((yb - ya).max())]
+        else:
+            steps = [(tid // (2 * P) + y0, tid // (2 * P) + y0 < N) for y0 in range(0, N, EROWS)]
+        for y, keep in steps:
+            y, cc = y[keep], c[keep]
             for dc in (-1, 0, 1):
                 for dy in (-1, 0, 1):
-                    rd = (c + dc) * CP + ((y + dy) & (N - 1))
+                    rd = (cc + dc) * CP + ((y + dy) & (N - 1))
                     assert rd.min() >= 0 and rd.max() < COLS * CP and np.all(used[rd])
-            np.add.at(out_hits, y * N + x0 + c - 1, 1)
+            np.add.at(out_hits, y * N + x0 + cc - 1, 1)
     assert np.all(out_hits == 1)
 
 
