@@ -163,6 +163,8 @@ struct ocean_s {
     int          adj_frames = 0;
     double*      sums   = nullptr;  // adjoint parameter sums (4 doubles)
     bool         spec_dirty = true; // the combined spectrum was rebuilt since the last row pass was launched
+    bool         rows_pending = false; // a row pass was launched and no column stage since (it writes the
+                                       // intermediate that the next row pass would overwrite)
     double       K      = 0.0;      // sqrt(g/(2*pi*L))
     double       w_dc   = 0.0;      // sqrt(g*1e-5): the floored DC frequency
 
@@ -443,13 +445,14 @@ int ocean_update_rows(ocean_t* o, double t, void* stream)
     // the row pass overlaps the stream's previous kernel unless that may be
     // the spectrum rebuild (ocean_set_h0 is stream-ordered) or the tuning
     // says otherwise for this N
-    ra.wait_first = (o->spec_dirty || !ocean::tuning_for(o->N).row_overlap) ? 1 : 0;
+    ra.wait_first = (o->spec_dirty || o->rows_pending || !ocean::tuning_for(o->N).row_overlap) ? 1 : 0;
     // NVTX ranges name the stages as the reference's GL debug groups do (main.cpp:623,644,665,689)
     nvtxRangePushA("ocean rows: evolution + horizontal FFT");
     cudaError_t e = ocean::launch_row_pass(o->N, ra, static_cast<cudaStream_t>(stream));
     nvtxRangePop();
     if (e != cudaSuccess) return cuda_fail(e, "row pass launch");
-    o->spec_dirty = false;
+    o->spec_dirty   = false;
+    o->rows_pending = true;
     return OCEAN_OK;
 }
 
@@ -494,6 +497,7 @@ int ocean_update_columns(ocean_t* o, void* stream)
     cudaError_t e = ocean::launch_col_fft(o->N, 1, col_args(o, none), static_cast<cudaStream_t>(stream), true);
     nvtxRangePop();
     if (e != cudaSuccess) return cuda_fail(e, "column transform launch");
+    o->rows_pending = false;   // it lets a following kernel start only once its tile is read
     return OCEAN_OK;
 }
 
@@ -523,6 +527,7 @@ int ocean_update_columns_outputs(ocean_t* o, const ocean_outputs* out, void* str
             ocean::launch_col_fused(o->N, pairs, 1, col_args(o, res), static_cast<cudaStream_t>(stream), true);
         nvtxRangePop();
         if (e != cudaSuccess) return cuda_fail(e, "fused column launch");
+        o->rows_pending = false;   // it lets a following kernel start only once its loads are in
         return OCEAN_OK;
     }
     if ((rc = ocean_update_columns(o, stream)) != OCEAN_OK) return rc;

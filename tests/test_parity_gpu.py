@@ -130,6 +130,32 @@ def test_matches_reference_shader_golden(torch_cuda, ocean_lib, name):
         assert rel_l2(o["nj"][..., :3], z[f"normal_{i}"][..., :3]) < 1e-5
 
 
+@pytest.mark.parametrize("N", [512, 1024])
+def test_repeated_row_pass_is_stream_ordered(torch_cuda, ocean_lib, N):
+    """Two row passes on one handle with no column stage between them (the
+    second would overwrite the intermediate while the first still writes it
+    if it overlapped): the column stage then sees the second time's frame, bit
+    for bit, also right after a back-to-back frame."""
+    torch = torch_cuda
+    d = P.c2(N)
+    dev = torch.device("cuda")
+    with ocean_lib.Ocean(P.lib_params(d), seed=d["seed"]) as oc:
+        outs = lambda: [torch.empty((N, N), device=dev) for _ in range(3)] + [torch.empty((N, N, 4), device=dev)]
+        ref = outs()
+        oc.update(9.25, *ref)
+        torch.cuda.synchronize()
+        got = outs()
+        scratch = outs()
+        oc.update(0.5, *scratch)                 # a frame in flight before the two row passes
+        oc.update_rows(3.0)
+        oc.update_rows(9.25)
+        oc.update_columns_outputs(*got)
+        torch.cuda.synchronize()
+        oc.device_status()
+        for a, b in zip(got, ref):
+            assert torch.equal(a, b)
+
+
 @pytest.mark.parametrize("N", [64, 512, 1024, 2048])
 def test_back_to_back_frames_bitwise(torch_cuda, ocean_lib, N):
     """Frames launched back to back with no host synchronisation (the stages
