@@ -302,3 +302,23 @@ def test_row_spectrum_prefetch(N, P, per_sm, threads, loop):
                 i += E * (threads >> 1)
     assert all(v == 1 for v in seen.values())
     assert len(seen) == (2 * (items - E) if E > 0 else 0)       # no free SMs: no prefetch
+
+
+@pytest.mark.parametrize("per_sm,expect_all_early", [(2, False), (3, True)])
+def test_row_ws_second_jobs_go_to_early_ctas(per_sm, expect_all_early):
+    """k_row_ws at N=1024 beside the 4-pair fused kernel: CTA b takes items b,
+    b + grid, ...  The CTAs that start early are the first E = (152 - 128) *
+    per_sm (the SMs the fused kernel leaves free).  At three CTAs per SM
+    (row_variant 5) every CTA with a second job is an early one, so every
+    late CTA has one job; at two (row_variant 3) most second jobs land on late
+    CTAs."""
+    N, sms, fused_ctas = 1024, 152, 1024 // 8
+    items = N // 2 + 1
+    grid = min(sms * per_sm, items)
+    E = (sms - fused_ctas) * per_sm
+    jobs = np.zeros(grid, np.int64)
+    for item in range(items):
+        jobs[item % grid] += 1
+    assert jobs.sum() == items and jobs.max() <= 2
+    two = np.nonzero(jobs == 2)[0]
+    assert (two.size == 0 or two.max() < E) == expect_all_early
